@@ -1,0 +1,381 @@
+#!/usr/bin/env python
+"""Rotations/s of the exhaustive FFT correlation scan at 128^3 on GB300.
+
+Workload (default ``shape_ace128``): one seeded synthetic pair, receptor 4000
+and ligand 1500 heavy atoms, 128^3 grid at 1.2 A, shape + 18 desolvation
+terms (18 folded correlation terms), 9000 uniform rotations scanned in
+batches of 64, 4 peaks kept per rotation.  One step = one scan of the whole
+rotation set.
+
+Arms
+* default: the GPU scan.  ``value`` is device-resident throughput (rotations
+  and peaks in HBM, CUDA events on the launching stream); ``e2e`` goes through
+  the C ABI with host buffers (``fftdock_scan``: H2D of the rotations, D2H of
+  the peaks inside the timed region).
+* ``--impl reference``: the reference's CPU path restated by the FP64 oracle
+  (one forward + one inverse 3-D FFT per term per rotation, real-space term
+  sum, full-grid selection) on all host threads, on a bounded sample of the
+  same workload.
+
+Multi-GPU: rotations are independent, every rank scans its own full rotation
+set (weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "rotations/s at 128^3 (1 GB300), exhaustive FFT scan"
+UNIT = "rotations/s"
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="shape_ace128")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def workload(name):
+    from proddl2_gb300 import synth
+    w = dict(synth.WORKLOADS[name])
+    w["name"] = name
+    return w
+
+
+def workload_desc(w):
+    terms = "shape + 18 desolvation types (18 folded terms)" if w["term_set"] == "shape_ace" else "shape (1 term)"
+    return ("%s: receptor %d / ligand %d atoms, %d^3 at %.1f A, %s, %d rotations, %d per batch, %d peaks/rotation"
+            % (w["name"], w["n_rec"], w["n_lig"], w["grid_n"], w["grid_step"], terms, w["n_rot"], w["rot_batch"],
+               w["peaks"]))
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def reference_schedule_bytes(n, k, batch):
+    """Algorithmic HBM bytes per rotation of the reference FFT schedule:
+    each 3-D transform is a plane pass and a line pass over the half spectrum
+    M = N^2 (N/2+1) complex; the ligand plane pass writes K M, the line pass
+    reads it plus the receptor (shared by `batch` rotations) and writes the
+    summed spectrum, the inverse plane pass reads it:
+    (2K + 2) M 8 + K M 8 / batch."""
+    m = n * n * (n // 2 + 1)
+    return (2 * k + 2) * m * 8 + k * m * 8 / batch
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic(name):
+    """DRAM bytes per pencil-kernel launch recorded from an ncu capture in
+    profiles/ (a line 'dram_bytes_per_launch: <int>'), or None."""
+    path = os.path.join(ROOT, "profiles", "pencil_%s.md" % name)
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU reference path (the FP64 oracle, reference schedule)
+# ---------------------------------------------------------------------------
+class CpuReference:
+    def __init__(self, w, pair, threads):
+        from oracle import fftdock_oracle as O
+        self.O = O
+        self.w = w
+        self.pair = pair
+        self.threads = threads
+        self.geom = O.Geometry.centred(w["grid_step"], w["grid_n"])
+        ts = O.TERMS_SHAPE_ACE if w["term_set"] == "shape_ace" else O.TERMS_SHAPE
+        tp = O.TermParams(term_set=ts, ace_matrix=pair.ace)
+        # the reference runs one FFTCorrelator per term: shape + each type
+        self.rg = O.receptor_terms(self.geom, pair.receptor.xyz, pair.receptor.ace_type, tp, folded=False)
+        self.rs = O.receptor_spectra(self.rg, workers=threads)
+        self.wts = O.ligand_term_weights(pair.ligand.ace_type, tp, folded=False)
+        self.k = w["peaks"]
+
+    def rotations(self, idx):
+        for i in idx:
+            self.O.scan_rotation(self.geom, self.rg, self.rs, self.pair.ligand.xyz, self.wts,
+                                 self.pair.rotations[i % len(self.pair.rotations)], self.k, workers=self.threads)
+
+    def rate(self, target_s=15.0, max_rot=64):
+        t0 = time.perf_counter()
+        self.rotations([0])
+        one = time.perf_counter() - t0
+        n = max(2, min(max_rot, int(target_s / max(one, 1e-3))))
+        t0 = time.perf_counter()
+        self.rotations(range(1, n + 1))
+        dt = time.perf_counter() - t0
+        return n / dt, n, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from proddl2_gb300 import synth
+    w = workload(args.workload)
+    threads = os.cpu_count() or 1
+    pair = synth.make_pair(w["n_rec"], w["n_lig"], w["n_rot"], seed=1)
+    ref = CpuReference(w, pair, threads)
+    t0 = time.perf_counter()
+    ref.rotations([0])
+    one = time.perf_counter() - t0
+    per_step = max(1, int(3.0 / max(one, 1e-3)))
+    nxt = 1
+    for _ in range(args.warmup):
+        ref.rotations(range(nxt, nxt + per_step))
+        nxt += per_step
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ref.rotations(range(nxt, nxt + per_step))
+        nxt += per_step
+    dt = time.perf_counter() - t0
+    value = per_step * args.steps / dt
+    sample = ("%d rotations per step of the %s workload, FP64 oracle, %d FFT terms (reference schedule: "
+              "forward + inverse 3-D FFT per term per rotation), scipy pocketfft on %d threads"
+              % (per_step, w["name"], ref.rg.shape[0], threads))
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded globules, uniform quaternion rotations)",
+        "config": {"workload": workload_desc(w), "mode": "exhaustive", "sample_rotations_per_step": per_step},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    from proddl2_gb300 import FFTScan, ScanConfig, synth, _lib
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = workload(args.workload)
+    pair = synth.make_pair(w["n_rec"], w["n_lig"], w["n_rot"], seed=1)
+    n_rot = w["n_rot"]
+    cfg = ScanConfig(grid_n=w["grid_n"], grid_step=w["grid_step"], term_set=w["term_set"], peaks_per_rot=w["peaks"],
+                     rot_batch=w["rot_batch"], ace_matrix=pair.ace, device=local)
+    scan = FFTScan(cfg)
+    t0 = time.perf_counter()
+    scan.set_receptor(pair.receptor.xyz, pair.receptor.ace_type)
+    receptor_ms = 1000.0 * (time.perf_counter() - t0)
+    scan.set_ligand(pair.ligand.xyz, pair.ligand.ace_type)
+
+    rot_host = np.ascontiguousarray(pair.rotations.reshape(n_rot, 9))
+    d_rot = torch.from_numpy(rot_host).to(dev)
+    peak_bytes = _lib.peak_dtype().itemsize
+    d_peaks = torch.zeros(n_rot * w["peaks"] * peak_bytes, dtype=torch.uint8, device=dev)
+    d_np = torch.zeros(n_rot, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        scan.scan_device(d_rot.data_ptr(), n_rot, d_peaks.data_ptr(), d_np.data_ptr(), stream_ptr=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+
+    gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[local if world > 1 else 0]) \
+        if os.environ.get("CUDA_VISIBLE_DEVICES", "").replace(",", "").isdigit() else local
+    sampler = ClockSampler(gpu_index)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    sampler.start()
+    scan.profile(True)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        dist.barrier()
+    clocks = sampler.stop()
+    ms_total = ev0.elapsed_time(ev1)
+    kstats = scan.kernel_stats()
+    scan.profile(False)
+    t = torch.tensor([ms_total], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_total = float(t.item())
+    ms_per_step = ms_total / args.steps
+    value = n_rot * world / (ms_per_step / 1000.0)
+
+    # end to end through the C ABI with host buffers
+    for _ in range(max(1, args.warmup)):
+        scan.scan(rot_host)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res = scan.scan(rot_host)
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_s = float(te.item())
+    e2e_value = n_rot * world * args.steps / e2e_s
+    h2d = rot_host.nbytes
+    d2h = res.peaks.nbytes + res.n_peaks.nbytes + 4 * n_rot
+
+    # roofline of the dominant kernel (pencil): algorithmic bytes of the
+    # reference schedule for the rotations one launch processes
+    launches, pencil_ms = kstats["pencil"]
+    k_terms = scan.n_terms
+    batch = w["rot_batch"]
+    rot_per_launch = n_rot * args.steps / max(launches, 1)
+    bytes_per_launch = reference_schedule_bytes(w["grid_n"], k_terms, batch) * rot_per_launch
+    avg_launch_ms = pencil_ms / max(launches, 1)
+    achieved_gbs = bytes_per_launch / (avg_launch_ms / 1000.0) / 1e9
+    peak_gbs, peak_kind = load_peaks()
+    traffic = committed_traffic(w["name"])
+    gpu_launches = sum(v[0] for v in kstats.values())
+
+    if rank != 0:
+        scan.close()
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        ref = CpuReference(w, pair, threads)
+        rate, n_s, dt = ref.rate(target_s=15.0)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "%d rotations of this workload in %.1f s, FP64 oracle, reference schedule (%d terms, "
+                         "forward + inverse 3-D FFT per term per rotation), scipy pocketfft on %d threads"
+                         % (n_s, dt, ref.rg.shape[0], threads)}
+
+    total_kernel_ms = sum(v[1] for v in kstats.values())
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (seeded globules, uniform quaternion rotations)",
+        "config": {"workload": workload_desc(w), "mode": "exhaustive",
+                   "parallelism": "replicas" if world == 1 else "rotation sets per rank (replicas)",
+                   "l2": "inputs larger than L2: 153 MB receptor spectra + 545 MB batch planes per step",
+                   "receptor_setup_ms": receptor_ms,
+                   "precision": "FP32 FFT/spectrum product, FP64 direct-space rescoring of 16 candidates"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": gpu_launches,
+        "kernels_ms_per_step": {k: v[1] / args.steps for k, v in kstats.items()},
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak_gbs, "unit": "GB/s",
+                     "frac": achieved_gbs / peak_gbs, "traffic": traffic,
+                     "kernel": "pencil", "peak_source": peak_kind,
+                     "bytes_basis": "reference FFT schedule, (2K+2)*M*8 + K*M*8/64 per rotation",
+                     "kernel_share": pencil_ms / total_kernel_ms if total_kernel_ms else None},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    print(json.dumps(out))
+    scan.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,177 @@
+/*
+ * fftdock.h -- C ABI of the GB300 FFT rotational/translational correlation
+ * scan (libfftdock.so).
+ *
+ * This library replaces the in-process C++ template API of the PRODDL2
+ * `rot-scan` worker for one ligand/receptor pair:
+ *   MolForce::{projectMol, collectTotal, nGrids}
+ *       include/PRODDL/docking_molforce.hpp:38-104
+ *   FFTCorrelators::{preprocessReceptor, correlate}
+ *       include/PRODDL/docking_fft.hpp:767-883
+ *   CorrelationProcessor::{init, selectFromFFT, getTranValuesFilled}
+ *       include/PRODDL/docking_fft.hpp:283-447
+ * as orchestrated by Worker::{init, prepareReceptor, scanRotation, run}
+ *       include/PRODDL/docking_app.hpp:326-513.
+ *
+ * Ownership: the caller owns every host buffer passed in; the library copies
+ * what it needs before returning.  The context owns all device memory.
+ * Threading: one context per host thread; calls on one context are not
+ * re-entrant, separate contexts are independent.  Everything runs on one GPU;
+ * there is no CPU fallback: on a machine without a usable GPU every call that
+ * needs one returns FFTDOCK_ECUDA.
+ * Errors: every entry point returns an FFTDOCK_* status; the text of the last
+ * error is available from fftdock_last_error(ctx).  No C++ exception crosses
+ * this boundary.
+ */
+#ifndef FFTDOCK_H_
+#define FFTDOCK_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FFTDOCK_ABI_VERSION 1
+
+/* status codes; the reference signals the same conditions with C++
+ * exceptions caught at main (src/PRODDL/docking_main.cpp:143,155) or leaves
+ * them undefined (ligand atoms outside the grid, docking_molforce.hpp:360-364) */
+enum {
+    FFTDOCK_OK = 0,
+    FFTDOCK_EINVAL = 1,        /* bad argument or configuration */
+    FFTDOCK_EOUT_OF_GRID = 2,  /* a rotated ligand atom falls outside the grid */
+    FFTDOCK_ECUDA = 3,         /* CUDA error or no usable GPU */
+    FFTDOCK_ENOMEM = 4,        /* device or host allocation failed */
+    FFTDOCK_ESTATE = 5,        /* call order (scan before receptor/ligand) */
+    FFTDOCK_EUNSUPPORTED = 6,  /* grid size or option not built into this library */
+    FFTDOCK_EIO = 7            /* scan-record file I/O */
+};
+
+/* correlation term sets (the reference's "potentialName",
+ * docking_app.hpp:54-66, plus this library's shape/desolvation terms) */
+enum {
+    FFTDOCK_TERMS_SHAPE = 1,     /* surface +1 / core -15 receptor grid, unit ligand weights; K = 1 */
+    FFTDOCK_TERMS_SHAPE_ACE = 2  /* shape + n_types ACE-style desolvation grids, folded to K = n_types */
+};
+
+/* precision of the stored receptor spectra */
+enum {
+    FFTDOCK_PREC_FP32 = 0
+};
+
+typedef struct fftdock_config {
+    int32_t struct_size;         /* sizeof(fftdock_config) */
+    int32_t grid_n;              /* FFT grid edge N (cubic); see fftdock_supported_grid() */
+    double grid_step;            /* h in Angstrom ("gridStep") */
+    int32_t term_set;            /* FFTDOCK_TERMS_* ("potentialName") */
+    int32_t peaks_per_rot;       /* translations kept per rotation ("maxNTrans"), 1..16 */
+    int32_t max_trans_inp;       /* bound of the per-rotation queue ("maxNTransInp") */
+    double max_val_corr;         /* only scores strictly below this are kept ("maxValCorr") */
+    int32_t rot_batch;           /* rotations per device batch, 1..1024 */
+    int32_t precision;           /* FFTDOCK_PREC_* */
+    int32_t device;              /* CUDA device ordinal */
+    int32_t n_types;             /* desolvation atom types (FFTDOCK_TERMS_SHAPE_ACE) */
+    const double* ace_matrix;    /* n_types x n_types row-major; copied by fftdock_create */
+    double shape_core_radius;    /* core if a cell centre is within this of an atom (A) */
+    double shape_surface_width;  /* surface shell width beyond the core radius (A) */
+    double ace_b, ace_k, ace_a;  /* sigmoid 1/(1+exp(b(k r - a))) (potentials_inc.hpp:394-397) */
+    double ace_cut;              /* cutoff of the desolvation field (A) */
+} fftdock_config;
+
+/* one selected translation; the reference's TranValue
+ * (include/PRODDL/types.hpp:68-84) plus the rotation id and the raw
+ * correlation cell. */
+typedef struct fftdock_peak {
+    int32_t rot_id;   /* first_rot_id + index of the rotation in the call */
+    int32_t cell[3];  /* correlation offset s (FFT output index, [0, N)^3) */
+    double t[3];      /* translation h * unwrap(s) (docking_fft.hpp:368-389) */
+    double score;     /* correlation energy, FP64 direct-space rescored; lower is better */
+} fftdock_peak;
+
+typedef struct fftdock_ctx fftdock_ctx;
+
+/* Fill *cfg with defaults: N 128, h 1.2, shape+ACE with 18 types (matrix
+ * must still be supplied), 4 peaks, queue 10000, maxValCorr +inf, batch 64. */
+void fftdock_config_init(fftdock_config* cfg);
+
+/* Grid sizes compiled into this library (1 if supported). */
+int fftdock_supported_grid(int32_t n);
+
+/* FFTW_Size::findBestSize (include/PRODDL/Math/fft.hpp:141-151): smallest
+ * size >= start_n over primes {2,3,5,7,11,13} with e11 + e13 <= 1. */
+int fftdock_find_best_size(int32_t start_n, int32_t* result);
+
+/* Create a context (Worker::init, docking_app.hpp:326-404, minus rotation
+ * file loading): validates the configuration and allocates device memory. */
+int fftdock_create(const fftdock_config* cfg, fftdock_ctx** out);
+void fftdock_destroy(fftdock_ctx* ctx);
+const char* fftdock_last_error(const fftdock_ctx* ctx);
+
+/* Receptor atoms in the grid frame (grid centred on the origin).  Builds the
+ * K receptor term grids and keeps their spectra on the device
+ * (Worker::prepareReceptor, docking_app.hpp:406-415, and
+ * FFTCorrelator::preprocessReceptor, docking_fft.hpp:614-618). */
+int fftdock_set_receptor(fftdock_ctx* ctx, int32_t n, const double* xyz, const int32_t* type);
+
+/* Ligand atoms in the ligand frame (rotations are applied about the origin,
+ * docking_app.hpp:454-456).  type[i] in [0, n_types) for shape+ACE. */
+int fftdock_set_ligand(fftdock_ctx* ctx, int32_t n, const double* xyz, const int32_t* type);
+
+/* Scan n_rot rotations (row-major 3x3 doubles, host memory).  For rotation i,
+ * peaks[i*peaks_per_rot + j] for j < n_peaks[i] hold the selected
+ * translations in ascending score order (Worker::scanRotation,
+ * docking_app.hpp:450-466).  Returns FFTDOCK_EOUT_OF_GRID if any rotated
+ * ligand atom leaves the grid; those rotations report n_peaks = 0. */
+int fftdock_scan(fftdock_ctx* ctx, int32_t n_rot, const double* rot, int32_t first_rot_id,
+                 fftdock_peak* peaks, int32_t* n_peaks);
+
+/* Same with device pointers on the given CUDA stream (NULL = the context's
+ * stream); the call returns after queueing the work and does not report
+ * out-of-grid rotations (their n_peaks is 0). */
+int fftdock_scan_device(fftdock_ctx* ctx, int32_t n_rot, const double* d_rot, int32_t first_rot_id,
+                        fftdock_peak* d_peaks, int32_t* d_n_peaks, void* stream);
+
+/* Introspection. */
+int fftdock_grid_n(const fftdock_ctx* ctx);
+int fftdock_n_terms(const fftdock_ctx* ctx);
+
+/* Copy receptor term grid `term` (real space, FP64, N^3 C order) to host. */
+int fftdock_get_receptor_grid(fftdock_ctx* ctx, int32_t term, double* out);
+
+/* Diagnostic: the FP32 correlation grid sum_t corr(R_t, L_t) for one
+ * rotation (N^3 floats, C order), as produced before selection. */
+int fftdock_correlation_grid(fftdock_ctx* ctx, const double* rot, float* out);
+
+/* Diagnostic: per-rotation FP32 candidate pool (16 smallest values and their
+ * flat offsets, ascending) before FP64 rescoring. */
+int fftdock_scan_candidates(fftdock_ctx* ctx, int32_t n_rot, const double* rot,
+                            float* values, int32_t* offsets);
+
+/* Per-kernel device time of the scan, from CUDA events recorded on the
+ * launching stream around each kernel of every batch while profiling is on.
+ * Kernels: 0 ligand rotate/bin/sort, 1 pencil (forward x transform, spectrum
+ * product over terms, inverse x transform), 2 plane (inverse y, real z,
+ * top-k), 3 finalize (merge, FP64 rescoring, translations). */
+typedef struct fftdock_kernel_stats {
+    int64_t launches[4];
+    double total_ms[4];
+} fftdock_kernel_stats;
+
+/* Start (enable != 0) or stop recording kernel events; starting clears the record. */
+int fftdock_profile(fftdock_ctx* ctx, int32_t enable);
+
+/* Synchronise the context's work and sum the recorded kernel times. */
+int fftdock_get_kernel_stats(fftdock_ctx* ctx, fftdock_kernel_stats* out);
+
+/* Append one RotFftScanIO_Bin record per rotation to `path`
+ * (include/PRODDL/docking_io_bin.hpp:55-71): [int32 2014011401][3x3 double
+ * rotation][size_t n][n x {double t[3], double value}]. */
+int fftdock_write_scan_records(const char* path, int32_t n_rot, const double* rot, int32_t peaks_per_rot,
+                               const fftdock_peak* peaks, const int32_t* n_peaks, int32_t append);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FFTDOCK_H_ */

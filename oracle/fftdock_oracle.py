@@ -1,0 +1,530 @@
+"""CPU FP64 oracle for the PRODDL2 FFT rotational/translational correlation scan.
+
+TEST INFRASTRUCTURE ONLY.  This module is the checker: the parity tests, the
+smoke check and the CPU-baseline leg of ``bench.py`` import it.  The product
+path (``proddl2_gb300`` + ``libfftdock.so``) never imports or calls it.
+
+It restates, in numpy float64, the reference's ``rot-scan`` worker path
+(``include/PRODDL/docking_app.hpp:450-466`` ``Worker::scanRotation`` ->
+``findTranslationalMinima`` at ``:417-447``) with the reference's conventions:
+
+* centred grid geometry and the truncating ``toLogical`` used for ligand
+  binning (``include/PRODDL/Grid/gridcoord.hpp:127-191``,
+  ``include/PRODDL/Grid/grid.hpp:442-451``);
+* receptor radial-field projection on cell centres inside the cropped
+  ``toLogical(c +- cut)`` box, with ``r^2`` clamped to ``(h/4)^2``
+  (``include/PRODDL/Grid/project.hpp:51-176``,
+  ``include/PRODDL/docking_molforce.hpp:298-320``);
+* ligand point scatter ``grid(cell(p')) += w`` after ``p' = R p``
+  (``docking_molforce.hpp:351-368``, ``Geom/transformation.hpp:206-222``,
+  matrix-vector order of ``Blitz/bztinyvec.hpp:52-65``);
+* per-term correlation ``C = IFFT(conj(FFT R) * FFT L) / V`` summed over the
+  terms in real space (``docking_fft.hpp:622-633``, ``:812-819``,
+  ``docking_molforce.hpp:249-269``);
+* selection of the ``k`` smallest values below ``maxValCorr`` in ascending
+  order (``docking_fft.hpp:316-345,452-468``, ``Common/queue.hpp:221-251``),
+  ties broken by the cell's flat offset;
+* offset -> translation through ``WrappedIndex::unwrap`` and ``toSpatialDiff``
+  (``docking_fft.hpp:368-389``, ``Math/fft.hpp:199-206``,
+  ``Grid/gridcoord.hpp:150``).
+
+Parity status.  The reference cannot be built or run here (FFTW3, Blitz++,
+Boost and HDF5 are absent) and ships no golden vectors for correlation scores,
+so score parity is *unpinned*: it rests on this restatement and on the
+independent exact direct-space scorer :func:`direct_score`.  The parts the
+reference's own unit tests do pin -- queue semantics
+(``src/PRODDL/Common/test_queue.cpp:21-99``), the FFT size rule
+(``src/PRODDL/Math/test_pfactors.cpp:73-132``), grid domain conventions
+(``src/PRODDL/Grid/test_grid.cpp:65-76``) and the scan record format
+(``src/PRODDL/IO/test_dock_io_bin.cpp:41-104``) -- are checked against those
+tests' vectors in ``tests/test_oracle_pins.py``.
+
+The shape (surface +1 / core -15) and 18-type ACE-style desolvation terms are
+not in the reference's FFT path; they are this project's plug-in terms built
+with the reference's radial-field projection mechanism, and this module is
+their definition: receptor grid ``S`` (set, not summed), ``D_t`` sums of the
+``PotAce`` sigmoid (``include/PRODDL/potentials_inc.hpp:357-406``, no cut
+shift), ligand grids of unit weights, total score
+``-corr(S, L) + sum_t corr(D_t, L_t)``, folded to ``sum_t corr(D_t - S, L_t)``.
+"""
+from __future__ import annotations
+
+import heapq
+import math
+import struct
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# ----------------------------------------------------------------------------
+# Term sets (mirrors the C ABI enum in include/fftdock.h)
+# ----------------------------------------------------------------------------
+TERMS_SHAPE = 1        # K = 1: -S correlated with all ligand atoms
+TERMS_SHAPE_ACE = 2    # K = n_types (folded): D_t - S correlated with type-t atoms
+
+SHAPE_SURFACE = 1.0
+SHAPE_CORE = -15.0
+
+
+# ----------------------------------------------------------------------------
+# FFT size rule: Math/pfactors.hpp:29-57, Math/fft.hpp:82-168, Math/fft.cc:8
+# ----------------------------------------------------------------------------
+FFTW_PRIMES = (2, 3, 5, 7, 11, 13)
+
+
+def find_first_prime_factoring(start_n, end_n, primes=FFTW_PRIMES):
+    """First N in [max(start_n, 2), end_n) that factors over ``primes``.
+
+    Returns ``(found, N, exponents)`` (``Math/pfactors.hpp:29-57``)."""
+    n0 = 2 if start_n <= 1 else start_n
+    for n_cand in range(n0, end_n):
+        rem = n_cand
+        exps = []
+        for p in primes:
+            e = 0
+            while rem % p == 0:
+                rem //= p
+                e += 1
+            exps.append(e)
+            if rem == 1:
+                exps += [0] * (len(primes) - len(exps))
+                return True, n_cand, exps
+    return False, None, None
+
+
+def find_best_size(start_n, end_n=2**31 - 1):
+    """``FFTW_Size::findBestSize`` (``Math/fft.hpp:82-115,141-151``): first size
+    >= start_n over {2,3,5,7,11,13} with exp(11) + exp(13) <= 1."""
+    while True:
+        ok, n, exps = find_first_prime_factoring(start_n, end_n)
+        if not ok:
+            return None
+        if exps[4] + exps[5] <= 1:
+            return n
+        start_n = n + 1
+
+
+# ----------------------------------------------------------------------------
+# BoundPriorityQueue: Common/queue.hpp:49-280
+# ----------------------------------------------------------------------------
+class _MaxItem:
+    """Heap entry ordered so that heapq's min-heap keeps the largest key on top."""
+    __slots__ = ("key", "seq", "item")
+
+    def __init__(self, key, seq, item):
+        self.key, self.seq, self.item = key, seq, item
+
+    def __lt__(self, other):
+        return other.key < self.key or (not self.key < other.key and self.seq > other.seq)
+
+
+class BoundPriorityQueue:
+    """Keeps at most ``size_limit`` smallest items whose key is < ``max_val``.
+
+    Same push/sort semantics as the reference (``queue.hpp:221-251,184-193``):
+    an item is dropped unless ``key(x) < max_val``; when full, it replaces the
+    current largest only if strictly smaller.  ``sort()`` returns ascending."""
+
+    def __init__(self, size_limit, max_val, key=lambda x: x):
+        if size_limit <= 0:
+            raise ValueError("size_limit must be > 0")
+        self.size_limit = size_limit
+        self.max_val = max_val
+        self.key = key
+        self._heap = []
+        self._seq = 0
+
+    def push(self, x):
+        k = self.key(x)
+        if not (k < self.max_val):
+            return
+        e = _MaxItem(k, self._seq, x)
+        self._seq += 1
+        if len(self._heap) >= self.size_limit:
+            if k < self._heap[0].key:
+                heapq.heapreplace(self._heap, e)
+            return
+        heapq.heappush(self._heap, e)
+
+    def top(self):
+        return self._heap[0].item
+
+    def pop(self):
+        heapq.heappop(self._heap)
+
+    def size(self):
+        return len(self._heap)
+
+    def clear(self):
+        self._heap = []
+
+    def sort(self):
+        return [e.item for e in sorted(self._heap, key=lambda e: (e.key, e.seq))]
+
+
+# ----------------------------------------------------------------------------
+# Grid geometry: Grid/gridcoord.hpp:127-191
+# ----------------------------------------------------------------------------
+@dataclass(frozen=True)
+class Geometry:
+    h: float
+    n: int
+    zero: float       # spatial coordinate of the grid's low corner
+    zero_h: float     # zero - h, used by toLogical
+    center0: float    # centre of cell 0
+
+    @staticmethod
+    def centred(h, n):
+        """``UniformCubicGeometry(step, logicalSize)`` (gridcoord.hpp:127-142)."""
+        h = float(h)
+        s_upper = h + h * float(n - 1)   # toSpatialRight(n-1) with zero 0
+        s_size = s_upper - 0.0
+        zero = (-1.0 * s_size) / 2.0
+        return Geometry(h=h, n=int(n), zero=zero, zero_h=zero - h, center0=zero + h / 2.0)
+
+    def to_logical(self, x):
+        """``toLogical``: int((x - (zero - h)) / h) - 1, C truncation toward 0."""
+        v = (np.asarray(x, dtype=np.float64) - self.zero_h) / self.h
+        return np.trunc(v).astype(np.int64) - 1
+
+    def to_spatial(self, i):
+        return self.center0 + self.h * np.asarray(i, dtype=np.float64)
+
+    def spatial_domain(self):
+        return self.zero, self.zero + self.h * self.n
+
+
+# ----------------------------------------------------------------------------
+# Rotations: Geom/euler.hpp:38-52, Geom/rotational_grid.hpp:25-64
+# ----------------------------------------------------------------------------
+def euler_to_matrix(angles):
+    """``Eu_xyz::eulerAngToRotMatr`` (euler.hpp:38-52), radians in."""
+    a, b, g = (float(v) for v in angles)
+    sa, ca, sb, cb, sg, cg = math.sin(a), math.cos(a), math.sin(b), math.cos(b), math.sin(g), math.cos(g)
+    return np.array([
+        [cg * ca, cg * sa, -sg],
+        [sb * sg * ca - cb * sa, sb * sg * sa + cb * ca, cg * sb],
+        [cb * sg * ca + sb * sa, cb * sg * sa - sb * ca, cg * cb],
+    ], dtype=np.float64)
+
+
+def load_rotational_grid(text):
+    """``loadRotationalGrid`` (rotational_grid.hpp:25-64): header count, then
+    Euler triples in degrees; a short final read is tolerated (the shipped
+    files' header counts are one more than their data rows)."""
+    lines = text.splitlines()
+    n = int(lines[0].split()[0])
+    pi = 4.0 * math.atan(1.0)
+    deg = pi / 180.0
+    rows = []
+    for ln in lines[1:]:
+        parts = ln.split()
+        if len(parts) >= 3:
+            rows.append([float(p) for p in parts[:3]])
+    mats = []
+    for i in range(n):
+        if i < len(rows):
+            ang = [v * deg for v in rows[i]]
+        else:
+            ang = [v * deg for v in rows[-1]]   # failed read leaves the last value
+        mats.append(euler_to_matrix(ang))
+    return np.stack(mats)
+
+
+def rotate_points(rot, xyz):
+    """p' = R p with the reference's accumulation order (bztinyvec.hpp:52-65):
+    y_i = ((0 + m_i0 x0) + m_i1 x1) + m_i2 x2, each product rounded."""
+    rot = np.asarray(rot, dtype=np.float64)
+    x = np.asarray(xyz, dtype=np.float64)
+    out = np.empty_like(x)
+    for i in range(3):
+        acc = rot[i, 0] * x[:, 0]
+        acc = acc + rot[i, 1] * x[:, 1]
+        acc = acc + rot[i, 2] * x[:, 2]
+        out[:, i] = acc
+    return out
+
+
+# ----------------------------------------------------------------------------
+# Receptor radial-field projection: Grid/project.hpp:51-176
+# ----------------------------------------------------------------------------
+def _projection_boxes(geom, center, cut):
+    lo = geom.to_logical(center - cut)
+    hi = geom.to_logical(center + cut)
+    lo = np.maximum(lo, 0)
+    hi = np.minimum(hi, geom.n - 1)
+    return lo, hi
+
+
+def _cells_in_box(geom, center, cut):
+    """Cells of the cropped toLogical box around ``center`` and their r^2
+    (project.hpp:87-98,150-152), r^2 summed x, y, z in that order."""
+    lo, hi = _projection_boxes(geom, center, cut)
+    if np.any(lo > hi):
+        return None
+    ix = np.arange(lo[0], hi[0] + 1)
+    iy = np.arange(lo[1], hi[1] + 1)
+    iz = np.arange(lo[2], hi[2] + 1)
+    dx = geom.to_spatial(ix) - center[0]
+    dy = geom.to_spatial(iy) - center[1]
+    dz = geom.to_spatial(iz) - center[2]
+    r2 = (dx[:, None, None] * dx[:, None, None] + dy[None, :, None] * dy[None, :, None]) \
+        + dz[None, None, :] * dz[None, None, :]
+    return (slice(lo[0], hi[0] + 1), slice(lo[1], hi[1] + 1), slice(lo[2], hi[2] + 1)), r2
+
+
+def shape_grid(geom, rec_xyz, r_core, width):
+    """Plug-in shape term: +1 on surface cells (centre within r_core+width of
+    an atom, not core), -15 on core cells (within r_core)."""
+    n = geom.n
+    flag = np.zeros((n, n, n), dtype=np.int8)
+    cut = float(r_core) + float(width)
+    rc2 = float(r_core) * float(r_core)
+    rs2 = cut * cut
+    for c in np.asarray(rec_xyz, dtype=np.float64):
+        got = _cells_in_box(geom, c, cut)
+        if got is None:
+            continue
+        sl, r2 = got
+        f = np.where(r2 <= rc2, 2, np.where(r2 <= rs2, 1, 0)).astype(np.int8)
+        np.maximum(flag[sl], f, out=flag[sl])
+    s = np.zeros((n, n, n), dtype=np.float64)
+    s[flag == 1] = SHAPE_SURFACE
+    s[flag == 2] = SHAPE_CORE
+    return s
+
+
+def ace_sigmoid(r2, b, k, a):
+    """``PotAce::f2`` with no cut shift (potentials_inc.hpp:394-397)."""
+    r = np.sqrt(r2)
+    return 1.0 / (1.0 + np.exp(b * (k * r - a)))
+
+
+def ace_type_density(geom, rec_xyz, rec_type, n_types, b, k, a, cut):
+    """G_tau(x) = sum over type-tau atoms of the sigmoid at the cell centre,
+    r^2 <= cut^2, r^2 clamped to (h/4)^2 (project.hpp:143-159,
+    docking_molforce.hpp:307-310)."""
+    n = geom.n
+    g = np.zeros((n_types, n, n, n), dtype=np.float64)
+    cut2 = float(cut) * float(cut)
+    min_d = geom.h / 4.0
+    min_d2 = min_d * min_d
+    for c, t in zip(np.asarray(rec_xyz, dtype=np.float64), np.asarray(rec_type)):
+        got = _cells_in_box(geom, c, cut)
+        if got is None:
+            continue
+        sl, r2 = got
+        inside = r2 <= cut2
+        r2c = np.where(r2 < min_d2, min_d2, r2)
+        val = np.where(inside, ace_sigmoid(r2c, b, k, a), 0.0)
+        g[int(t)][sl] += val
+    return g
+
+
+@dataclass
+class TermParams:
+    term_set: int = TERMS_SHAPE
+    shape_core_radius: float = 2.2
+    shape_surface_width: float = 1.8
+    n_types: int = 18
+    ace_matrix: np.ndarray | None = None
+    ace_b: float = 7.0
+    ace_k: float = 0.15
+    ace_a: float = 0.6
+    ace_cut: float = 6.0
+
+
+def receptor_terms(geom, rec_xyz, rec_type, tp: TermParams, folded=True):
+    """Receptor grids R_t (float64, K x N^3).
+
+    folded=True gives the K the GPU uses (shape: [-S]; shape+ACE:
+    [D_t - S for t]).  folded=False gives the reference-style term list with
+    one correlator per term ([-S] + [D_t]), paired with
+    :func:`ligand_term_weights` (folded=False)."""
+    s = shape_grid(geom, rec_xyz, tp.shape_core_radius, tp.shape_surface_width)
+    if tp.term_set == TERMS_SHAPE:
+        return (-s)[None]
+    if tp.term_set != TERMS_SHAPE_ACE:
+        raise ValueError("unknown term set")
+    e = np.asarray(tp.ace_matrix, dtype=np.float64)
+    g = ace_type_density(geom, rec_xyz, rec_type, tp.n_types, tp.ace_b, tp.ace_k, tp.ace_a, tp.ace_cut)
+    d = np.einsum("ut,uxyz->txyz", e, g)
+    if folded:
+        return d - s[None]
+    return np.concatenate([(-s)[None], d], axis=0)
+
+
+def ligand_term_weights(lig_type, tp: TermParams, folded=True):
+    """(n_atoms, K) weights of each ligand atom on each ligand grid."""
+    lig_type = np.asarray(lig_type)
+    n = lig_type.shape[0]
+    if tp.term_set == TERMS_SHAPE:
+        return np.ones((n, 1))
+    w = np.zeros((n, tp.n_types))
+    w[np.arange(n), lig_type] = 1.0
+    if folded:
+        return w
+    return np.concatenate([np.ones((n, 1)), w], axis=1)
+
+
+# ----------------------------------------------------------------------------
+# Ligand scatter: docking_molforce.hpp:351-368
+# ----------------------------------------------------------------------------
+def bin_ligand(geom, rot, lig_xyz):
+    """Rotated ligand cells (n, 3) int64 and an all-in-grid flag."""
+    p = rotate_points(rot, lig_xyz)
+    cells = geom.to_logical(p)
+    ok = bool(np.all((cells >= 0) & (cells < geom.n)))
+    return cells, ok
+
+
+def ligand_grids(geom, cells, weights):
+    n = geom.n
+    k = weights.shape[1]
+    grids = np.zeros((k, n, n, n), dtype=np.float64)
+    flat = (cells[:, 0] * n + cells[:, 1]) * n + cells[:, 2]
+    for t in range(k):
+        np.add.at(grids[t].reshape(-1), flat, weights[:, t])
+    return grids
+
+
+# ----------------------------------------------------------------------------
+# Correlation: docking_fft.hpp:622-633 (+ collectTotal, docking_molforce.hpp:249-269)
+# ----------------------------------------------------------------------------
+def receptor_spectra(rec_grids, workers=1):
+    import scipy.fft as sfft
+    return np.stack([sfft.rfftn(r, workers=workers) for r in rec_grids])
+
+
+def correlate(rec_spectra, lig_grids, workers=1):
+    """sum_t IFFT(conj(R^_t) * FFT(L_t)) (normalised by V), one forward and one
+    inverse transform per term as the reference does."""
+    import scipy.fft as sfft
+    n = lig_grids.shape[1]
+    total = None
+    for rs, lg in zip(rec_spectra, lig_grids):
+        lf = sfft.rfftn(lg, workers=workers)
+        c = sfft.irfftn(np.conj(rs) * lf, s=(n, n, n), workers=workers)
+        total = c if total is None else total + c
+    return total
+
+
+def select_minima(corr, k, max_val=np.inf):
+    """k smallest cells with value < max_val, ascending, ties by flat offset."""
+    flat = corr.reshape(-1)
+    idx = np.nonzero(flat < max_val)[0]
+    if idx.size == 0:
+        return np.zeros(0, dtype=np.int64), np.zeros(0)
+    vals = flat[idx]
+    if idx.size > k:
+        part = np.argpartition(vals, k - 1)[:k]
+        kth = vals[part].max()
+        pool = np.nonzero(vals <= kth)[0]
+        idx, vals = idx[pool], vals[pool]
+    order = np.lexsort((idx, vals))[:k]
+    return idx[order], vals[order]
+
+
+def unwrap(cell, n):
+    """``WrappedIndex::unwrap`` (Math/fft.hpp:199-206): y = -x, +n if y < -(n/2)."""
+    y = -np.asarray(cell, dtype=np.int64)
+    y = np.where(y < -(n // 2), y + n, y)
+    return y
+
+
+def offsets_to_cells(offsets, n):
+    offsets = np.asarray(offsets, dtype=np.int64)
+    return np.stack([offsets // (n * n), (offsets // n) % n, offsets % n], axis=-1)
+
+
+def translation(cell, geom):
+    """``toSpatialDiff(unwrap(cell))`` (gridcoord.hpp:150)."""
+    return geom.h * unwrap(cell, geom.n).astype(np.float64)
+
+
+# ----------------------------------------------------------------------------
+# Exact direct-space scorer (independent check of the FFT path)
+# ----------------------------------------------------------------------------
+def direct_score(rec_grids, cells, weights, shift_cell):
+    """C(s) = sum_j sum_t w_jt R_t(cell_j - s mod N), summed with math.fsum.
+
+    ``shift_cell`` is the correlation offset s (the FFT output index); the
+    ligand translation it stands for is h * unwrap(s)."""
+    n = rec_grids.shape[1]
+    s = np.asarray(shift_cell, dtype=np.int64)
+    c = (np.asarray(cells, dtype=np.int64) - s[None, :]) % n
+    terms = []
+    for t in range(rec_grids.shape[0]):
+        w = weights[:, t]
+        nz = w != 0
+        if not np.any(nz):
+            continue
+        vals = rec_grids[t][c[nz, 0], c[nz, 1], c[nz, 2]] * w[nz]
+        terms.extend(vals.tolist())
+    return math.fsum(terms)
+
+
+# ----------------------------------------------------------------------------
+# Whole-rotation scan (Worker::scanRotation)
+# ----------------------------------------------------------------------------
+@dataclass
+class ScanResult:
+    rot_id: int
+    offsets: np.ndarray
+    cells: np.ndarray
+    scores: np.ndarray
+    translations: np.ndarray
+    in_grid: bool = True
+    corr: np.ndarray | None = field(default=None, repr=False)
+
+
+def scan_rotation(geom, rec_grids, rec_spectra, lig_xyz, lig_weights, rot, k, max_val=np.inf,
+                  rot_id=0, keep_corr=False, workers=1):
+    cells, ok = bin_ligand(geom, rot, lig_xyz)
+    if not ok:
+        return ScanResult(rot_id, np.zeros(0, np.int64), np.zeros((0, 3), np.int64), np.zeros(0),
+                          np.zeros((0, 3)), in_grid=False)
+    lg = ligand_grids(geom, cells, lig_weights)
+    corr = correlate(rec_spectra, lg, workers=workers)
+    offs, vals = select_minima(corr, k, max_val)
+    pc = offsets_to_cells(offs, geom.n)
+    return ScanResult(rot_id, offs, pc, vals, translation(pc, geom), True, corr if keep_corr else None)
+
+
+# ----------------------------------------------------------------------------
+# Scan record format: docking_io_bin.hpp:21-76 (RotFftScanIO_Bin)
+# ----------------------------------------------------------------------------
+SCAN_SIGNATURE = 2014011401
+
+
+def pack_record(rot, translations, values):
+    """[int32 signature][3x3 float64 rotation][size_t n][n x (3 float64, float64)]."""
+    rot = np.asarray(rot, dtype=np.float64).reshape(9)
+    buf = struct.pack("<i", SCAN_SIGNATURE) + struct.pack("<9d", *rot)
+    n = len(values)
+    buf += struct.pack("<Q", n)
+    for t, v in zip(translations, values):
+        buf += struct.pack("<4d", float(t[0]), float(t[1]), float(t[2]), float(v))
+    return buf
+
+
+def unpack_records(data):
+    out = []
+    pos = 0
+    while pos + 4 <= len(data):
+        (sig,) = struct.unpack_from("<i", data, pos)
+        if sig != SCAN_SIGNATURE:
+            raise ValueError("Signature mismatch for binary format")
+        pos += 4
+        if pos + 72 + 8 > len(data):
+            break
+        rot = np.array(struct.unpack_from("<9d", data, pos)).reshape(3, 3)
+        pos += 72
+        (n,) = struct.unpack_from("<Q", data, pos)
+        pos += 8
+        if pos + 32 * n > len(data):
+            break
+        vals = np.array(struct.unpack_from("<%dd" % (4 * n), data, pos)).reshape(n, 4)
+        pos += 32 * n
+        out.append((rot, vals[:, :3], vals[:, 3]))
+    return out

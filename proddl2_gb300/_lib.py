@@ -1,0 +1,126 @@
+"""ctypes binding of libfftdock.so (include/fftdock.h).
+
+The library is built in-tree by ``proddl2_gb300.build``; importing this
+module does not build it.  :func:`lib` raises if the shared object is missing
+so that no caller can silently fall back to a CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libfftdock.so"
+
+FFTDOCK_OK = 0
+FFTDOCK_EINVAL = 1
+FFTDOCK_EOUT_OF_GRID = 2
+FFTDOCK_ECUDA = 3
+FFTDOCK_ENOMEM = 4
+FFTDOCK_ESTATE = 5
+FFTDOCK_EUNSUPPORTED = 6
+FFTDOCK_EIO = 7
+
+STATUS_NAMES = {
+    0: "FFTDOCK_OK", 1: "FFTDOCK_EINVAL", 2: "FFTDOCK_EOUT_OF_GRID", 3: "FFTDOCK_ECUDA",
+    4: "FFTDOCK_ENOMEM", 5: "FFTDOCK_ESTATE", 6: "FFTDOCK_EUNSUPPORTED", 7: "FFTDOCK_EIO",
+}
+
+FFTDOCK_TERMS_SHAPE = 1
+FFTDOCK_TERMS_SHAPE_ACE = 2
+FFTDOCK_PREC_FP32 = 0
+KC = 16
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_int32),
+        ("grid_n", C.c_int32),
+        ("grid_step", C.c_double),
+        ("term_set", C.c_int32),
+        ("peaks_per_rot", C.c_int32),
+        ("max_trans_inp", C.c_int32),
+        ("max_val_corr", C.c_double),
+        ("rot_batch", C.c_int32),
+        ("precision", C.c_int32),
+        ("device", C.c_int32),
+        ("n_types", C.c_int32),
+        ("ace_matrix", C.POINTER(C.c_double)),
+        ("shape_core_radius", C.c_double),
+        ("shape_surface_width", C.c_double),
+        ("ace_b", C.c_double),
+        ("ace_k", C.c_double),
+        ("ace_a", C.c_double),
+        ("ace_cut", C.c_double),
+    ]
+
+
+class Peak(C.Structure):
+    _fields_ = [
+        ("rot_id", C.c_int32),
+        ("cell", C.c_int32 * 3),
+        ("t", C.c_double * 3),
+        ("score", C.c_double),
+    ]
+
+
+class KernelStats(C.Structure):
+    _fields_ = [("launches", C.c_int64 * 4), ("total_ms", C.c_double * 4)]
+
+
+KERNEL_NAMES = ("ligand_prep", "pencil", "plane", "finalize")
+
+
+# numpy view of fftdock_peak
+def peak_dtype():
+    import numpy as np
+    return np.dtype([("rot_id", "<i4"), ("cell", "<i4", (3,)), ("t", "<f8", (3,)), ("score", "<f8")], align=True)
+
+
+# symbol -> (restype, argtypes); the exported surface of include/fftdock.h
+_P = C.c_void_p
+SIGNATURES = {
+    "fftdock_config_init": (None, [C.POINTER(Config)]),
+    "fftdock_supported_grid": (C.c_int, [C.c_int32]),
+    "fftdock_find_best_size": (C.c_int, [C.c_int32, C.POINTER(C.c_int32)]),
+    "fftdock_create": (C.c_int, [C.POINTER(Config), C.POINTER(_P)]),
+    "fftdock_destroy": (None, [_P]),
+    "fftdock_last_error": (C.c_char_p, [_P]),
+    "fftdock_set_receptor": (C.c_int, [_P, C.c_int32, _P, _P]),
+    "fftdock_set_ligand": (C.c_int, [_P, C.c_int32, _P, _P]),
+    "fftdock_scan": (C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, _P]),
+    "fftdock_scan_device": (C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, _P, _P]),
+    "fftdock_grid_n": (C.c_int, [_P]),
+    "fftdock_n_terms": (C.c_int, [_P]),
+    "fftdock_get_receptor_grid": (C.c_int, [_P, C.c_int32, _P]),
+    "fftdock_correlation_grid": (C.c_int, [_P, _P, _P]),
+    "fftdock_scan_candidates": (C.c_int, [_P, C.c_int32, _P, _P, _P]),
+    "fftdock_profile": (C.c_int, [_P, C.c_int32]),
+    "fftdock_get_kernel_stats": (C.c_int, [_P, C.POINTER(KernelStats)]),
+    "fftdock_write_scan_records": (C.c_int, [C.c_char_p, C.c_int32, _P, C.c_int32, _P, _P, C.c_int32]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load libfftdock.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(
+            "libfftdock.so is not built (%s); run `python -m proddl2_gb300.build` -- "
+            "there is no CPU fallback" % LIB_PATH)
+    h = C.CDLL(str(LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(h, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = h
+    return h
+
+
+class FFTDockError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(code, str(code)), msg))
+        self.code = code

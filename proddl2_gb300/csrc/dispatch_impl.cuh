@@ -1,0 +1,104 @@
+// Per-size launchers.  Included by the kernels_nXX.cu translation units, each
+// of which instantiates SizeOpsImpl<N> for its grid sizes.
+#pragma once
+
+#include "internal.h"
+#include "scan_kernels.cuh"
+
+namespace fftdock {
+
+template <int N> struct SizeOpsImpl {
+    static constexpr int G = SizeTraits<N>::G;
+    static constexpr int H = N / 2 + 1;
+
+    static size_t pencil_smem(int K, int n_ent) {
+        return (size_t)2 * N * 32 * sizeof(float2) + N * sizeof(float2) + ((size_t)K * N + 1) * sizeof(int32_t) +
+               (size_t)n_ent * sizeof(uint32_t);
+    }
+    static size_t plane_smem() { return (size_t)N * H * sizeof(float2) + N * sizeof(float2) + (size_t)G * KC * 8; }
+    template <typename T> static size_t line_smem() { return (size_t)(N * 32 + N) * sizeof(cplx_t<T>); }
+
+    static cudaError_t set_smem(const void* fn, size_t bytes) {
+        if (bytes <= 48 * 1024) return cudaSuccess;
+        return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    }
+
+    template <typename T, int SIGN>
+    static cudaError_t line_fft(cplx_t<T>* data, const cplx_t<T>* tw, long n_lines, long elem_stride,
+                                long inner_count, long inner_stride, long outer_stride, cudaStream_t s) {
+        const size_t sm = line_smem<T>();
+        cudaError_t e = set_smem((const void*)line_fft_kernel<T, N, SIGN>, sm);
+        if (e != cudaSuccess) return e;
+        const long blocks = (n_lines + 31) / 32;
+        line_fft_kernel<T, N, SIGN><<<(unsigned)blocks, 32 * G, sm, s>>>(data, tw, n_lines, elem_stride,
+                                                                        inner_count, inner_stride, outer_stride);
+        return cudaGetLastError();
+    }
+
+    static cudaError_t receptor_fft(const double* rgrid_t, double2* cbuf, double2* hbuf, const double2* tw64,
+                                    float2* spec_t, int PP, cudaStream_t s) {
+        const size_t V = (size_t)N * N * N;
+        complexify_kernel<<<(unsigned)((V + 255) / 256), 256, 0, s>>>(rgrid_t, cbuf, V);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        // z: lines (x, y), contiguous elements
+        e = line_fft<double, -1>(cbuf, tw64, (long)N * N, 1, N, N, (long)N * N, s);
+        if (e != cudaSuccess) return e;
+        const size_t NHt = (size_t)N * N * H;
+        half_extract_kernel<<<(unsigned)((NHt + 255) / 256), 256, 0, s>>>(cbuf, hbuf, N, H);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        // y: lines (x, kz) of [N][N][H]
+        e = line_fft<double, -1>(hbuf, tw64, (long)N * H, H, H, 1, (long)N * H, s);
+        if (e != cudaSuccess) return e;
+        // x: lines p = (ky, kz)
+        e = line_fft<double, -1>(hbuf, tw64, (long)N * H, (long)N * H, (long)N * H, 1, 0, s);
+        if (e != cudaSuccess) return e;
+        const size_t tot = (size_t)N * PP;
+        pack_spectrum_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(hbuf, spec_t, N, N * H, PP,
+                                                                         1.0 / (double)V);
+        return cudaGetLastError();
+    }
+
+    static cudaError_t scan_batch(const BatchArgs& a, cudaStream_t s) {
+        Geo geo{a.h, a.zero_h, a.center0, N};
+        const int nb = a.n_rot;
+        if (nb <= 0) return cudaSuccess;
+        cudaError_t e;
+        if (a.ev && (e = cudaEventRecord(a.ev[0], s)) != cudaSuccess) return e;
+        // K1
+        const size_t sm1 = ((size_t)a.K * N + 1) * sizeof(int32_t) + (size_t)a.n_ent * sizeof(uint32_t);
+        if ((e = set_smem((const void*)ligand_prep_kernel<N>, sm1)) != cudaSuccess) return e;
+        ligand_prep_kernel<N><<<nb, 256, sm1, s>>>(a.rot, a.lig_xyz, a.lig_term, a.n_ent, a.K, geo, a.ent, a.offs,
+                                                    a.status);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (a.ev && (e = cudaEventRecord(a.ev[1], s)) != cudaSuccess) return e;
+        // K2
+        const size_t sm2 = pencil_smem(a.K, a.n_ent);
+        if ((e = set_smem((const void*)pencil_kernel<N>, sm2)) != cudaSuccess) return e;
+        dim3 grid2(nb, a.PP / 32);
+        pencil_kernel<N><<<grid2, 32 * G, sm2, s>>>(a.spec, a.ent, a.offs, a.tw32, a.g2, a.K, a.PP, a.n_ent);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (a.ev && (e = cudaEventRecord(a.ev[2], s)) != cudaSuccess) return e;
+        // K3
+        const size_t sm3 = plane_smem();
+        if ((e = set_smem((const void*)plane_kernel<N>, sm3)) != cudaSuccess) return e;
+        dim3 grid3(N, nb);
+        plane_kernel<N><<<grid3, 32 * G, sm3, s>>>(a.g2, a.tw32, a.cand_v, a.cand_i, a.PP, a.dbg_corr);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (a.ev && (e = cudaEventRecord(a.ev[3], s)) != cudaSuccess) return e;
+        // K4
+        finalize_kernel<N><<<nb, 256, 0, s>>>(a.cand_v, a.cand_i, a.ent, a.status, a.rgrid, a.n_ent,
+                                              a.peak_stride, a.k_out, a.max_val, a.h, a.first_rot_id, a.peaks,
+                                              a.n_peaks, a.pool_v, a.pool_i);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (a.ev && (e = cudaEventRecord(a.ev[4], s)) != cudaSuccess) return e;
+        return cudaSuccess;
+    }
+
+    static const SizeOps* ops() {
+        static const SizeOps o{N, &receptor_fft, &scan_batch, &pencil_smem};
+        return &o;
+    }
+};
+
+}  // namespace fftdock

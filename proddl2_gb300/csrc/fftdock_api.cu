@@ -1,0 +1,635 @@
+// C ABI of libfftdock.so (declared in include/fftdock.h).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "fft_core.cuh"
+#include "fftdock.h"
+#include "internal.h"
+
+namespace fftdock {
+const SizeOps* size_ops_small(int n);
+const SizeOps* size_ops_mid(int n);
+const SizeOps* size_ops_big(int n);
+const SizeOps* size_ops_n128(int n);
+const SizeOps* size_ops_n144(int n);
+
+const SizeOps* size_ops(int n) {
+    const SizeOps* o = nullptr;
+    if ((o = size_ops_small(n))) return o;
+    if ((o = size_ops_mid(n))) return o;
+    if ((o = size_ops_big(n))) return o;
+    if ((o = size_ops_n128(n))) return o;
+    if ((o = size_ops_n144(n))) return o;
+    return nullptr;
+}
+
+constexpr int kKC = 16;
+constexpr int kMaxEntries = 32768;
+constexpr size_t kMaxSmem = 227 * 1024;
+}  // namespace fftdock
+
+using fftdock::BatchArgs;
+using fftdock::SizeOps;
+
+struct fftdock_ctx {
+    fftdock_config cfg{};
+    std::vector<double> ace;
+    const SizeOps* ops = nullptr;
+    int N = 0, H = 0, PP = 0, K = 0, B = 0;
+    size_t V = 0;
+    double h = 0, zero_h = 0, center0 = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    float2* tw32 = nullptr;
+    double2* tw64 = nullptr;
+    float2* spec = nullptr;
+    double* rgrid = nullptr;
+    double* emat = nullptr;
+
+    bool have_rec = false, have_lig = false;
+    int n_ent = 0;
+    double* lig_xyz = nullptr;
+    int32_t* lig_term = nullptr;
+
+    // per-batch work
+    uint32_t* ent = nullptr;
+    int32_t* offs = nullptr;
+    float2* g2 = nullptr;
+    float* cand_v = nullptr;
+    int32_t* cand_i = nullptr;
+
+    // per-call buffers (grown on demand)
+    int cap_rot = 0;
+    double* rot_all = nullptr;
+    int32_t* status_all = nullptr;
+    fftdock_peak* peaks_all = nullptr;
+    int32_t* npeaks_all = nullptr;
+    int cap_status_dev = 0;
+    int32_t* status_dev = nullptr;
+
+    // kernel timing (fftdock_profile)
+    bool profiling = false;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+};
+
+namespace {
+
+int fail(fftdock_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_fail(fftdock_ctx* c, cudaError_t e, const char* where) {
+    return fail(c, FFTDOCK_ECUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(expr)                                                   \
+    do {                                                           \
+        cudaError_t e_ = (expr);                                   \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #expr);   \
+    } while (0)
+
+template <typename T> cudaError_t dalloc(T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    return cudaMalloc((void**)p, n * sizeof(T));
+}
+
+template <typename T> void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+bool finite3(const double* p, int n) {
+    for (int i = 0; i < 3 * n; ++i)
+        if (!std::isfinite(p[i])) return false;
+    return true;
+}
+
+int grow_call_buffers(fftdock_ctx* ctx, int n_rot) {
+    if (n_rot <= ctx->cap_rot) return FFTDOCK_OK;
+    dfree(ctx->rot_all);
+    dfree(ctx->status_all);
+    dfree(ctx->peaks_all);
+    dfree(ctx->npeaks_all);
+    ctx->cap_rot = 0;
+    CK(dalloc(&ctx->rot_all, (size_t)n_rot * 9));
+    CK(dalloc(&ctx->status_all, (size_t)n_rot));
+    CK(dalloc(&ctx->peaks_all, (size_t)n_rot * ctx->cfg.peaks_per_rot));
+    CK(dalloc(&ctx->npeaks_all, (size_t)n_rot));
+    ctx->cap_rot = n_rot;
+    return FFTDOCK_OK;
+}
+
+int grow_status(fftdock_ctx* ctx, int n_rot) {
+    if (n_rot <= ctx->cap_status_dev) return FFTDOCK_OK;
+    dfree(ctx->status_dev);
+    ctx->cap_status_dev = 0;
+    CK(dalloc(&ctx->status_dev, (size_t)n_rot));
+    ctx->cap_status_dev = n_rot;
+    return FFTDOCK_OK;
+}
+
+BatchArgs batch_args(fftdock_ctx* ctx) {
+    BatchArgs a{};
+    a.lig_xyz = ctx->lig_xyz;
+    a.lig_term = ctx->lig_term;
+    a.spec = ctx->spec;
+    a.rgrid = ctx->rgrid;
+    a.tw32 = ctx->tw32;
+    a.n_ent = ctx->n_ent;
+    a.K = ctx->K;
+    a.PP = ctx->PP;
+    a.h = ctx->h;
+    a.zero_h = ctx->zero_h;
+    a.center0 = ctx->center0;
+    a.ent = ctx->ent;
+    a.offs = ctx->offs;
+    a.g2 = ctx->g2;
+    a.cand_v = ctx->cand_v;
+    a.cand_i = ctx->cand_i;
+    a.peak_stride = ctx->cfg.peaks_per_rot;
+    a.k_out = std::min(ctx->cfg.peaks_per_rot, ctx->cfg.max_trans_inp);
+    a.max_val = ctx->cfg.max_val_corr;
+    return a;
+}
+
+// queue every batch of a call; rot/peaks/npeaks/status are device arrays
+// covering the whole call
+int run_batches(fftdock_ctx* ctx, int n_rot, const double* rot, int first_id, fftdock_peak* peaks,
+                int32_t* npeaks, int32_t* status, cudaStream_t s, float* dbg, float* pool_v, int32_t* pool_i) {
+    BatchArgs a = batch_args(ctx);
+    for (int b0 = 0; b0 < n_rot; b0 += ctx->B) {
+        a.ev = nullptr;
+        if (ctx->profiling) {
+            while (ctx->ev_pool.size() < ctx->ev_used + 5) {
+                cudaEvent_t ev;
+                cudaError_t e = cudaEventCreate(&ev);
+                if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaEventCreate");
+                ctx->ev_pool.push_back(ev);
+            }
+            a.ev = ctx->ev_pool.data() + ctx->ev_used;
+            ctx->ev_used += 5;
+        }
+        const int nb = std::min(ctx->B, n_rot - b0);
+        a.rot = rot + (size_t)b0 * 9;
+        a.n_rot = nb;
+        a.status = status + b0;
+        a.peaks = peaks + (size_t)b0 * ctx->cfg.peaks_per_rot;
+        a.n_peaks = npeaks + b0;
+        a.first_rot_id = first_id + b0;
+        a.dbg_corr = dbg ? dbg + (size_t)b0 * ctx->V : nullptr;
+        a.pool_v = pool_v ? pool_v + (size_t)b0 * fftdock::kKC : nullptr;
+        a.pool_i = pool_i ? pool_i + (size_t)b0 * fftdock::kKC : nullptr;
+        cudaError_t e = ctx->ops->scan_batch(a, s);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "scan batch launch");
+    }
+    return FFTDOCK_OK;
+}
+
+int check_ready(fftdock_ctx* ctx) {
+    if (!ctx) return FFTDOCK_EINVAL;
+    if (!ctx->have_rec) return fail(ctx, FFTDOCK_ESTATE, "fftdock_set_receptor has not been called");
+    if (!ctx->have_lig) return fail(ctx, FFTDOCK_ESTATE, "fftdock_set_ligand has not been called");
+    return FFTDOCK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void fftdock_config_init(fftdock_config* cfg) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->struct_size = (int32_t)sizeof(fftdock_config);
+    cfg->grid_n = 128;
+    cfg->grid_step = 1.2;
+    cfg->term_set = FFTDOCK_TERMS_SHAPE_ACE;
+    cfg->peaks_per_rot = 4;
+    cfg->max_trans_inp = 10000;
+    cfg->max_val_corr = INFINITY;
+    cfg->rot_batch = 64;
+    cfg->precision = FFTDOCK_PREC_FP32;
+    cfg->device = 0;
+    cfg->n_types = 18;
+    cfg->ace_matrix = nullptr;
+    cfg->shape_core_radius = 2.2;
+    cfg->shape_surface_width = 1.8;
+    cfg->ace_b = 7.0;
+    cfg->ace_k = 0.15;
+    cfg->ace_a = 0.6;
+    cfg->ace_cut = 6.0;
+}
+
+int fftdock_supported_grid(int32_t n) { return fftdock::size_ops(n) != nullptr ? 1 : 0; }
+
+int fftdock_find_best_size(int32_t start_n, int32_t* result) {
+    if (!result) return FFTDOCK_EINVAL;
+    static const int primes[6] = {2, 3, 5, 7, 11, 13};
+    for (long n = start_n <= 1 ? 2 : start_n; n < 2147483647L; ++n) {
+        long rem = n;
+        int e[6] = {0, 0, 0, 0, 0, 0};
+        for (int i = 0; i < 6 && rem != 1; ++i)
+            while (rem % primes[i] == 0) { rem /= primes[i]; ++e[i]; }
+        if (rem == 1 && e[4] + e[5] <= 1) {
+            *result = (int32_t)n;
+            return FFTDOCK_OK;
+        }
+    }
+    return FFTDOCK_EINVAL;
+}
+
+const char* fftdock_last_error(const fftdock_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int fftdock_grid_n(const fftdock_ctx* ctx) { return ctx ? ctx->N : 0; }
+int fftdock_n_terms(const fftdock_ctx* ctx) { return ctx ? ctx->K : 0; }
+
+void fftdock_destroy(fftdock_ctx* ctx) {
+    if (!ctx) return;
+    dfree(ctx->tw32);
+    dfree(ctx->tw64);
+    dfree(ctx->spec);
+    dfree(ctx->rgrid);
+    dfree(ctx->emat);
+    dfree(ctx->lig_xyz);
+    dfree(ctx->lig_term);
+    dfree(ctx->ent);
+    dfree(ctx->offs);
+    dfree(ctx->g2);
+    dfree(ctx->cand_v);
+    dfree(ctx->cand_i);
+    dfree(ctx->rot_all);
+    dfree(ctx->status_all);
+    dfree(ctx->peaks_all);
+    dfree(ctx->npeaks_all);
+    dfree(ctx->status_dev);
+    for (cudaEvent_t ev : ctx->ev_pool) cudaEventDestroy(ev);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
+    if (!out) return FFTDOCK_EINVAL;
+    *out = nullptr;
+    fftdock_ctx* ctx = new (std::nothrow) fftdock_ctx();
+    if (!ctx) return FFTDOCK_ENOMEM;
+    *out = ctx;
+    if (!cfg_in) return fail(ctx, FFTDOCK_EINVAL, "null configuration");
+    if (cfg_in->struct_size != (int32_t)sizeof(fftdock_config))
+        return fail(ctx, FFTDOCK_EINVAL, "fftdock_config.struct_size does not match this library");
+    fftdock_config& c = ctx->cfg;
+    c = *cfg_in;
+    ctx->ops = fftdock::size_ops(c.grid_n);
+    if (!ctx->ops) return fail(ctx, FFTDOCK_EUNSUPPORTED, "grid_n " + std::to_string(c.grid_n) + " is not built");
+    if (!(c.grid_step > 0.0) || !std::isfinite(c.grid_step)) return fail(ctx, FFTDOCK_EINVAL, "grid_step must be > 0");
+    if (c.peaks_per_rot < 1 || c.peaks_per_rot > fftdock::kKC)
+        return fail(ctx, FFTDOCK_EINVAL, "peaks_per_rot must be in [1, 16]");
+    if (c.max_trans_inp < 1) return fail(ctx, FFTDOCK_EINVAL, "max_trans_inp must be >= 1");
+    if (c.rot_batch < 1 || c.rot_batch > 1024) return fail(ctx, FFTDOCK_EINVAL, "rot_batch must be in [1, 1024]");
+    if (c.precision != FFTDOCK_PREC_FP32) return fail(ctx, FFTDOCK_EUNSUPPORTED, "precision mode not built");
+    if (std::isnan(c.max_val_corr)) return fail(ctx, FFTDOCK_EINVAL, "max_val_corr is NaN");
+    if (!(c.shape_core_radius >= 0.0) || !(c.shape_surface_width >= 0.0))
+        return fail(ctx, FFTDOCK_EINVAL, "shape radii must be >= 0");
+    if (c.term_set == FFTDOCK_TERMS_SHAPE) {
+        ctx->K = 1;
+    } else if (c.term_set == FFTDOCK_TERMS_SHAPE_ACE) {
+        if (c.n_types < 1 || c.n_types > 32) return fail(ctx, FFTDOCK_EINVAL, "n_types must be in [1, 32]");
+        if (!c.ace_matrix) return fail(ctx, FFTDOCK_EINVAL, "ace_matrix is required for the shape+ACE term set");
+        if (!(c.ace_cut > 0.0)) return fail(ctx, FFTDOCK_EINVAL, "ace_cut must be > 0");
+        ctx->ace.assign(c.ace_matrix, c.ace_matrix + (size_t)c.n_types * c.n_types);
+        for (double v : ctx->ace)
+            if (!std::isfinite(v)) return fail(ctx, FFTDOCK_EINVAL, "ace_matrix has a non-finite entry");
+        ctx->K = c.n_types;
+    } else {
+        return fail(ctx, FFTDOCK_EINVAL, "unknown term_set");
+    }
+    c.ace_matrix = nullptr;
+    const int N = c.grid_n;
+    ctx->N = N;
+    ctx->H = N / 2 + 1;
+    ctx->PP = ((N * ctx->H) + 31) / 32 * 32;
+    ctx->V = (size_t)N * N * N;
+    ctx->B = c.rot_batch;
+    // centred geometry exactly as UniformCubicGeometry(step, logicalSize)
+    const double h = c.grid_step;
+    const double s_size = h + h * (double)(N - 1);
+    const double zero = (-1.0 * s_size) / 2.0;
+    ctx->h = h;
+    ctx->zero_h = zero - h;
+    ctx->center0 = zero + h / 2.0;
+
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) return fail(ctx, FFTDOCK_ECUDA, "no CUDA device available");
+    if (c.device < 0 || c.device >= ndev) return fail(ctx, FFTDOCK_EINVAL, "device ordinal out of range");
+    CK(cudaSetDevice(c.device));
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, c.device));
+    if (prop.major != 10 || prop.minor != 3)
+        return fail(ctx, FFTDOCK_EUNSUPPORTED, std::string("libfftdock is built for sm_103a only; device is ") +
+                                                   prop.name);
+    CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+
+    std::vector<float2> tw32(N);
+    std::vector<double2> tw64(N);
+    for (int k = 0; k < N; ++k) {
+        const double cr = fftdock::cos2pi(k, N), si = -fftdock::sin2pi(k, N);
+        tw32[k] = make_float2((float)cr, (float)si);
+        tw64[k] = make_double2(cr, si);
+    }
+    CK(dalloc(&ctx->tw32, N));
+    CK(dalloc(&ctx->tw64, N));
+    CK(cudaMemcpy(ctx->tw32, tw32.data(), N * sizeof(float2), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->tw64, tw64.data(), N * sizeof(double2), cudaMemcpyHostToDevice));
+    if (!ctx->ace.empty()) {
+        CK(dalloc(&ctx->emat, ctx->ace.size()));
+        CK(cudaMemcpy(ctx->emat, ctx->ace.data(), ctx->ace.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    CK(dalloc(&ctx->spec, (size_t)ctx->K * N * ctx->PP));
+    CK(dalloc(&ctx->rgrid, (size_t)ctx->K * ctx->V));
+    CK(dalloc(&ctx->offs, (size_t)ctx->B * (ctx->K * N + 1)));
+    CK(dalloc(&ctx->g2, (size_t)ctx->B * N * ctx->PP));
+    CK(dalloc(&ctx->cand_v, (size_t)ctx->B * N * fftdock::kKC));
+    CK(dalloc(&ctx->cand_i, (size_t)ctx->B * N * fftdock::kKC));
+    return FFTDOCK_OK;
+}
+
+int fftdock_set_receptor(fftdock_ctx* ctx, int32_t n, const double* xyz, const int32_t* type) {
+    if (!ctx) return FFTDOCK_EINVAL;
+    if (!ctx->ops) return fail(ctx, FFTDOCK_ESTATE, "context was not created successfully");
+    if (n < 0 || (n > 0 && !xyz)) return fail(ctx, FFTDOCK_EINVAL, "bad receptor atom arrays");
+    if (!finite3(xyz, n)) return fail(ctx, FFTDOCK_EINVAL, "receptor coordinates must be finite");
+    const fftdock_config& c = ctx->cfg;
+    const bool ace = c.term_set == FFTDOCK_TERMS_SHAPE_ACE;
+    if (ace) {
+        if (n > 0 && !type) return fail(ctx, FFTDOCK_EINVAL, "receptor atom types are required");
+        for (int i = 0; i < n; ++i)
+            if (type[i] < 0 || type[i] >= c.n_types) return fail(ctx, FFTDOCK_EINVAL, "receptor type out of range");
+    }
+    CK(cudaSetDevice(c.device));
+    ctx->have_rec = false;
+    const int N = ctx->N;
+    const size_t V = ctx->V;
+    cudaStream_t s = ctx->stream;
+    fftdock::Geo g{ctx->h, ctx->zero_h, ctx->center0, N};
+    double* d_xyz = nullptr;
+    int32_t* d_type = nullptr;
+    int* flags = nullptr;
+    double* dens = nullptr;
+    double2* cbuf = nullptr;
+    double2* hbuf = nullptr;
+    int rc = FFTDOCK_OK;
+    auto cleanup = [&]() {
+        cudaStreamSynchronize(s);
+        dfree(d_xyz);
+        dfree(d_type);
+        dfree(flags);
+        dfree(dens);
+        dfree(cbuf);
+        dfree(hbuf);
+    };
+#define CKR(expr)                                 \
+    do {                                          \
+        cudaError_t e_ = (expr);                  \
+        if (e_ != cudaSuccess) {                  \
+            rc = cuda_fail(ctx, e_, #expr);       \
+            cleanup();                            \
+            return rc;                            \
+        }                                         \
+    } while (0)
+    CKR(dalloc(&d_xyz, (size_t)n * 3));
+    CKR(dalloc(&d_type, (size_t)n));
+    CKR(dalloc(&flags, V));
+    if (n > 0) {
+        CKR(cudaMemcpyAsync(d_xyz, xyz, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, s));
+        if (ace) CKR(cudaMemcpyAsync(d_type, type, (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    }
+    if (ace) CKR(dalloc(&dens, (size_t)c.n_types * V));
+    {
+        fftdock::ReceptorGridArgs ra{};
+        ra.xyz = d_xyz;
+        ra.type = d_type;
+        ra.n = n;
+        ra.geo = g;
+        ra.term_set = c.term_set;
+        ra.n_types = c.n_types;
+        ra.K = ctx->K;
+        ra.shape_core = c.shape_core_radius;
+        ra.shape_width = c.shape_surface_width;
+        ra.ace_b = c.ace_b;
+        ra.ace_k = c.ace_k;
+        ra.ace_a = c.ace_a;
+        ra.ace_cut = c.ace_cut;
+        ra.emat = ctx->emat;
+        ra.flags = flags;
+        ra.dens = dens;
+        ra.rgrid = ctx->rgrid;
+        CKR(fftdock::build_receptor_grids(ra, s));
+    }
+    CKR(dalloc(&cbuf, V));
+    CKR(dalloc(&hbuf, (size_t)N * N * ctx->H));
+    for (int t = 0; t < ctx->K; ++t) {
+        CKR(ctx->ops->receptor_fft(ctx->rgrid + (size_t)t * V, cbuf, hbuf, ctx->tw64,
+                                   ctx->spec + (size_t)t * N * ctx->PP, ctx->PP, s));
+    }
+    CKR(cudaStreamSynchronize(s));
+    cleanup();
+#undef CKR
+    ctx->have_rec = true;
+    return FFTDOCK_OK;
+}
+
+int fftdock_set_ligand(fftdock_ctx* ctx, int32_t n, const double* xyz, const int32_t* type) {
+    if (!ctx) return FFTDOCK_EINVAL;
+    if (!ctx->ops) return fail(ctx, FFTDOCK_ESTATE, "context was not created successfully");
+    if (n < 1 || !xyz) return fail(ctx, FFTDOCK_EINVAL, "the ligand needs at least one atom");
+    if (n > fftdock::kMaxEntries) return fail(ctx, FFTDOCK_EINVAL, "ligand has more than 32768 atoms");
+    if (!finite3(xyz, n)) return fail(ctx, FFTDOCK_EINVAL, "ligand coordinates must be finite");
+    const fftdock_config& c = ctx->cfg;
+    std::vector<int32_t> term(n, 0);
+    if (c.term_set == FFTDOCK_TERMS_SHAPE_ACE) {
+        if (!type) return fail(ctx, FFTDOCK_EINVAL, "ligand atom types are required");
+        for (int i = 0; i < n; ++i) {
+            if (type[i] < 0 || type[i] >= c.n_types) return fail(ctx, FFTDOCK_EINVAL, "ligand type out of range");
+            term[i] = type[i];
+        }
+    }
+    if (ctx->ops->pencil_smem(ctx->K, n) > fftdock::kMaxSmem)
+        return fail(ctx, FFTDOCK_EINVAL, "ligand too large for the pencil kernel's shared memory");
+    CK(cudaSetDevice(c.device));
+    ctx->have_lig = false;
+    CK(cudaStreamSynchronize(ctx->stream));
+    dfree(ctx->lig_xyz);
+    dfree(ctx->lig_term);
+    dfree(ctx->ent);
+    CK(dalloc(&ctx->lig_xyz, (size_t)n * 3));
+    CK(dalloc(&ctx->lig_term, (size_t)n));
+    CK(dalloc(&ctx->ent, (size_t)ctx->B * n));
+    CK(cudaMemcpy(ctx->lig_xyz, xyz, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->lig_term, term.data(), (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice));
+    ctx->n_ent = n;
+    ctx->have_lig = true;
+    return FFTDOCK_OK;
+}
+
+int fftdock_scan(fftdock_ctx* ctx, int32_t n_rot, const double* rot, int32_t first_rot_id, fftdock_peak* peaks,
+                 int32_t* n_peaks) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (n_rot < 0 || (n_rot > 0 && (!rot || !peaks || !n_peaks))) return fail(ctx, FFTDOCK_EINVAL, "bad arguments");
+    if (n_rot == 0) return FFTDOCK_OK;
+    CK(cudaSetDevice(ctx->cfg.device));
+    if ((rc = grow_call_buffers(ctx, n_rot))) return rc;
+    cudaStream_t s = ctx->stream;
+    const int P = ctx->cfg.peaks_per_rot;
+    CK(cudaMemcpyAsync(ctx->rot_all, rot, (size_t)n_rot * 9 * sizeof(double), cudaMemcpyHostToDevice, s));
+    if ((rc = run_batches(ctx, n_rot, ctx->rot_all, first_rot_id, ctx->peaks_all, ctx->npeaks_all, ctx->status_all,
+                          s, nullptr, nullptr, nullptr)))
+        return rc;
+    CK(cudaMemcpyAsync(peaks, ctx->peaks_all, (size_t)n_rot * P * sizeof(fftdock_peak), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(n_peaks, ctx->npeaks_all, (size_t)n_rot * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    std::vector<int32_t> status(n_rot);
+    CK(cudaMemcpyAsync(status.data(), ctx->status_all, (size_t)n_rot * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (int i = 0; i < n_rot; ++i) {
+        if (status[i] != 0)
+            return fail(ctx, FFTDOCK_EOUT_OF_GRID,
+                        "rotation " + std::to_string(first_rot_id + i) + " moves a ligand atom outside the grid");
+    }
+    return FFTDOCK_OK;
+}
+
+int fftdock_scan_device(fftdock_ctx* ctx, int32_t n_rot, const double* d_rot, int32_t first_rot_id,
+                        fftdock_peak* d_peaks, int32_t* d_n_peaks, void* stream) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (n_rot < 0 || (n_rot > 0 && (!d_rot || !d_peaks || !d_n_peaks))) return fail(ctx, FFTDOCK_EINVAL, "bad arguments");
+    if (n_rot == 0) return FFTDOCK_OK;
+    CK(cudaSetDevice(ctx->cfg.device));
+    if ((rc = grow_status(ctx, n_rot))) return rc;
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    return run_batches(ctx, n_rot, d_rot, first_rot_id, d_peaks, d_n_peaks, ctx->status_dev, s, nullptr, nullptr,
+                       nullptr);
+}
+
+int fftdock_get_receptor_grid(fftdock_ctx* ctx, int32_t term, double* out) {
+    if (!ctx || !out) return FFTDOCK_EINVAL;
+    if (!ctx->have_rec) return fail(ctx, FFTDOCK_ESTATE, "fftdock_set_receptor has not been called");
+    if (term < 0 || term >= ctx->K) return fail(ctx, FFTDOCK_EINVAL, "term out of range");
+    CK(cudaSetDevice(ctx->cfg.device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(out, ctx->rgrid + (size_t)term * ctx->V, ctx->V * sizeof(double), cudaMemcpyDeviceToHost));
+    return FFTDOCK_OK;
+}
+
+int fftdock_correlation_grid(fftdock_ctx* ctx, const double* rot, float* out) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (!rot || !out) return fail(ctx, FFTDOCK_EINVAL, "bad arguments");
+    CK(cudaSetDevice(ctx->cfg.device));
+    if ((rc = grow_call_buffers(ctx, 1))) return rc;
+    cudaStream_t s = ctx->stream;
+    float* dbg = nullptr;
+    CK(dalloc(&dbg, ctx->V));
+    CK(cudaMemcpyAsync(ctx->rot_all, rot, 9 * sizeof(double), cudaMemcpyHostToDevice, s));
+    rc = run_batches(ctx, 1, ctx->rot_all, 0, ctx->peaks_all, ctx->npeaks_all, ctx->status_all, s, dbg, nullptr,
+                     nullptr);
+    cudaError_t e = rc ? cudaSuccess : cudaMemcpyAsync(out, dbg, ctx->V * sizeof(float), cudaMemcpyDeviceToHost, s);
+    cudaError_t e2 = cudaStreamSynchronize(s);
+    cudaFree(dbg);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "copy correlation grid");
+    if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "synchronize");
+    return FFTDOCK_OK;
+}
+
+int fftdock_scan_candidates(fftdock_ctx* ctx, int32_t n_rot, const double* rot, float* values, int32_t* offsets) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (n_rot < 1 || !rot || !values || !offsets) return fail(ctx, FFTDOCK_EINVAL, "bad arguments");
+    CK(cudaSetDevice(ctx->cfg.device));
+    if ((rc = grow_call_buffers(ctx, n_rot))) return rc;
+    cudaStream_t s = ctx->stream;
+    float* pv = nullptr;
+    int32_t* pi = nullptr;
+    CK(dalloc(&pv, (size_t)n_rot * fftdock::kKC));
+    cudaError_t e = dalloc(&pi, (size_t)n_rot * fftdock::kKC);
+    if (e != cudaSuccess) {
+        cudaFree(pv);
+        return cuda_fail(ctx, e, "alloc candidate pool");
+    }
+    e = cudaMemcpyAsync(ctx->rot_all, rot, (size_t)n_rot * 9 * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        rc = run_batches(ctx, n_rot, ctx->rot_all, 0, ctx->peaks_all, ctx->npeaks_all, ctx->status_all, s, nullptr,
+                         pv, pi);
+    if (e == cudaSuccess && !rc)
+        e = cudaMemcpyAsync(values, pv, (size_t)n_rot * fftdock::kKC * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && !rc)
+        e = cudaMemcpyAsync(offsets, pi, (size_t)n_rot * fftdock::kKC * sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    cudaError_t e2 = cudaStreamSynchronize(s);
+    cudaFree(pv);
+    cudaFree(pi);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "candidate pool");
+    if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "synchronize");
+    return FFTDOCK_OK;
+}
+
+int fftdock_profile(fftdock_ctx* ctx, int32_t enable) {
+    if (!ctx) return FFTDOCK_EINVAL;
+    ctx->profiling = enable != 0;
+    if (enable) ctx->ev_used = 0;
+    return FFTDOCK_OK;
+}
+
+int fftdock_get_kernel_stats(fftdock_ctx* ctx, fftdock_kernel_stats* out) {
+    if (!ctx || !out) return FFTDOCK_EINVAL;
+    std::memset(out, 0, sizeof(*out));
+    if (ctx->ev_used == 0) return FFTDOCK_OK;
+    CK(cudaSetDevice(ctx->cfg.device));
+    CK(cudaEventSynchronize(ctx->ev_pool[ctx->ev_used - 1]));
+    for (size_t b = 0; b + 5 <= ctx->ev_used; b += 5) {
+        for (int k = 0; k < 4; ++k) {
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, ctx->ev_pool[b + k], ctx->ev_pool[b + k + 1]));
+            out->launches[k] += 1;
+            out->total_ms[k] += ms;
+        }
+    }
+    return FFTDOCK_OK;
+}
+
+int fftdock_write_scan_records(const char* path, int32_t n_rot, const double* rot, int32_t peaks_per_rot,
+                               const fftdock_peak* peaks, const int32_t* n_peaks, int32_t append) {
+    if (!path || n_rot < 0 || peaks_per_rot < 1 || (n_rot > 0 && (!rot || !peaks || !n_peaks)))
+        return FFTDOCK_EINVAL;
+    FILE* f = std::fopen(path, append ? "ab" : "wb");
+    if (!f) return FFTDOCK_EIO;
+    const int32_t sig = 2014011401;
+    bool ok = true;
+    for (int i = 0; i < n_rot && ok; ++i) {
+        const int32_t np = n_peaks[i];
+        if (np < 0 || np > peaks_per_rot) { ok = false; break; }
+        ok = ok && std::fwrite(&sig, sizeof(sig), 1, f) == 1;
+        ok = ok && std::fwrite(rot + (size_t)9 * i, sizeof(double), 9, f) == 9;
+        const uint64_t nn = (uint64_t)np;
+        ok = ok && std::fwrite(&nn, sizeof(nn), 1, f) == 1;
+        for (int j = 0; j < np && ok; ++j) {
+            const fftdock_peak& p = peaks[(size_t)i * peaks_per_rot + j];
+            const double rec[4] = {p.t[0], p.t[1], p.t[2], p.score};
+            ok = std::fwrite(rec, sizeof(double), 4, f) == 4;
+        }
+    }
+    if (std::fclose(f) != 0) ok = false;
+    return ok ? FFTDOCK_OK : FFTDOCK_EIO;
+}
+
+}  // extern "C"

@@ -1,0 +1,85 @@
+// Internal declarations shared by the C ABI implementation and the per-size
+// kernel translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fftdock.h"
+
+namespace fftdock {
+
+// Grid geometry of the reference's centred UniformCubicGeometry
+// (include/PRODDL/Grid/gridcoord.hpp:127-191).
+struct Geo {
+    double h;        // step
+    double zero_h;   // spatial zero - h (toLogical)
+    double center0;  // centre of cell 0 (toSpatial)
+    int n;
+};
+
+struct ReceptorGridArgs {
+    const double* xyz;     // [n][3]
+    const int32_t* type;   // [n]
+    int n;
+    Geo geo;
+    int term_set;
+    int n_types;
+    int K;
+    double shape_core, shape_width;
+    double ace_b, ace_k, ace_a, ace_cut;
+    const double* emat;    // [n_types][n_types]
+    int* flags;            // [N^3] work
+    double* dens;          // [n_types][N^3] work (shape+ACE)
+    double* rgrid;         // [K][N^3] out
+};
+
+cudaError_t build_receptor_grids(const ReceptorGridArgs& a, cudaStream_t s);
+
+// Everything one device batch of rotations needs.
+struct BatchArgs {
+    // inputs
+    const double* rot;          // [B][9]
+    const double* lig_xyz;      // [n_ent][3]
+    const int32_t* lig_term;    // [n_ent]
+    const float2* spec;         // [K][N][PP]
+    const double* rgrid;        // [K][N^3]
+    const float2* tw32;         // [N]
+    int n_rot;                  // rotations in this batch (<= B)
+    int n_ent;
+    int K;
+    int PP;
+    double h, zero_h, center0;
+    // work
+    uint32_t* ent;              // [B][n_ent]
+    int32_t* offs;              // [B][K*N+1]
+    int32_t* status;            // [B]
+    float2* g2;                 // [B][N][PP]
+    float* cand_v;              // [B][N][KC]
+    int32_t* cand_i;
+    // outputs
+    fftdock_peak* peaks;        // [B][peak_stride]
+    int32_t* n_peaks;           // [B]
+    int peak_stride;
+    int k_out;
+    double max_val;
+    int first_rot_id;
+    float* dbg_corr;            // optional [B][N^3]
+    float* pool_v;              // optional [B][KC]
+    int32_t* pool_i;
+    cudaEvent_t* ev;            // optional: 5 events recorded around the 4 kernels
+};
+
+struct SizeOps {
+    int n;
+    // forward 3-D FFT of one real FP64 term grid into spec_t ([N][PP], scaled 1/V)
+    cudaError_t (*receptor_fft)(const double* rgrid_t, double2* cbuf, double2* hbuf, const double2* tw64,
+                                float2* spec_t, int PP, cudaStream_t s);
+    cudaError_t (*scan_batch)(const BatchArgs& a, cudaStream_t s);
+    // shared-memory bytes of the pencil kernel for (K, n_ent)
+    size_t (*pencil_smem)(int K, int n_ent);
+};
+
+const SizeOps* size_ops(int n);
+
+}  // namespace fftdock

@@ -1,0 +1,282 @@
+"""GPU scan vs the FP64 oracle, through the C ABI.
+
+Tolerances (the scan's parity bar):
+* receptor term grids: shape exact; desolvation within 1e-12 relative;
+* FP32 correlation grid: |gpu - oracle| <= 1e-4 * max|oracle| per grid;
+* FP32 candidate values: within 1e-4 relative of their exact FP64 energy
+  (relative to max(|energy|, 1));
+* reported peaks: FP64-rescored scores equal the oracle's exact direct-space
+  energy of the same cell to 1e-9 relative; per-rotation score lists equal the
+  oracle's within 1e-4 relative; translation cells identical except for ties
+  within that tolerance at the k-th place.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import fftdock_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+TERM_NAMES = {O.TERMS_SHAPE: "shape", O.TERMS_SHAPE_ACE: "shape_ace"}
+REL = 1e-4
+
+
+def _scan(n, term_set, ace, k=4, batch=64, **kw):
+    from proddl2_gb300 import FFTScan, ScanConfig
+    return FFTScan(ScanConfig(grid_n=int(n), grid_step=1.2, term_set=TERM_NAMES[int(term_set)], peaks_per_rot=k,
+                              rot_batch=batch, ace_matrix=ace, **kw))
+
+
+def _fixture(name):
+    return np.load(GOLDEN / (name + ".npz"))
+
+
+def _oracle_setup(n, term_set, ace, rec_xyz, rec_type, lig_type):
+    geom = O.Geometry.centred(1.2, n)
+    tp = O.TermParams(term_set=int(term_set), ace_matrix=ace)
+    rg = O.receptor_terms(geom, rec_xyz, rec_type, tp)
+    w = O.ligand_term_weights(lig_type, tp)
+    return geom, rg, w
+
+
+def assert_peaks_match(g_off, g_score, r_off, r_score, exact_fn):
+    """Tie-aware comparison of one rotation's peak list with the oracle's."""
+    assert len(g_off) == len(r_off)
+    if len(r_off) == 0:
+        return
+    scale = np.maximum(np.abs(r_score), 1.0)
+    assert np.all(np.abs(np.asarray(g_score) - np.asarray(r_score)) <= REL * scale), (g_score, r_score)
+    last = r_score[-1]
+    tie = REL * max(abs(last), 1.0)
+    gset = set(int(o) for o in g_off)
+    for o, s in zip(r_off, r_score):
+        if s < last - tie:
+            assert int(o) in gset, ("missing strict peak", o, s)
+    rset = set(int(o) for o in r_off)
+    for o, s in zip(g_off, g_score):
+        e = exact_fn(int(o))
+        assert abs(e - s) <= 1e-9 * max(1.0, abs(e)), ("rescored value", o, s, e)
+        if int(o) not in rset:
+            assert abs(e - last) <= tie, ("extra peak that is not a tie", o, e, last)
+
+
+@pytest.mark.parametrize("name", sorted(p.stem for p in GOLDEN.glob("*.npz")))
+def test_receptor_grids_match_oracle(name):
+    f = _fixture(name)
+    n = int(f["grid_n"])
+    geom, rg, _ = _oracle_setup(n, f["term_set"], f["ace"], f["rec_xyz"], f["rec_type"], f["lig_type"])
+    with _scan(n, f["term_set"], f["ace"]) as s:
+        s.set_receptor(f["rec_xyz"], f["rec_type"])
+        assert s.n_terms == rg.shape[0]
+        for t in range(rg.shape[0]):
+            g = s.receptor_grid(t)
+            if int(f["term_set"]) == O.TERMS_SHAPE:
+                assert np.array_equal(g, rg[t])
+            else:
+                assert np.allclose(g, rg[t], rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["scan_shape_ace_n32", "scan_shape_n48"])
+def test_correlation_grid_matches_oracle(name):
+    f = _fixture(name)
+    n = int(f["grid_n"])
+    with _scan(n, f["term_set"], f["ace"]) as s:
+        s.set_receptor(f["rec_xyz"], f["rec_type"])
+        s.set_ligand(f["lig_xyz"], f["lig_type"])
+        c = s.correlation_grid(f["rotations"][0]).astype(np.float64)
+    ref = f["corr0"].astype(np.float64)
+    err = np.abs(c - ref).max()
+    assert err <= REL * np.abs(ref).max(), (err, np.abs(ref).max())
+
+
+@pytest.mark.parametrize("name", sorted(p.stem for p in GOLDEN.glob("*.npz")))
+def test_peaks_match_golden(name):
+    f = _fixture(name)
+    n, k = int(f["grid_n"]), int(f["k"])
+    geom, rg, w = _oracle_setup(n, f["term_set"], f["ace"], f["rec_xyz"], f["rec_type"], f["lig_type"])
+    with _scan(n, f["term_set"], f["ace"], k=k) as s:
+        s.set_receptor(f["rec_xyz"], f["rec_type"])
+        s.set_ligand(f["lig_xyz"], f["lig_type"])
+        res = s.scan(f["rotations"])
+    for i, rot in enumerate(f["rotations"]):
+        cells, _ = O.bin_ligand(geom, rot, f["lig_xyz"])
+        cell, t, score = res.rotation(i)
+        off = (cell[:, 0] * n + cell[:, 1]) * n + cell[:, 2]
+        assert np.all(res.peaks[i, :res.n_peaks[i]]["rot_id"] == i)
+        # translation = h * unwrap(cell)
+        assert np.array_equal(t, O.translation(cell, geom))
+        exact = lambda o: O.direct_score(rg, cells, w, O.offsets_to_cells([o], n)[0])  # noqa: E731
+        assert_peaks_match(off, score, f["offsets"][i], f["scores"][i], exact)
+
+
+def _live_case(n, term_set, n_rec, n_lig, n_rot, seed, k=4):
+    from proddl2_gb300 import synth
+    pair = synth.make_pair(n_rec, n_lig, n_rot, seed=seed)
+    geom, rg, w = _oracle_setup(n, term_set, pair.ace, pair.receptor.xyz, pair.receptor.ace_type, pair.ligand.ace_type)
+    rs = O.receptor_spectra(rg, workers=8)
+    with _scan(n, term_set, pair.ace, k=k) as s:
+        s.set_receptor(pair.receptor.xyz, pair.receptor.ace_type)
+        s.set_ligand(pair.ligand.xyz, pair.ligand.ace_type)
+        res = s.scan(pair.rotations)
+        cand_v, cand_o = s.candidates(pair.rotations)
+    for i, rot in enumerate(pair.rotations):
+        ref = O.scan_rotation(geom, rg, rs, pair.ligand.xyz, w, rot, k, workers=8)
+        cells, _ = O.bin_ligand(geom, rot, pair.ligand.xyz)
+        cell, t, score = res.rotation(i)
+        off = (cell[:, 0] * n + cell[:, 1]) * n + cell[:, 2]
+        exact = lambda o: O.direct_score(rg, cells, w, O.offsets_to_cells([o], n)[0])  # noqa: E731
+        assert_peaks_match(off, score, ref.offsets, ref.scores, exact)
+        # the FP32 candidate pool is ascending and within tolerance of FP64
+        assert np.all(np.diff(cand_v[i]) >= 0)
+        scale = max(1.0, abs(ref.scores[0]))
+        for v, o in zip(cand_v[i][:4], cand_o[i][:4]):
+            assert abs(v - exact(int(o))) <= REL * scale
+
+
+@pytest.mark.parametrize("n", [16, 24, 32, 48])
+def test_small_sizes_shape_ace_vs_live_oracle(n):
+    n_rec = {16: 40, 24: 120, 32: 300, 48: 700}[n]
+    n_lig = {16: 12, 24: 30, 32: 70, 48: 150}[n]
+    _live_case(n, O.TERMS_SHAPE_ACE, n_rec, n_lig, n_rot=5, seed=100 + n)
+
+
+@pytest.mark.parametrize("n", [64, 80, 96, 112, 144])
+def test_all_sizes_shape_vs_live_oracle(n):
+    _live_case(n, O.TERMS_SHAPE, n_rec=1500, n_lig=400, n_rot=3, seed=200 + n)
+
+
+def test_full_size_shape_ace_128():
+    """4000 / 1500 atoms, 128^3, 18 folded terms: peaks vs the oracle FFT for
+    a few rotations, FP64 rescoring exact, bit-identical reruns."""
+    from proddl2_gb300 import synth
+    n, k = 128, 4
+    pair = synth.make_pair(4000, 1500, 70, seed=7)
+    with _scan(n, O.TERMS_SHAPE_ACE, pair.ace, k=k) as s:
+        s.set_receptor(pair.receptor.xyz, pair.receptor.ace_type)
+        s.set_ligand(pair.ligand.xyz, pair.ligand.ace_type)
+        res = s.scan(pair.rotations)
+        res2 = s.scan(pair.rotations)
+    assert np.array_equal(res.peaks, res2.peaks) and np.array_equal(res.n_peaks, res2.n_peaks)
+    assert np.all(res.n_peaks == k)
+    geom, rg, w = _oracle_setup(n, O.TERMS_SHAPE_ACE, pair.ace, pair.receptor.xyz, pair.receptor.ace_type,
+                                pair.ligand.ace_type)
+    # every rotation: scores ascending and equal to the exact energy of their cell
+    for i in range(0, 70, 7):
+        cells, _ = O.bin_ligand(geom, pair.rotations[i], pair.ligand.xyz)
+        cell, t, score = res.rotation(i)
+        assert np.all(np.diff(score) >= 0)
+        for c, sc in zip(cell, score):
+            e = O.direct_score(rg, cells, w, c)
+            assert abs(e - sc) <= 1e-9 * max(1.0, abs(e))
+    # two rotations against the full FP64 FFT oracle
+    rs = O.receptor_spectra(rg, workers=8)
+    for i in (0, 65):
+        ref = O.scan_rotation(geom, rg, rs, pair.ligand.xyz, w, pair.rotations[i], k, workers=8)
+        cells, _ = O.bin_ligand(geom, pair.rotations[i], pair.ligand.xyz)
+        cell, t, score = res.rotation(i)
+        off = (cell[:, 0] * n + cell[:, 1]) * n + cell[:, 2]
+        exact = lambda o: O.direct_score(rg, cells, w, O.offsets_to_cells([o], n)[0])  # noqa: E731
+        assert_peaks_match(off, score, ref.offsets, ref.scores, exact)
+
+
+def test_batch_size_does_not_change_results():
+    f = _fixture("scan_shape_ace_n32")
+    out = []
+    for batch in (1, 4, 64):
+        with _scan(32, f["term_set"], f["ace"], batch=batch) as s:
+            s.set_receptor(f["rec_xyz"], f["rec_type"])
+            s.set_ligand(f["lig_xyz"], f["lig_type"])
+            out.append(s.scan(f["rotations"], first_rot_id=10))
+    for r in out[1:]:
+        assert np.array_equal(r.peaks, out[0].peaks)
+    assert np.all(out[0].peaks["rot_id"][:, 0] == 10 + np.arange(len(f["rotations"])))
+
+
+def test_out_of_grid_rotations_are_reported():
+    from proddl2_gb300 import FFTDockError, _lib
+    f = _fixture("scan_shape_n48")
+    lig = np.array(f["lig_xyz"]) + np.array([20.0, 0.0, 0.0])  # pushed towards the +x face
+    rots = np.stack([np.eye(3), np.diag([-1.0, -1.0, 1.0]), np.eye(3)])
+    with _scan(48, f["term_set"], f["ace"]) as s:
+        s.set_receptor(f["rec_xyz"], f["rec_type"])
+        s.set_ligand(lig, f["lig_type"])
+        geom = O.Geometry.centred(1.2, 48)
+        ok = [O.bin_ligand(geom, r, lig)[1] for r in rots]
+        assert ok == [False, True, False] or ok == [True, False, True] or not all(ok)
+        with pytest.raises(FFTDockError) as ei:
+            s.scan(rots)
+        assert ei.value.code == _lib.FFTDOCK_EOUT_OF_GRID
+        res = s.scan(rots, raise_out_of_grid=False)
+        for i, good in enumerate(ok):
+            assert (res.n_peaks[i] > 0) == good
+
+
+def test_value_limit_and_queue_bound():
+    f = _fixture("scan_shape_ace_n32")
+    sc = f["scores"]
+    limit = float(np.median(sc[:, 1]))
+    with _scan(32, f["term_set"], f["ace"], max_val_corr=limit, max_trans_inp=3) as s:
+        s.set_receptor(f["rec_xyz"], f["rec_type"])
+        s.set_ligand(f["lig_xyz"], f["lig_type"])
+        res = s.scan(f["rotations"])
+    for i in range(len(f["rotations"])):
+        expect = min(3, int(np.sum(sc[i] < limit)))
+        assert res.n_peaks[i] == expect
+        assert np.all(res.peaks[i, :expect]["score"] < limit)
+
+
+def test_empty_receptor_and_single_atom_ligand():
+    with _scan(32, O.TERMS_SHAPE, None) as s:
+        s.set_receptor(np.zeros((0, 3)))
+        s.set_ligand(np.zeros((1, 3)))
+        res = s.scan(np.eye(3)[None])
+    # every energy is 0: ties resolved by offset
+    assert res.n_peaks[0] == 4
+    assert list(res.peaks[0]["score"]) == [0.0] * 4
+    offs = [(c[0] * 32 + c[1]) * 32 + c[2] for c in res.peaks[0]["cell"]]
+    assert offs == [0, 1, 2, 3]
+
+
+def test_state_and_argument_errors():
+    from proddl2_gb300 import FFTDockError, _lib
+    f = _fixture("scan_shape_ace_n32")
+    with _scan(32, f["term_set"], f["ace"]) as s:
+        with pytest.raises(FFTDockError) as ei:
+            s.scan(f["rotations"])
+        assert ei.value.code == _lib.FFTDOCK_ESTATE
+        bad_types = np.array(f["rec_type"]).copy()
+        bad_types[0] = 99
+        with pytest.raises(FFTDockError) as ei:
+            s.set_receptor(f["rec_xyz"], bad_types)
+        assert ei.value.code == _lib.FFTDOCK_EINVAL
+        nan_xyz = np.array(f["lig_xyz"]).copy()
+        nan_xyz[3, 1] = np.nan
+        with pytest.raises(FFTDockError) as ei:
+            s.set_ligand(nan_xyz, f["lig_type"])
+        assert ei.value.code == _lib.FFTDOCK_EINVAL
+        s.set_receptor(f["rec_xyz"], f["rec_type"])
+        s.set_ligand(f["lig_xyz"], f["lig_type"])
+        assert s.scan(np.zeros((0, 9))).n_peaks.shape == (0,)
+
+
+def test_device_scan_matches_host_scan():
+    import torch
+    from proddl2_gb300 import _lib
+    f = _fixture("scan_shape_ace_n64")
+    with _scan(64, f["term_set"], f["ace"], k=int(f["k"])) as s:
+        s.set_receptor(f["rec_xyz"], f["rec_type"])
+        s.set_ligand(f["lig_xyz"], f["lig_type"])
+        host = s.scan(f["rotations"])
+        n = len(f["rotations"])
+        d_rot = torch.tensor(np.asarray(f["rotations"]).reshape(n, 9), dtype=torch.float64, device="cuda")
+        d_peaks = torch.zeros(n * int(f["k"]) * 48, dtype=torch.uint8, device="cuda")
+        d_np = torch.zeros(n, dtype=torch.int32, device="cuda")
+        s.scan_device(d_rot.data_ptr(), n, d_peaks.data_ptr(), d_np.data_ptr(),
+                      stream_ptr=torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        peaks = d_peaks.cpu().numpy().view(_lib.peak_dtype()).reshape(n, int(f["k"]))
+        assert np.array_equal(d_np.cpu().numpy(), host.n_peaks)
+        assert np.array_equal(peaks, host.peaks)

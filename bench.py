@@ -48,6 +48,7 @@ def parse_args():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="shape_ace128")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--n-rot", type=int, default=0, help="scan only this many rotations per step (profiling runs)")
     return p.parse_args()
 
 
@@ -242,6 +243,8 @@ def run_ours(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     w = workload(args.workload)
+    if args.n_rot > 0:
+        w["n_rot"] = args.n_rot
     pair = synth.make_pair(w["n_rec"], w["n_lig"], w["n_rot"], seed=1)
     n_rot = w["n_rot"]
     cfg = ScanConfig(grid_n=w["grid_n"], grid_step=w["grid_step"], term_set=w["term_set"], peaks_per_rot=w["peaks"],
@@ -257,7 +260,11 @@ def run_ours(args):
     peak_bytes = _lib.peak_dtype().itemsize
     d_peaks = torch.zeros(n_rot * w["peaks"] * peak_bytes, dtype=torch.uint8, device=dev)
     d_np = torch.zeros(n_rot, dtype=torch.int32, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated stream: the library launches on it and the timing events are
+    # recorded on it (the legacy default stream would not order against the
+    # library's own non-blocking stream)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
 
     def step():
         scan.scan_device(d_rot.data_ptr(), n_rot, d_peaks.data_ptr(), d_np.data_ptr(), stream_ptr=stream.cuda_stream)

@@ -132,6 +132,21 @@ int fftdock_scan(fftdock_ctx* ctx, int32_t n_rot, const double* rot, int32_t fir
 int fftdock_scan_device(fftdock_ctx* ctx, int32_t n_rot, const double* d_rot, int32_t first_rot_id,
                         fftdock_peak* d_peaks, int32_t* d_n_peaks, void* stream);
 
+/* Scan without allocating device memory (no counterpart in the reference,
+ * whose scan runs in its own process and allocates freely).  For callers that
+ * cannot allocate at scan time: a host whose memory pool already owns the
+ * GPU, or a pipeline that forbids allocation once running.  Same arguments
+ * and results as fftdock_scan_device, but the per-batch work memory lives in
+ * one 16 MiB array compiled into the library (one per GPU, kept until the
+ * process exits) instead of the context's buffers; the context must already
+ * hold a receptor and a ligand.  Batches shrink to fit the array; a context
+ * whose single rotation needs more than 16 MiB is rejected with
+ * FFTDOCK_EINVAL.  The first call on a device looks up the array's device
+ * address, so make it before any stream capture.  All calls share the array:
+ * calls whose GPU work overlaps race and must be serialised by the caller. */
+int fftdock_scan_device_noalloc(fftdock_ctx* ctx, int32_t n_rot, const double* d_rot, int32_t first_rot_id,
+                                fftdock_peak* d_peaks, int32_t* d_n_peaks, void* stream);
+
 /* Introspection. */
 int fftdock_grid_n(const fftdock_ctx* ctx);
 int fftdock_n_terms(const fftdock_ctx* ctx);

@@ -89,6 +89,7 @@ SIGNATURES = {
     "fftdock_set_ligand": (C.c_int, [_P, C.c_int32, _P, _P]),
     "fftdock_scan": (C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, _P]),
     "fftdock_scan_device": (C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, _P, _P]),
+    "fftdock_scan_device_noalloc": (C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, _P, _P]),
     "fftdock_grid_n": (C.c_int, [_P]),
     "fftdock_n_terms": (C.c_int, [_P]),
     "fftdock_get_receptor_grid": (C.c_int, [_P, C.c_int32, _P]),

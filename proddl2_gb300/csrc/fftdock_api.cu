@@ -204,6 +204,29 @@ int check_ready(fftdock_ctx* ctx) {
 
 }  // namespace
 
+namespace fftdock {
+
+// Inputs of a scan held by a ready context, for entry points that bring
+// their own work memory.
+int ctx_scan_inputs(fftdock_ctx* ctx, ScanInputs* in) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    in->args = batch_args(ctx);
+    in->ops = ctx->ops;
+    in->device = ctx->cfg.device;
+    in->stream = ctx->stream;
+    in->N = ctx->N;
+    in->K = ctx->K;
+    in->PP = ctx->PP;
+    in->B = ctx->B;
+    in->n_ent = ctx->n_ent;
+    return FFTDOCK_OK;
+}
+
+int ctx_fail(fftdock_ctx* ctx, int code, const char* msg) { return fail(ctx, code, msg); }
+
+}  // namespace fftdock
+
 extern "C" {
 
 void fftdock_config_init(fftdock_config* cfg) {

@@ -82,4 +82,16 @@ struct SizeOps {
 
 const SizeOps* size_ops(int n);
 
+// Read-only view of a ready context's scan inputs (receptor spectra and
+// grids, ligand, geometry); the work pointers of `args` are the context's own.
+struct ScanInputs {
+    BatchArgs args;
+    const SizeOps* ops;
+    int device;
+    cudaStream_t stream;
+    int N, K, PP, B, n_ent;
+};
+int ctx_scan_inputs(fftdock_ctx* ctx, ScanInputs* in);
+int ctx_fail(fftdock_ctx* ctx, int code, const char* msg);
+
 }  // namespace fftdock

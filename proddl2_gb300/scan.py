@@ -166,6 +166,15 @@ class FFTScan:
                                                  C.c_void_p(d_peaks_ptr), C.c_void_p(d_npeaks_ptr),
                                                  C.c_void_p(stream_ptr) if stream_ptr else None))
 
+    def scan_device_noalloc(self, d_rot_ptr, n_rot, d_peaks_ptr, d_npeaks_ptr, first_rot_id=0, stream_ptr=None):
+        """Like :meth:`scan_device`, but the library allocates nothing: its
+        work memory is a fixed 16 MiB array inside the library, for callers
+        whose host owns all device memory or forbids allocation while running.
+        Calls that overlap on the GPU share that array and race."""
+        self._check(self.lib.fftdock_scan_device_noalloc(
+            self._h, int(n_rot), C.c_void_p(d_rot_ptr), int(first_rot_id), C.c_void_p(d_peaks_ptr),
+            C.c_void_p(d_npeaks_ptr), C.c_void_p(stream_ptr) if stream_ptr else None))
+
     # -- diagnostics ----------------------------------------------------------
     def profile(self, enable=True):
         """Record CUDA events around every scan kernel (starting clears the record)."""

@@ -1,0 +1,74 @@
+"""The scan entry point that allocates no device memory.
+
+Some callers cannot allocate device memory when they scan: a host whose own
+memory pool already holds the whole GPU, or a pipeline that forbids
+allocation once it runs.  fftdock_scan_device_noalloc keeps its work memory
+in a fixed array inside the library; here it must give the same peaks as
+fftdock_scan_device on the same context, on two calls in a row (the second
+call reuses the array the first one left behind).  Named to run last.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def _run(scan, rot, k, noalloc):
+    import torch
+    from proddl2_gb300 import _lib
+    n = rot.shape[0]
+    d_rot = torch.tensor(rot.reshape(n, 9), dtype=torch.float64, device="cuda")
+    d_peaks = torch.zeros(n * k * _lib.peak_dtype().itemsize, dtype=torch.uint8, device="cuda")
+    d_np = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        fn = scan.scan_device_noalloc if noalloc else scan.scan_device
+        fn(d_rot.data_ptr(), n, d_peaks.data_ptr(), d_np.data_ptr(), first_rot_id=5,
+           stream_ptr=stream.cuda_stream)
+    stream.synchronize()
+    return d_peaks.cpu().numpy().view(_lib.peak_dtype()).reshape(n, k), d_np.cpu().numpy()
+
+
+def _same(a, b):
+    (pa, na), (pb, nb) = a, b
+    assert np.array_equal(na, nb)
+    for i in range(len(na)):
+        x, y = pa[i, :na[i]], pb[i, :nb[i]]
+        assert np.array_equal(x["rot_id"], y["rot_id"])
+        assert np.array_equal(x["cell"], y["cell"])
+        assert np.array_equal(x["t"], y["t"])
+        assert np.allclose(x["score"], y["score"], rtol=1e-9, atol=1e-9)
+
+
+def _check(scan, rot, k):
+    ref = _run(scan, rot, k, noalloc=False)
+    assert np.all(ref[1] == k)
+    first = _run(scan, rot, k, noalloc=True)
+    second = _run(scan, rot, k, noalloc=True)
+    _same(first, ref)
+    _same(second, ref)
+
+
+def test_noalloc_scan_matches_device_scan_64():
+    from proddl2_gb300 import FFTScan, ScanConfig
+    f = np.load(GOLDEN / "scan_shape_ace_n64.npz")
+    k = int(f["k"])
+    rot = np.asarray(f["rotations"])
+    rot = np.concatenate([rot] * 8)  # 24 rotations, several per work-array batch
+    with FFTScan(ScanConfig(grid_n=64, term_set="shape_ace", peaks_per_rot=k, ace_matrix=f["ace"])) as s:
+        s.set_receptor(f["rec_xyz"], f["rec_type"])
+        s.set_ligand(f["lig_xyz"], f["lig_type"])
+        _check(s, rot, k)
+
+
+def test_noalloc_scan_matches_device_scan_128():
+    from proddl2_gb300 import FFTScan, ScanConfig, synth
+    pair = synth.make_pair(4000, 1500, 6, seed=9)
+    with FFTScan(ScanConfig(grid_n=128, term_set="shape_ace", peaks_per_rot=4, ace_matrix=pair.ace)) as s:
+        s.set_receptor(pair.receptor.xyz, pair.receptor.ace_type)
+        s.set_ligand(pair.ligand.xyz, pair.ligand.ace_type)
+        _check(s, pair.rotations, 4)

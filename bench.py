@@ -49,6 +49,7 @@ def parse_args():
     p.add_argument("--workload", default="shape_ace128")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--n-rot", type=int, default=0, help="scan only this many rotations per step (profiling runs)")
+    p.add_argument("--pencil", default="auto", choices=["auto", "fft", "tensor"])
     return p.parse_args()
 
 
@@ -133,19 +134,22 @@ def reference_schedule_bytes(n, k, batch):
     return (2 * k + 2) * m * 8 + k * m * 8 / batch
 
 
-def load_peaks():
+FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+
+
+def load_peaks(key):
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             d = json.load(f)
-        return float(d["hbm_gbs"]), "measured"
+        return float(d[key]), "measured"
     except Exception:
-        return 6800.0, "fallback"
+        return FALLBACK_PEAKS[key], "fallback"
 
 
-def committed_traffic(name):
-    """DRAM bytes per pencil-kernel launch recorded from an ncu capture in
-    profiles/ (a line 'dram_bytes_per_launch: <int>'), or None."""
-    path = os.path.join(ROOT, "profiles", "pencil_%s.md" % name)
+def committed_traffic(stem):
+    """DRAM bytes per launch of the dominant kernel recorded from an ncu
+    capture in profiles/<stem>.md (a line 'dram_bytes_per_launch: <int>')."""
+    path = os.path.join(ROOT, "profiles", "%s.md" % stem)
     try:
         for line in open(path):
             if line.startswith("dram_bytes_per_launch:"):
@@ -248,7 +252,7 @@ def run_ours(args):
     pair = synth.make_pair(w["n_rec"], w["n_lig"], w["n_rot"], seed=1)
     n_rot = w["n_rot"]
     cfg = ScanConfig(grid_n=w["grid_n"], grid_step=w["grid_step"], term_set=w["term_set"], peaks_per_rot=w["peaks"],
-                     rot_batch=w["rot_batch"], ace_matrix=pair.ace, device=local)
+                     rot_batch=w["rot_batch"], ace_matrix=pair.ace, device=local, pencil_mode=args.pencil)
     scan = FFTScan(cfg)
     t0 = time.perf_counter()
     scan.set_receptor(pair.receptor.xyz, pair.receptor.ace_type)
@@ -319,18 +323,44 @@ def run_ours(args):
     h2d = rot_host.nbytes
     d2h = res.peaks.nbytes + res.n_peaks.nbytes + 4 * n_rot
 
-    # roofline of the dominant kernel (pencil): algorithmic bytes of the
-    # reference schedule for the rotations one launch processes
+    # roofline of the dominant kernel (the pencil stage)
+    info = scan.info()
     launches, pencil_ms = kstats["pencil"]
-    k_terms = scan.n_terms
-    batch = w["rot_batch"]
-    rot_per_launch = n_rot * args.steps / max(launches, 1)
-    bytes_per_launch = reference_schedule_bytes(w["grid_n"], k_terms, batch) * rot_per_launch
+    k_terms = info["n_terms"]
+    batch = info["rot_batch"]
     avg_launch_ms = pencil_ms / max(launches, 1)
-    achieved_gbs = bytes_per_launch / (avg_launch_ms / 1000.0) / 1e9
-    peak_gbs, peak_kind = load_peaks()
-    traffic = committed_traffic(w["name"])
     gpu_launches = sum(v[0] for v in kstats.values())
+    total_kernel_ms = sum(v[1] for v in kstats.values())
+    share = pencil_ms / total_kernel_ms if total_kernel_ms else None
+    n = w["grid_n"]
+    if info["pencil_path"] == "tensor":
+        # executed tcgen05 work: per pencil and 128-rotation group, K * W/8
+        # chunks of 6 MMAs (real and imaginary output x hi*hi, hi*lo, lo*hi)
+        # of 128 x 128 x 16
+        n_batches = math.ceil(n_rot / batch)
+        groups_per_step = sum(math.ceil(min(batch, n_rot - b0) / 128) for b0 in range(0, n_rot, batch))
+        nh = n * (n // 2 + 1)
+        flops_per_group = nh * k_terms * (info["window_w"] // 8) * 6 * (2.0 * 128 * 128 * 16)
+        flops_per_launch = flops_per_group * groups_per_step / n_batches
+        achieved = flops_per_launch / (avg_launch_ms / 1000.0) / 1e12
+        peak, peak_kind = load_peaks("bf16_tflops")
+        traffic = committed_traffic("pencil_tc_%s" % w["name"])
+        roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak, "traffic": traffic, "kernel": "pencil_tc",
+                    "peak_source": peak_kind,
+                    "flops_basis": "executed FP16 MMA work: N^2(N/2+1) pencils x K x W/8 chunks x 6 MMAs "
+                                   "of 128x128x16 per 128-rotation group (W = %d)" % info["window_w"],
+                    "kernel_share": share}
+    else:
+        rot_per_launch = n_rot * args.steps / max(launches, 1)
+        bytes_per_launch = reference_schedule_bytes(n, k_terms, batch) * rot_per_launch
+        achieved_gbs = bytes_per_launch / (avg_launch_ms / 1000.0) / 1e9
+        peak_gbs, peak_kind = load_peaks("hbm_gbs")
+        roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": peak_gbs, "unit": "GB/s",
+                    "frac": achieved_gbs / peak_gbs, "traffic": committed_traffic("pencil_%s" % w["name"]),
+                    "kernel": "pencil", "peak_source": peak_kind,
+                    "bytes_basis": "reference FFT schedule, (2K+2)*M*8 + K*M*8/batch per rotation",
+                    "kernel_share": share}
 
     if rank != 0:
         scan.close()
@@ -348,7 +378,6 @@ def run_ours(args):
                          "forward + inverse 3-D FFT per term per rotation), scipy pocketfft on %d threads"
                          % (n_s, dt, ref.rg.shape[0], threads)}
 
-    total_kernel_ms = sum(v[1] for v in kstats.values())
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -356,17 +385,17 @@ def run_ours(args):
         "data": "synthetic (seeded globules, uniform quaternion rotations)",
         "config": {"workload": workload_desc(w), "mode": "exhaustive",
                    "parallelism": "replicas" if world == 1 else "rotation sets per rank (replicas)",
-                   "l2": "inputs larger than L2: 153 MB receptor spectra + 545 MB batch planes per step",
+                   "l2": "inputs larger than L2: %.0f MB receptor spectra + %.0f MB x-planes per batch"
+                         % (k_terms * n * n * (n // 2 + 1) * 8 / 1e6, batch * n * n * (n // 2 + 1) * 8 / 1e6),
                    "receptor_setup_ms": receptor_ms,
-                   "precision": "FP32 FFT/spectrum product, FP64 direct-space rescoring of 16 candidates"},
+                   "pencil_stage": info["pencil_path"],
+                   "precision": ("split-FP16 tcgen05 GEMM with FP32 accumulation (hi*hi+hi*lo+lo*hi) for the x stage, "
+                                 "FP32 FFTs elsewhere" if info["pencil_path"] == "tensor" else "FP32 FFTs")
+                                + ", FP64 direct-space rescoring of 16 candidates"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": gpu_launches,
         "kernels_ms_per_step": {k: v[1] / args.steps for k, v in kstats.items()},
-        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak_gbs, "unit": "GB/s",
-                     "frac": achieved_gbs / peak_gbs, "traffic": traffic,
-                     "kernel": "pencil", "peak_source": peak_kind,
-                     "bytes_basis": "reference FFT schedule, (2K+2)*M*8 + K*M*8/64 per rotation",
-                     "kernel_share": pencil_ms / total_kernel_ms if total_kernel_ms else None},
+        "roofline": roofline,
         "cpu_baseline": cpu,
         "clocks": clocks,
     }

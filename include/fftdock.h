@@ -60,6 +60,18 @@ enum {
     FFTDOCK_PREC_FP32 = 0
 };
 
+/* how the per-pencil x stage (x transforms and the spectrum product summed
+ * over terms) runs.  AUTO = FFT.  TENSOR (grid edges <= 128) restates the
+ * stage as a circular correlation along x computed with split-FP16 tcgen05
+ * GEMMs (hi*hi + hi*lo + lo*hi, FP32 accumulate); on GB300 at 128^3 with 18
+ * terms it measured 3.4x slower than FFT and its FP32 candidate values carry
+ * up to ~2e-4 relative error against 1.6e-5 for FFT, so it is opt-in only. */
+enum {
+    FFTDOCK_PENCIL_AUTO = 0,
+    FFTDOCK_PENCIL_FFT = 1,     /* FP32 x-FFTs on the CUDA cores */
+    FFTDOCK_PENCIL_TENSOR = 2   /* circular correlation as split-FP16 tcgen05 GEMMs, FP32 accumulate */
+};
+
 typedef struct fftdock_config {
     int32_t struct_size;         /* sizeof(fftdock_config) */
     int32_t grid_n;              /* FFT grid edge N (cubic); see fftdock_supported_grid() */
@@ -77,6 +89,7 @@ typedef struct fftdock_config {
     double shape_surface_width;  /* surface shell width beyond the core radius (A) */
     double ace_b, ace_k, ace_a;  /* sigmoid 1/(1+exp(b(k r - a))) (potentials_inc.hpp:394-397) */
     double ace_cut;              /* cutoff of the desolvation field (A) */
+    int32_t pencil_mode;         /* FFTDOCK_PENCIL_* */
 } fftdock_config;
 
 /* one selected translation; the reference's TranValue
@@ -150,6 +163,17 @@ int fftdock_scan_device_noalloc(fftdock_ctx* ctx, int32_t n_rot, const double* d
 /* Introspection. */
 int fftdock_grid_n(const fftdock_ctx* ctx);
 int fftdock_n_terms(const fftdock_ctx* ctx);
+
+typedef struct fftdock_scan_info {
+    int32_t grid_n;
+    int32_t n_terms;       /* K correlation terms */
+    int32_t pencil_path;   /* FFTDOCK_PENCIL_FFT or FFTDOCK_PENCIL_TENSOR (the form that runs) */
+    int32_t rot_batch;     /* rotations per device batch */
+    int32_t n_entries;     /* ligand entries (0 before fftdock_set_ligand) */
+    int32_t window_x0;     /* tensor path: first x cell of the ligand window */
+    int32_t window_w;      /* tensor path: window width in cells (multiple of 8) */
+} fftdock_scan_info;
+int fftdock_get_scan_info(const fftdock_ctx* ctx, fftdock_scan_info* out);
 
 /* Copy receptor term grid `term` (real space, FP64, N^3 C order) to host. */
 int fftdock_get_receptor_grid(fftdock_ctx* ctx, int32_t term, double* out);

@@ -28,6 +28,9 @@ STATUS_NAMES = {
 FFTDOCK_TERMS_SHAPE = 1
 FFTDOCK_TERMS_SHAPE_ACE = 2
 FFTDOCK_PREC_FP32 = 0
+FFTDOCK_PENCIL_AUTO = 0
+FFTDOCK_PENCIL_FFT = 1
+FFTDOCK_PENCIL_TENSOR = 2
 KC = 16
 
 
@@ -51,6 +54,7 @@ class Config(C.Structure):
         ("ace_k", C.c_double),
         ("ace_a", C.c_double),
         ("ace_cut", C.c_double),
+        ("pencil_mode", C.c_int32),
     ]
 
 
@@ -68,6 +72,12 @@ class KernelStats(C.Structure):
 
 
 KERNEL_NAMES = ("ligand_prep", "pencil", "plane", "finalize")
+
+
+class ScanInfo(C.Structure):
+    _fields_ = [("grid_n", C.c_int32), ("n_terms", C.c_int32), ("pencil_path", C.c_int32),
+                ("rot_batch", C.c_int32), ("n_entries", C.c_int32), ("window_x0", C.c_int32),
+                ("window_w", C.c_int32)]
 
 
 # numpy view of fftdock_peak
@@ -92,6 +102,7 @@ SIGNATURES = {
     "fftdock_scan_device_noalloc": (C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, _P, _P]),
     "fftdock_grid_n": (C.c_int, [_P]),
     "fftdock_n_terms": (C.c_int, [_P]),
+    "fftdock_get_scan_info": (C.c_int, [_P, C.POINTER(ScanInfo)]),
     "fftdock_get_receptor_grid": (C.c_int, [_P, C.c_int32, _P]),
     "fftdock_correlation_grid": (C.c_int, [_P, _P, _P]),
     "fftdock_scan_candidates": (C.c_int, [_P, C.c_int32, _P, _P, _P]),

@@ -4,6 +4,7 @@
 
 #include "internal.h"
 #include "scan_kernels.cuh"
+#include "pencil_tc.cuh"
 
 namespace fftdock {
 
@@ -35,8 +36,22 @@ template <int N> struct SizeOpsImpl {
         return cudaGetLastError();
     }
 
+    static constexpr bool kHasTc = N <= 128;
+
+    static size_t tc_smem() { return (size_t)TC_STAGES * TC_STAGE_BYTES + N * sizeof(TcPair) + N * sizeof(float2); }
+
+    static cudaError_t circ_scales(const float2* circ, int K, int8_t* cscale, cudaStream_t s) {
+        if constexpr (kHasTc) {
+            const int nh = N * H;
+            circ_scale_kernel<N><<<(nh + 127) / 128, 128, 0, s>>>(circ, K, cscale);
+            return cudaGetLastError();
+        } else {
+            return cudaErrorNotSupported;
+        }
+    }
+
     static cudaError_t receptor_fft(const double* rgrid_t, double2* cbuf, double2* hbuf, const double2* tw64,
-                                    float2* spec_t, int PP, cudaStream_t s) {
+                                    float2* spec_t, int PP, float2* circ_t, cudaStream_t s) {
         const size_t V = (size_t)N * N * N;
         complexify_kernel<<<(unsigned)((V + 255) / 256), 256, 0, s>>>(rgrid_t, cbuf, V);
         cudaError_t e = cudaGetLastError();
@@ -50,6 +65,13 @@ template <int N> struct SizeOpsImpl {
         // y: lines (x, kz) of [N][N][H]
         e = line_fft<double, -1>(hbuf, tw64, (long)N * H, H, H, 1, (long)N * H, s);
         if (e != cudaSuccess) return e;
+        if (circ_t) {
+            // receptor transformed along z and y only: circulant samples of the tensor path
+            const size_t tot = (size_t)N * N * H;
+            pack_circ_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(hbuf, circ_t, N, N * H,
+                                                                         1.0 / ((double)N * N));
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
         // x: lines p = (ky, kz)
         e = line_fft<double, -1>(hbuf, tw64, (long)N * H, (long)N * H, (long)N * H, 1, 0, s);
         if (e != cudaSuccess) return e;
@@ -73,17 +95,36 @@ template <int N> struct SizeOpsImpl {
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if (a.ev && (e = cudaEventRecord(a.ev[1], s)) != cudaSuccess) return e;
         // K2
-        const size_t sm2 = pencil_smem(a.K, a.n_ent);
-        if ((e = set_smem((const void*)pencil_kernel<N>, sm2)) != cudaSuccess) return e;
-        dim3 grid2(nb, a.PP / 32);
-        pencil_kernel<N><<<grid2, 32 * G, sm2, s>>>(a.spec, a.ent, a.offs, a.tw32, a.g2, a.K, a.PP, a.n_ent);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        bool pmajor = false;
+        if constexpr (kHasTc) {
+            if (a.use_tc) {
+                pmajor = true;
+                const size_t smt = tc_smem();
+                if ((e = set_smem((const void*)pencil_tc_kernel<N>, smt)) != cudaSuccess) return e;
+                dim3 gridt(N * H, (nb + TC_ROT - 1) / TC_ROT);
+                pencil_tc_kernel<N><<<gridt, 160, smt, s>>>(a.circ, a.cscale, a.ent, a.offs, a.tw32, a.g2, a.K,
+                                                           a.n_ent, nb, a.x0, a.W, a.err);
+                if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            }
+        }
+        if (!pmajor) {
+            const size_t sm2 = pencil_smem(a.K, a.n_ent);
+            if ((e = set_smem((const void*)pencil_kernel<N>, sm2)) != cudaSuccess) return e;
+            dim3 grid2(nb, a.PP / 32);
+            pencil_kernel<N><<<grid2, 32 * G, sm2, s>>>(a.spec, a.ent, a.offs, a.tw32, a.g2, a.K, a.PP, a.n_ent);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
         if (a.ev && (e = cudaEventRecord(a.ev[2], s)) != cudaSuccess) return e;
         // K3
         const size_t sm3 = plane_smem();
-        if ((e = set_smem((const void*)plane_kernel<N>, sm3)) != cudaSuccess) return e;
         dim3 grid3(N, nb);
-        plane_kernel<N><<<grid3, 32 * G, sm3, s>>>(a.g2, a.tw32, a.cand_v, a.cand_i, a.PP, a.dbg_corr);
+        if (pmajor) {
+            if ((e = set_smem((const void*)plane_kernel<N, true>, sm3)) != cudaSuccess) return e;
+            plane_kernel<N, true><<<grid3, 32 * G, sm3, s>>>(a.g2, a.tw32, a.cand_v, a.cand_i, a.PP, a.dbg_corr);
+        } else {
+            if ((e = set_smem((const void*)plane_kernel<N, false>, sm3)) != cudaSuccess) return e;
+            plane_kernel<N, false><<<grid3, 32 * G, sm3, s>>>(a.g2, a.tw32, a.cand_v, a.cand_i, a.PP, a.dbg_corr);
+        }
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if (a.ev && (e = cudaEventRecord(a.ev[3], s)) != cudaSuccess) return e;
         // K4
@@ -96,7 +137,7 @@ template <int N> struct SizeOpsImpl {
     }
 
     static const SizeOps* ops() {
-        static const SizeOps o{N, &receptor_fft, &scan_batch, &pencil_smem};
+        static const SizeOps o{N, &receptor_fft, &circ_scales, kHasTc, &scan_batch, &pencil_smem};
         return &o;
     }
 };

@@ -1,6 +1,7 @@
 // C ABI of libfftdock.so (declared in include/fftdock.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -73,6 +74,13 @@ struct fftdock_ctx {
     int32_t* npeaks_all = nullptr;
     int cap_status_dev = 0;
     int32_t* status_dev = nullptr;
+
+    // tensor-core pencil stage
+    bool use_tc = false;
+    float2* circ = nullptr;
+    int8_t* cscale = nullptr;
+    int* err_dev = nullptr;
+    int x0 = 0, W = 0;
 
     // kernel timing (fftdock_profile)
     bool profiling = false;
@@ -159,7 +167,25 @@ BatchArgs batch_args(fftdock_ctx* ctx) {
     a.peak_stride = ctx->cfg.peaks_per_rot;
     a.k_out = std::min(ctx->cfg.peaks_per_rot, ctx->cfg.max_trans_inp);
     a.max_val = ctx->cfg.max_val_corr;
+    a.use_tc = ctx->use_tc ? 1 : 0;
+    a.circ = ctx->circ;
+    a.cscale = ctx->cscale;
+    a.x0 = ctx->x0;
+    a.W = ctx->W;
+    a.err = ctx->err_dev;
     return a;
+}
+
+// nonzero device error word -> FFTDOCK_ECUDA (after a synchronisation)
+int check_pipeline(fftdock_ctx* ctx) {
+    int err = 0;
+    CK(cudaMemcpy(&err, ctx->err_dev, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err != 0) {
+        cudaMemset(ctx->err_dev, 0, sizeof(int));
+        return fail(ctx, FFTDOCK_ECUDA,
+                    "tensor pencil stage timed out waiting on a pipeline barrier (code " + std::to_string(err) + ")");
+    }
+    return FFTDOCK_OK;
 }
 
 // queue every batch of a call; rot/peaks/npeaks/status are device arrays
@@ -273,6 +299,18 @@ int fftdock_find_best_size(int32_t start_n, int32_t* result) {
 const char* fftdock_last_error(const fftdock_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
 int fftdock_grid_n(const fftdock_ctx* ctx) { return ctx ? ctx->N : 0; }
+
+int fftdock_get_scan_info(const fftdock_ctx* ctx, fftdock_scan_info* out) {
+    if (!ctx || !out) return FFTDOCK_EINVAL;
+    out->grid_n = ctx->N;
+    out->n_terms = ctx->K;
+    out->pencil_path = ctx->use_tc ? FFTDOCK_PENCIL_TENSOR : FFTDOCK_PENCIL_FFT;
+    out->rot_batch = ctx->B;
+    out->n_entries = ctx->have_lig ? ctx->n_ent : 0;
+    out->window_x0 = ctx->x0;
+    out->window_w = ctx->W;
+    return FFTDOCK_OK;
+}
 int fftdock_n_terms(const fftdock_ctx* ctx) { return ctx ? ctx->K : 0; }
 
 void fftdock_destroy(fftdock_ctx* ctx) {
@@ -294,6 +332,9 @@ void fftdock_destroy(fftdock_ctx* ctx) {
     dfree(ctx->peaks_all);
     dfree(ctx->npeaks_all);
     dfree(ctx->status_dev);
+    dfree(ctx->circ);
+    dfree(ctx->cscale);
+    dfree(ctx->err_dev);
     for (cudaEvent_t ev : ctx->ev_pool) cudaEventDestroy(ev);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -319,6 +360,13 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
     if (c.rot_batch < 1 || c.rot_batch > 1024) return fail(ctx, FFTDOCK_EINVAL, "rot_batch must be in [1, 1024]");
     if (c.precision != FFTDOCK_PREC_FP32) return fail(ctx, FFTDOCK_EUNSUPPORTED, "precision mode not built");
     if (std::isnan(c.max_val_corr)) return fail(ctx, FFTDOCK_EINVAL, "max_val_corr is NaN");
+    if (c.pencil_mode < FFTDOCK_PENCIL_AUTO || c.pencil_mode > FFTDOCK_PENCIL_TENSOR)
+        return fail(ctx, FFTDOCK_EINVAL, "unknown pencil_mode");
+    if (c.pencil_mode == FFTDOCK_PENCIL_TENSOR && !ctx->ops->has_tc)
+        return fail(ctx, FFTDOCK_EUNSUPPORTED, "the tensor-core pencil stage covers grid edges up to 128");
+    // AUTO runs the FP32 FFT form: the tensor form measured slower and less
+    // accurate on the candidate values (see fftdock.h, FFTDOCK_PENCIL_TENSOR)
+    ctx->use_tc = c.pencil_mode == FFTDOCK_PENCIL_TENSOR;
     if (!(c.shape_core_radius >= 0.0) || !(c.shape_surface_width >= 0.0))
         return fail(ctx, FFTDOCK_EINVAL, "shape radii must be >= 0");
     if (c.term_set == FFTDOCK_TERMS_SHAPE) {
@@ -382,6 +430,12 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
     CK(dalloc(&ctx->g2, (size_t)ctx->B * N * ctx->PP));
     CK(dalloc(&ctx->cand_v, (size_t)ctx->B * N * fftdock::kKC));
     CK(dalloc(&ctx->cand_i, (size_t)ctx->B * N * fftdock::kKC));
+    CK(dalloc(&ctx->err_dev, 1));
+    CK(cudaMemset(ctx->err_dev, 0, sizeof(int)));
+    if (ctx->use_tc) {
+        CK(dalloc(&ctx->circ, (size_t)ctx->K * N * ctx->H * N));
+        CK(dalloc(&ctx->cscale, (size_t)N * ctx->H));
+    }
     return FFTDOCK_OK;
 }
 
@@ -461,8 +515,10 @@ int fftdock_set_receptor(fftdock_ctx* ctx, int32_t n, const double* xyz, const i
     CKR(dalloc(&hbuf, (size_t)N * N * ctx->H));
     for (int t = 0; t < ctx->K; ++t) {
         CKR(ctx->ops->receptor_fft(ctx->rgrid + (size_t)t * V, cbuf, hbuf, ctx->tw64,
-                                   ctx->spec + (size_t)t * N * ctx->PP, ctx->PP, s));
+                                   ctx->spec + (size_t)t * N * ctx->PP, ctx->PP,
+                                   ctx->use_tc ? ctx->circ + (size_t)t * N * ctx->H * N : nullptr, s));
     }
+    if (ctx->use_tc) CKR(ctx->ops->circ_scales(ctx->circ, ctx->K, ctx->cscale, s));
     CKR(cudaStreamSynchronize(s));
     cleanup();
 #undef CKR
@@ -498,6 +554,25 @@ int fftdock_set_ligand(fftdock_ctx* ctx, int32_t n, const double* xyz, const int
     CK(dalloc(&ctx->ent, (size_t)ctx->B * n));
     CK(cudaMemcpy(ctx->lig_xyz, xyz, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->lig_term, term.data(), (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice));
+    // window of x cells that holds the ligand under every rotation about the
+    // origin: |R p| <= max |p|, with a cell of margin on each side
+    double rmax = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double r2 = xyz[3 * i] * xyz[3 * i] + xyz[3 * i + 1] * xyz[3 * i + 1] + xyz[3 * i + 2] * xyz[3 * i + 2];
+        rmax = std::max(rmax, std::sqrt(r2));
+    }
+    rmax = rmax * (1.0 + 1e-9) + 1e-9;
+    const int N = ctx->N;
+    long lo = (long)std::floor((-rmax - ctx->zero_h) / ctx->h) - 2;
+    long hi = (long)std::floor((rmax - ctx->zero_h) / ctx->h) + 0;
+    lo = std::max(lo, 0L);
+    hi = std::min(hi, (long)N - 1);
+    int W = (int)((hi - lo + 1 + 7) / 8 * 8);
+    if (W > N) W = N;
+    long x0 = lo;
+    if (x0 + W > N) x0 = N - W;
+    ctx->x0 = (int)x0;
+    ctx->W = W;
     ctx->n_ent = n;
     ctx->have_lig = true;
     return FFTDOCK_OK;
@@ -522,6 +597,7 @@ int fftdock_scan(fftdock_ctx* ctx, int32_t n_rot, const double* rot, int32_t fir
     std::vector<int32_t> status(n_rot);
     CK(cudaMemcpyAsync(status.data(), ctx->status_all, (size_t)n_rot * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    if ((rc = check_pipeline(ctx))) return rc;
     for (int i = 0; i < n_rot; ++i) {
         if (status[i] != 0)
             return fail(ctx, FFTDOCK_EOUT_OF_GRID,

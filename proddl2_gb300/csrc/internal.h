@@ -68,13 +68,22 @@ struct BatchArgs {
     float* pool_v;              // optional [B][KC]
     int32_t* pool_i;
     cudaEvent_t* ev;            // optional: 5 events recorded around the 4 kernels
+    // tensor-core pencil stage (use_tc): g2 is then [B][N*H][N] (x fastest)
+    int use_tc;
+    const float2* circ;         // [K][N*H][N] receptor circulant samples
+    const int8_t* cscale;       // [N*H] power-of-two scale exponents
+    int x0, W;                  // ligand window along x
+    int* err;                   // device word: nonzero after a pipeline timeout
 };
 
 struct SizeOps {
     int n;
     // forward 3-D FFT of one real FP64 term grid into spec_t ([N][PP], scaled 1/V)
     cudaError_t (*receptor_fft)(const double* rgrid_t, double2* cbuf, double2* hbuf, const double2* tw64,
-                                float2* spec_t, int PP, cudaStream_t s);
+                                float2* spec_t, int PP, float2* circ_t, cudaStream_t s);
+    // per-pencil scale exponents of the circulant samples (tensor path)
+    cudaError_t (*circ_scales)(const float2* circ, int K, int8_t* cscale, cudaStream_t s);
+    bool has_tc;
     cudaError_t (*scan_batch)(const BatchArgs& a, cudaStream_t s);
     // shared-memory bytes of the pencil kernel for (K, n_ent)
     size_t (*pencil_smem)(int K, int n_ent);

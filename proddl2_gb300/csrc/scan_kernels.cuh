@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) pencil_kernel(
 // top-KC.  (FFTW c2r of FFTCorrelator::correlate + CorrelationProcessor::
 // selectIntoQueue, docking_fft.hpp:452-468.)
 // ---------------------------------------------------------------------------
-template <int N>
+template <int N, bool PMAJOR>
 __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     const float2* __restrict__ g2, const float2* __restrict__ tw, float* __restrict__ cand_v,
     int32_t* __restrict__ cand_i, int PP, float* __restrict__ dbg) {
@@ -314,7 +314,10 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     const int tid = threadIdx.x;
     const int w = tid >> 5, l = tid & 31;
     for (int i = tid; i < N; i += blockDim.x) tws[i] = tw[i];
-    const float2* src = g2 + ((size_t)q * N + x) * PP;
+    // element (ky, kz) of plane x: [B][N][PP] (x-planes contiguous) or, after
+    // the tensor pencil stage, [B][N*H][N] (x fastest)
+    const float2* src = PMAJOR ? g2 + (size_t)q * N * H * N + x : g2 + ((size_t)q * N + x) * PP;
+    constexpr int ES = PMAJOR ? N : 1;
     __syncthreads();
 
     // columns: inverse DFT along ky
@@ -329,10 +332,10 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
             float2 a = make_float2(0.f, 0.f);
             if (valid) {
                 if (s == 0) {
-                    const float2 d = src[ky * H], ny = src[ky * H + NS];
+                    const float2 d = src[(size_t)(ky * H) * ES], ny = src[(size_t)(ky * H + NS) * ES];
                     a = make_float2(d.x - ny.y, d.y + ny.x);
                 } else {
-                    a = src[ky * H + s];
+                    a = src[(size_t)(ky * H + s) * ES];
                 }
             }
             v[r] = a;

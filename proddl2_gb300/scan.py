@@ -19,6 +19,7 @@ from . import _lib
 from ._lib import FFTDockError
 
 TERM_SETS = {"shape": _lib.FFTDOCK_TERMS_SHAPE, "shape_ace": _lib.FFTDOCK_TERMS_SHAPE_ACE}
+PENCIL_MODES = {"auto": _lib.FFTDOCK_PENCIL_AUTO, "fft": _lib.FFTDOCK_PENCIL_FFT, "tensor": _lib.FFTDOCK_PENCIL_TENSOR}
 
 
 @dataclass
@@ -39,6 +40,7 @@ class ScanConfig:
     ace_a: float = 0.6
     ace_cut: float = 6.0
     device: int = 0
+    pencil_mode: str = "auto"       # "auto", "fft" (CUDA-core x-FFTs) or "tensor" (tcgen05 GEMM form)
 
     @classmethod
     def from_options(cls, opts: dict, **kw):
@@ -93,6 +95,7 @@ class FFTScan:
         cfg.ace_b, cfg.ace_k, cfg.ace_a, cfg.ace_cut = (float(config.ace_b), float(config.ace_k),
                                                         float(config.ace_a), float(config.ace_cut))
         cfg.device = int(config.device)
+        cfg.pencil_mode = PENCIL_MODES[config.pencil_mode]
         h = C.c_void_p()
         rc = self.lib.fftdock_create(C.byref(cfg), C.byref(h))
         self._h = h
@@ -134,6 +137,14 @@ class FFTScan:
     @property
     def n_terms(self):
         return self.lib.fftdock_n_terms(self._h)
+
+    def info(self):
+        """Grid, terms, the pencil-stage form that runs, batch and ligand window."""
+        st = _lib.ScanInfo()
+        self._check(self.lib.fftdock_get_scan_info(self._h, C.byref(st)))
+        path = {_lib.FFTDOCK_PENCIL_FFT: "fft", _lib.FFTDOCK_PENCIL_TENSOR: "tensor"}[st.pencil_path]
+        return dict(grid_n=st.grid_n, n_terms=st.n_terms, pencil_path=path, rot_batch=st.rot_batch,
+                    n_entries=st.n_entries, window_x0=st.window_x0, window_w=st.window_w)
 
     # -- the scan -------------------------------------------------------------
     def set_receptor(self, xyz, types=None):

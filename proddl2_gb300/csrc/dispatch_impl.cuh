@@ -81,6 +81,14 @@ template <int N> struct SizeOpsImpl {
         return cudaGetLastError();
     }
 
+    template <bool PMAJOR, bool DBG>
+    static cudaError_t launch_plane(dim3 grid, size_t sm, const BatchArgs& a, cudaStream_t s) {
+        cudaError_t e = set_smem((const void*)plane_kernel<N, PMAJOR, DBG>, sm);
+        if (e != cudaSuccess) return e;
+        plane_kernel<N, PMAJOR, DBG><<<grid, 32 * G, sm, s>>>(a.g2, a.tw32, a.cand_v, a.cand_i, a.dbg_corr);
+        return cudaGetLastError();
+    }
+
     static cudaError_t scan_batch(const BatchArgs& a, cudaStream_t s) {
         Geo geo{a.h, a.zero_h, a.center0, N};
         const int nb = a.n_rot;
@@ -111,7 +119,7 @@ template <int N> struct SizeOpsImpl {
             const size_t sm2 = pencil_smem(a.K, a.n_ent);
             if ((e = set_smem((const void*)pencil_kernel<N>, sm2)) != cudaSuccess) return e;
             dim3 grid2(nb, a.PP / 32);
-            pencil_kernel<N><<<grid2, 32 * G, sm2, s>>>(a.spec, a.ent, a.offs, a.tw32, a.g2, a.K, a.PP, a.n_ent);
+            pencil_kernel<N><<<grid2, 32 * G, sm2, s>>>(a.spec, a.ent, a.offs, a.tw32, a.g2, a.K, a.n_ent);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
         }
         if (a.ev && (e = cudaEventRecord(a.ev[2], s)) != cudaSuccess) return e;
@@ -119,12 +127,13 @@ template <int N> struct SizeOpsImpl {
         const size_t sm3 = plane_smem();
         dim3 grid3(N, nb);
         if (pmajor) {
-            if ((e = set_smem((const void*)plane_kernel<N, true>, sm3)) != cudaSuccess) return e;
-            plane_kernel<N, true><<<grid3, 32 * G, sm3, s>>>(a.g2, a.tw32, a.cand_v, a.cand_i, a.PP, a.dbg_corr);
+            if (a.dbg_corr) e = launch_plane<true, true>(grid3, sm3, a, s);
+            else e = launch_plane<true, false>(grid3, sm3, a, s);
         } else {
-            if ((e = set_smem((const void*)plane_kernel<N, false>, sm3)) != cudaSuccess) return e;
-            plane_kernel<N, false><<<grid3, 32 * G, sm3, s>>>(a.g2, a.tw32, a.cand_v, a.cand_i, a.PP, a.dbg_corr);
+            if (a.dbg_corr) e = launch_plane<false, true>(grid3, sm3, a, s);
+            else e = launch_plane<false, false>(grid3, sm3, a, s);
         }
+        if (e != cudaSuccess) return e;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if (a.ev && (e = cudaEventRecord(a.ev[3], s)) != cudaSuccess) return e;
         // K4

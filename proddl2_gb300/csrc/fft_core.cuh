@@ -19,6 +19,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 namespace fftdock {
 
 // ---------------------------------------------------------------------------
@@ -139,13 +141,75 @@ template <int SIGN, int OFF, int STRIDE> struct Dft<4, SIGN, OFF, STRIDE> {
     }
 };
 
+// cos/sin(2 pi M / R) as constants evaluated by the compiler
+template <int M, int R> struct TwC {
+    static constexpr double c = cos2pi(M, R);
+    static constexpr double s = sin2pi(M, R);
+};
+
+// y * exp(SIGN 2 pi i M / R): quarter turns are swaps and sign flips, eighth
+// turns cost two adds and two multiplies, the rest a full complex multiply
+// (IEEE rules keep the compiler from dropping products with 0 and 1 itself)
+template <int SIGN, int M0, int R, typename C> __device__ __forceinline__ C twiddle_const(C y) {
+    using T = decltype(y.x);
+    constexpr int M = ((M0 % R) + R) % R;
+    if constexpr (M == 0) {
+        return y;
+    } else if constexpr ((4 * M) % R == 0) {
+        constexpr int q = (4 * M) / R;  // 1, 2, 3 quarter turns
+        if constexpr (q == 2) {
+            C r; r.x = -y.x; r.y = -y.y; return r;
+        } else if constexpr ((q == 1) == (SIGN > 0)) {
+            return mul_isign<+1>(y);
+        } else {
+            return mul_isign<-1>(y);
+        }
+    } else if constexpr ((8 * M) % R == 0) {
+        constexpr int e = (8 * M) / R;  // 1, 3, 5, 7 eighth turns
+        constexpr double h = 0.70710678118654752440084436210484903;
+        constexpr double cs = (e == 1 || e == 7) ? h : -h;
+        constexpr double sn = SIGN * ((e == 1 || e == 3) ? h : -h);
+        C r;
+        if constexpr ((cs > 0) == (sn > 0)) {  // s = c
+            r.x = (T)cs * (y.x - y.y);
+            r.y = (T)cs * (y.y + y.x);
+        } else {                               // s = -c
+            r.x = (T)cs * (y.x + y.y);
+            r.y = (T)cs * (y.y - y.x);
+        }
+        return r;
+    } else {
+        C w;
+        w.x = (T)TwC<M, R>::c;
+        w.y = (T)(SIGN * TwC<M, R>::s);
+        return cmul(y, w);
+    }
+}
+
 // odd prime radix by the symmetric direct formula
 template <int R, int SIGN, int OFF, int STRIDE> struct DftPrime {
+    static constexpr int H = (R - 1) / 2;
+    template <typename C, int K, int... Ns>
+    __device__ __forceinline__ static void out_k(const C* sp, const C* sm, C x0, C* out,
+                                                 std::integer_sequence<int, Ns...>) {
+        using T = decltype(x0.x);
+        C re = x0, im;
+        im.x = 0;
+        im.y = 0;
+        ((re = re + cscale(sp[Ns + 1], (T)TwC<((Ns + 1) * K) % R, R>::c)), ...);
+        ((im = im + cscale(sm[Ns + 1], (T)TwC<((Ns + 1) * K) % R, R>::s)), ...);
+        const C ji = mul_isign<SIGN>(im);
+        out[K] = re + ji;
+        out[R - K] = re - ji;
+    }
+    template <typename C, int... Ks>
+    __device__ __forceinline__ static void outs(const C* sp, const C* sm, C x0, C* out,
+                                                std::integer_sequence<int, Ks...>) {
+        (out_k<C, Ks + 1>(sp, sm, x0, out, std::make_integer_sequence<int, H>{}), ...);
+    }
     template <typename C> __device__ __forceinline__ static void run(C* v) {
-        using T = decltype(v[0].x);
-        constexpr int H = (R - 1) / 2;
         C sp[H + 1], sm[H + 1];
-        C x0 = v[OFF];
+        const C x0 = v[OFF];
         C tot = x0;
 #pragma unroll
         for (int n = 1; n <= H; ++n) {
@@ -154,20 +218,7 @@ template <int R, int SIGN, int OFF, int STRIDE> struct DftPrime {
             tot = tot + sp[n];
         }
         C out[R];
-#pragma unroll
-        for (int k = 1; k <= H; ++k) {
-            C re = x0, im; im.x = 0; im.y = 0;
-#pragma unroll
-            for (int n = 1; n <= H; ++n) {
-                const T c = (T)cos2pi((long)n * k, R);
-                const T s = (T)sin2pi((long)n * k, R);
-                re = re + cscale(sp[n], c);
-                im = im + cscale(sm[n], s);
-            }
-            C ji = mul_isign<SIGN>(im);
-            out[k] = re + ji;
-            out[R - k] = re - ji;
-        }
+        outs<C>(sp, sm, x0, out, std::make_integer_sequence<int, H>{});
         v[OFF] = tot;
 #pragma unroll
         for (int k = 1; k < R; ++k) v[OFF + k * STRIDE] = out[k];
@@ -190,29 +241,23 @@ template <int R, int SIGN, int OFF, int STRIDE> struct DftComposite {
             if constexpr (N1 + 1 < A) Sub<N1 + 1>::run(v);
         }
     };
+    // output column k1: twiddle Y_{n1}[k1] by w_R^(n1 k1), DFT_A over n1,
+    // X[k1 + B k2] = Z[k2]
+    template <typename C, int K1, int... N1s>
+    __device__ __forceinline__ static void column(const C* v, C* tmp, std::integer_sequence<int, N1s...>) {
+        C z[A] = {twiddle_const<SIGN, N1s * K1, R>(v[OFF + STRIDE * (A * K1 + N1s)])...};
+        Dft<A, SIGN, 0, 1>::run(z);
+        ((tmp[K1 + B * N1s] = z[N1s]), ...);
+    }
+    template <typename C, int... K1s>
+    __device__ __forceinline__ static void columns(const C* v, C* tmp, std::integer_sequence<int, K1s...>) {
+        (column<C, K1s>(v, tmp, std::make_integer_sequence<int, A>{}), ...);
+    }
     template <typename C> __device__ __forceinline__ static void run(C* v) {
-        using T = decltype(v[0].x);
         Sub<0>::run(v);
         // after the sub-DFTs, Y_{n1}[k1] sits at v[OFF + STRIDE*(A*k1 + n1)]
         C tmp[R];
-#pragma unroll
-        for (int k1 = 0; k1 < B; ++k1) {
-            C z[A];
-#pragma unroll
-            for (int n1 = 0; n1 < A; ++n1) {
-                C y = v[OFF + STRIDE * (A * k1 + n1)];
-                if (n1 * k1 != 0) {
-                    C w;
-                    w.x = (T)cos2pi((long)n1 * k1, R);
-                    w.y = (T)(SIGN * sin2pi((long)n1 * k1, R));
-                    y = cmul(y, w);
-                }
-                z[n1] = y;
-            }
-            Dft<A, SIGN, 0, 1>::run(z);
-#pragma unroll
-            for (int k2 = 0; k2 < A; ++k2) tmp[k1 + B * k2] = z[k2];
-        }
+        columns<C>(v, tmp, std::make_integer_sequence<int, B>{});
 #pragma unroll
         for (int k = 0; k < R; ++k) v[OFF + STRIDE * k] = tmp[k];
     }

@@ -386,7 +386,7 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
     const int N = c.grid_n;
     ctx->N = N;
     ctx->H = N / 2 + 1;
-    ctx->PP = ((N * ctx->H) + 31) / 32 * 32;
+    ctx->PP = fftdock::pencil_pitch(N);
     ctx->V = (size_t)N * N * N;
     ctx->B = c.rot_batch;
     // centred geometry exactly as UniformCubicGeometry(step, logicalSize)

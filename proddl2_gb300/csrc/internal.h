@@ -9,6 +9,9 @@
 
 namespace fftdock {
 
+// pencils per x-plane, N (N/2 + 1), rounded up to whole 32-lane tiles
+__host__ __device__ constexpr int pencil_pitch(int n) { return (n * (n / 2 + 1) + 31) / 32 * 32; }
+
 // Grid geometry of the reference's centred UniformCubicGeometry
 // (include/PRODDL/Grid/gridcoord.hpp:127-191).
 struct Geo {

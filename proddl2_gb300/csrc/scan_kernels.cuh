@@ -63,6 +63,9 @@ struct WarpTopK {
     __device__ __forceinline__ void init() { lv = INFINITY; li = 0x7fffffff; tv = INFINITY; ti = 0x7fffffff; }
     // offer one candidate per lane (all lanes of the warp must call)
     __device__ __forceinline__ void offer(float v, int idx, int lane) {
+        // v <= tv is necessary for (v, idx) < (tv, ti); the exact test runs
+        // only on the rare candidates
+        if (__ballot_sync(0xffffffffu, v <= tv) == 0u) return;
         unsigned mask = __ballot_sync(0xffffffffu, better(v, idx, tv, ti));
         while (mask) {
             const int src = __ffs(mask) - 1;
@@ -201,9 +204,10 @@ __global__ void __launch_bounds__(256) ligand_prep_kernel(
 template <int N>
 __global__ void __launch_bounds__(32 * SizeTraits<N>::G) pencil_kernel(
     const float2* __restrict__ spec, const uint32_t* __restrict__ ent, const int32_t* __restrict__ offs,
-    const float2* __restrict__ tw, float2* __restrict__ g2, int K, int PP, int n_ent) {
+    const float2* __restrict__ tw, float2* __restrict__ g2, int K, int n_ent) {
     using P = LinePlan<N, SizeTraits<N>::G>;
     constexpr int G = P::G, R1 = P::R1, H = N / 2 + 1;
+    constexpr int PP = pencil_pitch(N);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* xbuf = reinterpret_cast<float2*>(smem_raw);  // [2][N][32]
     float2* tws = xbuf + 2 * N * 32;                     // [N]
@@ -290,10 +294,11 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) pencil_kernel(
 // top-KC.  (FFTW c2r of FFTCorrelator::correlate + CorrelationProcessor::
 // selectIntoQueue, docking_fft.hpp:452-468.)
 // ---------------------------------------------------------------------------
-template <int N, bool PMAJOR>
+template <int N, bool PMAJOR, bool DBG>
 __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     const float2* __restrict__ g2, const float2* __restrict__ tw, float* __restrict__ cand_v,
-    int32_t* __restrict__ cand_i, int PP, float* __restrict__ dbg) {
+    int32_t* __restrict__ cand_i, float* __restrict__ dbg) {
+    constexpr int PP = pencil_pitch(N);
     using PC = LinePlan<N, SizeTraits<N>::G>;
     using PR = LinePlan<N / 2, SizeTraits<N>::GR>;
     constexpr int G = PC::G, R1 = PC::R1;
@@ -308,6 +313,8 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     float2* tws = plane + N * H;                          // [N]
     float* lv_s = reinterpret_cast<float*>(tws + N);      // [G*KC]
     int* li_s = reinterpret_cast<int*>(lv_s + G * KC);    // [G*KC]
+    __shared__ float thr_v[32];                           // each warp's current KC-th value
+    __shared__ int thr_i[32];
 
     const int x = blockIdx.x;
     const int q = blockIdx.y;
@@ -366,6 +373,12 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     }
     __syncthreads();
 
+    if (l == 0) {
+        thr_v[w] = INFINITY;
+        thr_i[w] = 0x7fffffff;
+    }
+    __syncthreads();
+
     // rows: C2R along kz via an N/2-point complex inverse DFT, then top-k
     const int gi = w / GR, m = w % GR;
     WarpTopK tk;
@@ -391,6 +404,20 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
             v[r] = yk;
         }
         __syncthreads();
+        // a value worse than any warp's KC-th best cannot be in the plane's
+        // top KC: filter with the best threshold published in earlier rounds
+        // (complete before the barrier above, rewritten only after the next)
+        if (ro > 0) {
+            float bv = tk.tv;
+            int bi = tk.ti;
+            for (int k = 0; k < G; ++k) {
+                const float ov = thr_v[k];
+                const int oi = thr_i[k];
+                if (better(ov, oi, bv, bi)) { bv = ov; bi = oi; }
+            }
+            tk.tv = bv;
+            tk.ti = bi;
+        }
         dft<R1R, +1>(v);
         if (valid) {
 #pragma unroll
@@ -408,14 +435,20 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
                 const float2 o = out[i * GR + r];
                 const float v0 = valid ? o.x : INFINITY;
                 const float v1 = valid ? o.y : INFINITY;
-                if (dbg != nullptr && valid) {
-                    float* d = dbg + (size_t)q * N * N * N + rowbase;
-                    d[2 * mm] = o.x;
-                    d[2 * mm + 1] = o.y;
+                if constexpr (DBG) {
+                    if (valid) {
+                        float* d = dbg + (size_t)q * N * N * N + rowbase;
+                        d[2 * mm] = o.x;
+                        d[2 * mm + 1] = o.y;
+                    }
                 }
                 tk.offer(v0, valid ? rowbase + 2 * mm : 0x7fffffff, l);
                 tk.offer(v1, valid ? rowbase + 2 * mm + 1 : 0x7fffffff, l);
             }
+        if (l == 0) {
+            thr_v[w] = tk.tv;
+            thr_i[w] = tk.ti;
+        }
     }
     if (l < KC) {
         lv_s[w * KC + l] = tk.lv;

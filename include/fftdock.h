@@ -203,6 +203,37 @@ int fftdock_profile(fftdock_ctx* ctx, int32_t enable);
 /* Synchronise the context's work and sum the recorded kernel times. */
 int fftdock_get_kernel_stats(fftdock_ctx* ctx, fftdock_kernel_stats* out);
 
+/* One docking pose of the gathered result: the reference's RotTranValue
+ * (include/PRODDL/types.hpp:80-84), a rotation applied first then a
+ * translation, with its score. */
+typedef struct fftdock_pose {
+    double value;
+    double rot[9];   /* row-major */
+    double t[3];
+} fftdock_pose;
+
+/* Foreman::run (include/PRODDL/docking_app.hpp:174-220): read the
+ * RotFftScanIO_Bin files in order, turn every translation t of a record with
+ * rotation R into the pose (R, t), keep the max_matches smallest values below
+ * 1e16 and return them ascending (ties in file order).  out holds max_matches
+ * poses; *n_out receives the count.  FFTDOCK_EIO on a missing file or a
+ * signature mismatch. */
+int fftdock_gather_records(const char* const* paths, int32_t n_paths, int32_t max_matches, fftdock_pose* out,
+                           int32_t* n_out);
+
+/* Same over a list file of record-file paths, one per line
+ * (RotFftScanIO_Collector, docking_io_bin.hpp:81-116). */
+int fftdock_gather_list(const char* list_path, int32_t max_matches, fftdock_pose* out, int32_t* n_out);
+
+/* Foreman::writeResults (docking_app.hpp:269-281): move each pose to the
+ * original frame, rec_frame^-1 * pose * lig_frame (docking_molstruct.hpp:
+ * 31-51; each frame is 12 doubles, row-major rotation then vector, NULL =
+ * identity), and write IORigid records (IO/rigid.hpp:115-176): binary
+ * [int32 2005052501][int32 n][n x float32 {value, euler[3], xyz[3]}] or, if
+ * text != 0, the reference's tab-separated text form. */
+int fftdock_write_rigid(const char* path, const fftdock_pose* poses, int32_t n, const double* rec_frame,
+                        const double* lig_frame, int32_t text);
+
 /* Append one RotFftScanIO_Bin record per rotation to `path`
  * (include/PRODDL/docking_io_bin.hpp:55-71): [int32 2014011401][3x3 double
  * rotation][size_t n][n x {double t[3], double value}]. */

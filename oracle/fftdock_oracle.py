@@ -528,3 +528,83 @@ def unpack_records(data):
         pos += 32 * n
         out.append((rot, vals[:, :3], vals[:, 3]))
     return out
+
+
+# ----------------------------------------------------------------------------
+# Rigid transforms: Geom/transformation.hpp:135-360 (row-major 3x3 + vector)
+# ----------------------------------------------------------------------------
+def mat_vec(m, v):
+    """blitz_ext::product (Blitz/bztinyvec.hpp:52-65): ((0 + m0 v0) + m1 v1) + m2 v2."""
+    return np.array([(m[i][0] * v[0] + m[i][1] * v[1]) + m[i][2] * v[2] for i in range(3)])
+
+
+def mat_mat(a, b):
+    """blitz_ext::product of two matrices, same accumulation order."""
+    return np.array([[(a[i][0] * b[0][j] + a[i][1] * b[1][j]) + a[i][2] * b[2][j] for j in range(3)]
+                     for i in range(3)])
+
+
+def rt_compose(a, b):
+    """RotationTranslation a * b = apply b, then a (transformation.hpp:300-305)."""
+    (ra, va), (rb, vb) = a, b
+    return mat_mat(ra, rb), mat_vec(ra, vb) + va
+
+
+def rt_inverse(a):
+    """RotationTranslation::inverse (transformation.hpp:336-338): the
+    transpose as rotation, then the negated vector: (R^T, R^T (0 - v))."""
+    r, v = a
+    rt = np.array(r).T
+    return rt, mat_vec(rt, 0.0 - np.asarray(v))
+
+
+def matrix_to_euler(m):
+    """Eu_xyz::rotMatrToEulerAng (Geom/euler.hpp:58-102), radians."""
+    half_pi = 4.0 * math.atan(1.0) / 2.0
+    if m[0][2] < 1.0:
+        if m[0][2] > -1.0:
+            a0 = math.atan2(-m[1][2], m[2][2])
+            a1 = math.asin(m[0][2])
+            a2 = math.atan2(-m[0][1], m[0][0])
+        else:
+            a0 = -math.atan2(m[1][0], m[1][1])
+            a1 = -half_pi
+            a2 = 0.0
+    else:
+        a0 = math.atan2(m[1][0], m[1][1])
+        a1 = half_pi
+        a2 = 0.0
+    return np.array([-a2, -a0, -a1])
+
+
+# ----------------------------------------------------------------------------
+# Gather: Foreman::run (docking_app.hpp:174-220) + writeResults (:269-281)
+# ----------------------------------------------------------------------------
+def gather_records(records, max_matches):
+    """records: iterable of (rot 3x3, translations (n,3), values (n,)) in file
+    order.  Each translation t becomes Translation(t) * rot = (rot, t); the
+    max_matches smallest values below 1e16 are kept and returned ascending
+    as (value, rot, t) (ties in arrival order)."""
+    q = BoundPriorityQueue(max_matches, (1e16, -1), key=lambda e: (e[0], e[3]))
+    seq = 0
+    for rot, trans, vals in records:
+        for t, v in zip(trans, vals):
+            q.push((float(v), np.asarray(rot, dtype=np.float64), np.asarray(t, dtype=np.float64), seq))
+            seq += 1
+    return [(v, r, t) for v, r, t, _ in q.sort()]
+
+
+RIGID_SIGNATURE = 2005052501
+
+
+def pack_rigid(poses, rec_frame, lig_frame):
+    """IORigid::writeCoords binary form (IO/rigid.hpp:115-146) of poses moved
+    to the original frame, tR^-1 * pose * tL (docking_molstruct.hpp:31-51):
+    [int32 signature][int32 n][n x float32 {value, euler[3], xyz[3]}]."""
+    inv_r = rt_inverse(rec_frame)
+    out = struct.pack("<ii", RIGID_SIGNATURE, len(poses))
+    for v, r, t in poses:
+        rr, tt = rt_compose(rt_compose(inv_r, (r, t)), lig_frame)
+        ang = matrix_to_euler(rr)
+        out += struct.pack("<7f", v, *ang, *tt)
+    return out

@@ -80,6 +80,15 @@ class ScanInfo(C.Structure):
                 ("window_w", C.c_int32)]
 
 
+class Pose(C.Structure):
+    _fields_ = [("value", C.c_double), ("rot", C.c_double * 9), ("t", C.c_double * 3)]
+
+
+def pose_dtype():
+    import numpy as np
+    return np.dtype([("value", "<f8"), ("rot", "<f8", (9,)), ("t", "<f8", (3,))])
+
+
 # numpy view of fftdock_peak
 def peak_dtype():
     import numpy as np
@@ -108,6 +117,9 @@ SIGNATURES = {
     "fftdock_scan_candidates": (C.c_int, [_P, C.c_int32, _P, _P, _P]),
     "fftdock_profile": (C.c_int, [_P, C.c_int32]),
     "fftdock_get_kernel_stats": (C.c_int, [_P, C.POINTER(KernelStats)]),
+    "fftdock_gather_records": (C.c_int, [C.POINTER(C.c_char_p), C.c_int32, C.c_int32, _P, C.POINTER(C.c_int32)]),
+    "fftdock_gather_list": (C.c_int, [C.c_char_p, C.c_int32, _P, C.POINTER(C.c_int32)]),
+    "fftdock_write_rigid": (C.c_int, [C.c_char_p, _P, C.c_int32, _P, _P, C.c_int32]),
     "fftdock_write_scan_records": (C.c_int, [C.c_char_p, C.c_int32, _P, C.c_int32, _P, _P, C.c_int32]),
 }
 

@@ -61,7 +61,7 @@ def _compile(src: Path, extra):
 def build(verbose=False, extra_flags=(), jobs=None):
     """Compile and link; returns the library path."""
     BUILD.mkdir(exist_ok=True)
-    srcs = sorted(CSRC.glob("*.cu"))
+    srcs = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
     jobs = jobs or min(len(srcs), os.cpu_count() or 4)
     errors = []
     objs = []

@@ -179,3 +179,43 @@ def test_select_minima_queue_semantics():
     assert list(offs) == q.sort()
     assert np.all(vals < -2.5)
     assert np.all(np.diff(vals) >= 0)
+
+
+def test_transform_algebra_matches_reference_test():
+    # src/PRODDL/Geom/test_transformation.cpp:20-50
+    cm = np.array([5.0, 4.0, 3.0])
+    v_trans = np.array([1.0, 2.0, 3.0])
+    m1 = np.array([[0, 1, 1], [0.2, 0.3, 0.4], [1, 0.3, 0.5]])
+    m2 = np.array([[0.4, 1.7, 1.8], [0.7, 0.9, 0.3], [1.3, 0.1, 0.9]])
+    ident = np.eye(3)
+    zero = np.zeros(3)
+    # Rot(m2) * Tran(cm + v) * (Rot(m1) * Tran(0 - cm)), then inverse
+    inner = O.rt_compose((m1, zero), (ident, 0.0 - cm))
+    rt = O.rt_compose((m2, zero), O.rt_compose((ident, cm + v_trans), inner))
+    r, v = O.rt_inverse(rt)
+    assert np.allclose(r, [[2.14, 0.48, 0.92], [1.45, 1.06, 1.6], [1.98, 1.21, 1.79]])
+    assert np.allclose(v, [-0.2324, 1.5222, 1.3322])
+
+
+def test_euler_round_trip():
+    rng = np.random.default_rng(2)
+    for _ in range(20):
+        ang = rng.uniform(-1.4, 1.4, 3)
+        m = O.euler_to_matrix(ang)
+        # rotMatrToEulerAng inverts eulerAngToRotMatr (with its angle order swap)
+        m2 = O.euler_to_matrix(O.matrix_to_euler(m))
+        assert np.allclose(m, m2, atol=1e-12)
+
+
+def test_gather_keeps_smallest_ascending():
+    rng = np.random.default_rng(4)
+    recs = []
+    for i in range(6):
+        rot = O.euler_to_matrix(rng.uniform(-1, 1, 3))
+        n = int(rng.integers(0, 5))
+        recs.append((rot, rng.normal(size=(n, 3)), rng.normal(size=n)))
+    allv = sorted(v for _, _, vals in recs for v in vals)
+    out = O.gather_records(recs, 7)
+    assert [p[0] for p in out] == allv[:7]
+    blob = O.pack_rigid(out, (np.eye(3), np.zeros(3)), (np.eye(3), np.zeros(3)))
+    assert len(blob) == 8 + 28 * len(out)

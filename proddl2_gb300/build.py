@@ -18,6 +18,8 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libfftdock.so"
+CLI = PKG / "fftdock-scan"
+CLI_MAIN = CSRC / "fftdock_scan_main.cpp"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
@@ -61,7 +63,7 @@ def _compile(src: Path, extra):
 def build(verbose=False, extra_flags=(), jobs=None):
     """Compile and link; returns the library path."""
     BUILD.mkdir(exist_ok=True)
-    srcs = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
+    srcs = sorted(CSRC.glob("*.cu")) + sorted(p for p in CSRC.glob("*.cpp") if p != CLI_MAIN)
     jobs = jobs or min(len(srcs), os.cpu_count() or 4)
     errors = []
     objs = []
@@ -77,8 +79,15 @@ def build(verbose=False, extra_flags=(), jobs=None):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
+    # command-line front end, linked against the library beside it
+    if not CLI.exists() or CLI.stat().st_mtime < max(LIB.stat().st_mtime, CLI_MAIN.stat().st_mtime):
+        cmd = [nvcc(), "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(CLI_MAIN), "-o", str(CLI),
+               "-L", str(PKG), "-lfftdock", "-Xlinker", "-rpath=$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("fftdock-scan link failed:\n%s\n%s" % (r.stdout, r.stderr))
     if verbose:
-        print("built", LIB)
+        print("built", LIB, "and", CLI)
     return LIB
 
 

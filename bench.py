@@ -50,6 +50,8 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--n-rot", type=int, default=0, help="scan only this many rotations per step (profiling runs)")
     p.add_argument("--pencil", default="auto", choices=["auto", "fft", "tensor"])
+    p.add_argument("--precision", default="fp32", choices=["fp32", "bf16"],
+                   help="receptor spectra storage (bf16: the precision-study mode)")
     return p.parse_args()
 
 
@@ -252,7 +254,8 @@ def run_ours(args):
     pair = synth.make_pair(w["n_rec"], w["n_lig"], w["n_rot"], seed=1)
     n_rot = w["n_rot"]
     cfg = ScanConfig(grid_n=w["grid_n"], grid_step=w["grid_step"], term_set=w["term_set"], peaks_per_rot=w["peaks"],
-                     rot_batch=w["rot_batch"], ace_matrix=pair.ace, device=local, pencil_mode=args.pencil)
+                     rot_batch=w["rot_batch"], ace_matrix=pair.ace, device=local, pencil_mode=args.pencil,
+                     precision=args.precision)
     scan = FFTScan(cfg)
     t0 = time.perf_counter()
     scan.set_receptor(pair.receptor.xyz, pair.receptor.ace_type)
@@ -391,6 +394,7 @@ def run_ours(args):
                    "pencil_stage": info["pencil_path"],
                    "precision": ("split-FP16 tcgen05 GEMM with FP32 accumulation (hi*hi+hi*lo+lo*hi) for the x stage, "
                                  "FP32 FFTs elsewhere" if info["pencil_path"] == "tensor" else "FP32 FFTs")
+                                + (", BF16-stored receptor spectra" if args.precision == "bf16" else "")
                                 + ", FP64 direct-space rescoring of 16 candidates"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": gpu_launches,

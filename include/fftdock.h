@@ -55,9 +55,13 @@ enum {
     FFTDOCK_TERMS_SHAPE_ACE = 2  /* shape + n_types ACE-style desolvation grids, folded to K = n_types */
 };
 
-/* precision of the stored receptor spectra */
+/* precision of the stored receptor spectra (FFT pencil stage): FP32 pairs,
+ * or BF16 pairs widened to FP32 for the spectrum product (half the
+ * spectrum memory and traffic; candidate values then carry BF16-level
+ * error, and the FP64 rescoring still fixes the reported scores) */
 enum {
-    FFTDOCK_PREC_FP32 = 0
+    FFTDOCK_PREC_FP32 = 0,
+    FFTDOCK_PREC_BF16_SPECTRA = 1
 };
 
 /* how the per-pencil x stage (x transforms and the spectrum product summed

@@ -28,6 +28,7 @@ STATUS_NAMES = {
 FFTDOCK_TERMS_SHAPE = 1
 FFTDOCK_TERMS_SHAPE_ACE = 2
 FFTDOCK_PREC_FP32 = 0
+FFTDOCK_PREC_BF16_SPECTRA = 1
 FFTDOCK_PENCIL_AUTO = 0
 FFTDOCK_PENCIL_FFT = 1
 FFTDOCK_PENCIL_TENSOR = 2

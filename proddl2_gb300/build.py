@@ -81,7 +81,8 @@ def build(verbose=False, extra_flags=(), jobs=None):
             raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
     # command-line front end, linked against the library beside it
     if not CLI.exists() or CLI.stat().st_mtime < max(LIB.stat().st_mtime, CLI_MAIN.stat().st_mtime):
-        cmd = [nvcc(), "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(CLI_MAIN), "-o", str(CLI),
+        cmd = [nvcc(), "-O2", "-std=c++17", "-Xcompiler", "-ffp-contract=off", "-I", str(ROOT / "include"),
+               str(CLI_MAIN), "-o", str(CLI),
                "-L", str(PKG), "-lfftdock", "-Xlinker", "-rpath=$ORIGIN"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

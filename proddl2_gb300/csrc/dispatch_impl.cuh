@@ -51,7 +51,7 @@ template <int N> struct SizeOpsImpl {
     }
 
     static cudaError_t receptor_fft(const double* rgrid_t, double2* cbuf, double2* hbuf, const double2* tw64,
-                                    float2* spec_t, int PP, float2* circ_t, cudaStream_t s) {
+                                    void* spec_t, int spec_bf16, int PP, float2* circ_t, cudaStream_t s) {
         const size_t V = (size_t)N * N * N;
         complexify_kernel<<<(unsigned)((V + 255) / 256), 256, 0, s>>>(rgrid_t, cbuf, V);
         cudaError_t e = cudaGetLastError();
@@ -76,8 +76,22 @@ template <int N> struct SizeOpsImpl {
         e = line_fft<double, -1>(hbuf, tw64, (long)N * H, (long)N * H, (long)N * H, 1, 0, s);
         if (e != cudaSuccess) return e;
         const size_t tot = (size_t)N * PP;
-        pack_spectrum_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(hbuf, spec_t, N, N * H, PP,
-                                                                         1.0 / (double)V);
+        if (spec_bf16)
+            pack_spectrum_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(
+                hbuf, static_cast<__nv_bfloat162*>(spec_t), N, N * H, PP, 1.0 / (double)V);
+        else
+            pack_spectrum_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(
+                hbuf, static_cast<float2*>(spec_t), N, N * H, PP, 1.0 / (double)V);
+        return cudaGetLastError();
+    }
+
+    template <typename SpecT> static cudaError_t launch_pencil(const BatchArgs& a, int nb, cudaStream_t s) {
+        const size_t sm2 = pencil_smem(a.K, a.n_ent);
+        cudaError_t e = set_smem((const void*)pencil_kernel<N, SpecT>, sm2);
+        if (e != cudaSuccess) return e;
+        dim3 grid2(nb, a.PP / 32);
+        pencil_kernel<N, SpecT><<<grid2, 32 * G, sm2, s>>>(static_cast<const SpecT*>(a.spec), a.ent, a.offs,
+                                                           a.tw32, a.g2, a.K, a.n_ent);
         return cudaGetLastError();
     }
 
@@ -116,11 +130,8 @@ template <int N> struct SizeOpsImpl {
             }
         }
         if (!pmajor) {
-            const size_t sm2 = pencil_smem(a.K, a.n_ent);
-            if ((e = set_smem((const void*)pencil_kernel<N>, sm2)) != cudaSuccess) return e;
-            dim3 grid2(nb, a.PP / 32);
-            pencil_kernel<N><<<grid2, 32 * G, sm2, s>>>(a.spec, a.ent, a.offs, a.tw32, a.g2, a.K, a.n_ent);
-            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            e = a.spec_bf16 ? launch_pencil<__nv_bfloat162>(a, nb, s) : launch_pencil<float2>(a, nb, s);
+            if (e != cudaSuccess) return e;
         }
         if (a.ev && (e = cudaEventRecord(a.ev[2], s)) != cudaSuccess) return e;
         // K3

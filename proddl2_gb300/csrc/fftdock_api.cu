@@ -50,7 +50,7 @@ struct fftdock_ctx {
 
     float2* tw32 = nullptr;
     double2* tw64 = nullptr;
-    float2* spec = nullptr;
+    void* spec = nullptr;       // float2 or __nv_bfloat162 pairs (cfg.precision)
     double* rgrid = nullptr;
     double* emat = nullptr;
 
@@ -151,6 +151,7 @@ BatchArgs batch_args(fftdock_ctx* ctx) {
     a.lig_xyz = ctx->lig_xyz;
     a.lig_term = ctx->lig_term;
     a.spec = ctx->spec;
+    a.spec_bf16 = ctx->cfg.precision == FFTDOCK_PREC_BF16_SPECTRA ? 1 : 0;
     a.rgrid = ctx->rgrid;
     a.tw32 = ctx->tw32;
     a.n_ent = ctx->n_ent;
@@ -358,7 +359,8 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
         return fail(ctx, FFTDOCK_EINVAL, "peaks_per_rot must be in [1, 16]");
     if (c.max_trans_inp < 1) return fail(ctx, FFTDOCK_EINVAL, "max_trans_inp must be >= 1");
     if (c.rot_batch < 1 || c.rot_batch > 1024) return fail(ctx, FFTDOCK_EINVAL, "rot_batch must be in [1, 1024]");
-    if (c.precision != FFTDOCK_PREC_FP32) return fail(ctx, FFTDOCK_EUNSUPPORTED, "precision mode not built");
+    if (c.precision != FFTDOCK_PREC_FP32 && c.precision != FFTDOCK_PREC_BF16_SPECTRA)
+        return fail(ctx, FFTDOCK_EUNSUPPORTED, "precision mode not built");
     if (std::isnan(c.max_val_corr)) return fail(ctx, FFTDOCK_EINVAL, "max_val_corr is NaN");
     if (c.pencil_mode < FFTDOCK_PENCIL_AUTO || c.pencil_mode > FFTDOCK_PENCIL_TENSOR)
         return fail(ctx, FFTDOCK_EINVAL, "unknown pencil_mode");
@@ -424,7 +426,12 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
         CK(dalloc(&ctx->emat, ctx->ace.size()));
         CK(cudaMemcpy(ctx->emat, ctx->ace.data(), ctx->ace.size() * sizeof(double), cudaMemcpyHostToDevice));
     }
-    CK(dalloc(&ctx->spec, (size_t)ctx->K * N * ctx->PP));
+    {
+        const size_t elem = c.precision == FFTDOCK_PREC_BF16_SPECTRA ? 4 : 8;
+        unsigned char* sp = nullptr;
+        CK(dalloc(&sp, (size_t)ctx->K * N * ctx->PP * elem));
+        ctx->spec = sp;
+    }
     CK(dalloc(&ctx->rgrid, (size_t)ctx->K * ctx->V));
     CK(dalloc(&ctx->offs, (size_t)ctx->B * (ctx->K * N + 1)));
     CK(dalloc(&ctx->g2, (size_t)ctx->B * N * ctx->PP));
@@ -514,8 +521,10 @@ int fftdock_set_receptor(fftdock_ctx* ctx, int32_t n, const double* xyz, const i
     CKR(dalloc(&cbuf, V));
     CKR(dalloc(&hbuf, (size_t)N * N * ctx->H));
     for (int t = 0; t < ctx->K; ++t) {
+        const size_t elem = c.precision == FFTDOCK_PREC_BF16_SPECTRA ? 4 : 8;
         CKR(ctx->ops->receptor_fft(ctx->rgrid + (size_t)t * V, cbuf, hbuf, ctx->tw64,
-                                   ctx->spec + (size_t)t * N * ctx->PP, ctx->PP,
+                                   static_cast<unsigned char*>(ctx->spec) + (size_t)t * N * ctx->PP * elem,
+                                   c.precision == FFTDOCK_PREC_BF16_SPECTRA ? 1 : 0, ctx->PP,
                                    ctx->use_tc ? ctx->circ + (size_t)t * N * ctx->H * N : nullptr, s));
     }
     if (ctx->use_tc) CKR(ctx->ops->circ_scales(ctx->circ, ctx->K, ctx->cscale, s));

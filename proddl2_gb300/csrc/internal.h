@@ -45,7 +45,8 @@ struct BatchArgs {
     const double* rot;          // [B][9]
     const double* lig_xyz;      // [n_ent][3]
     const int32_t* lig_term;    // [n_ent]
-    const float2* spec;         // [K][N][PP]
+    const void* spec;           // [K][N][PP] float2, or __nv_bfloat162 when spec_bf16
+    int spec_bf16;
     const double* rgrid;        // [K][N^3]
     const float2* tw32;         // [N]
     int n_rot;                  // rotations in this batch (<= B)
@@ -83,7 +84,7 @@ struct SizeOps {
     int n;
     // forward 3-D FFT of one real FP64 term grid into spec_t ([N][PP], scaled 1/V)
     cudaError_t (*receptor_fft)(const double* rgrid_t, double2* cbuf, double2* hbuf, const double2* tw64,
-                                float2* spec_t, int PP, float2* circ_t, cudaStream_t s);
+                                void* spec_t, int spec_bf16, int PP, float2* circ_t, cudaStream_t s);
     // per-pencil scale exponents of the circulant samples (tensor path)
     cudaError_t (*circ_scales)(const float2* circ, int K, int8_t* cscale, cudaStream_t s);
     bool has_tc;

@@ -13,6 +13,7 @@
 //   cand  [B][N][KC]           per-plane FP32 candidate pools
 #pragma once
 
+#include <cuda_bf16.h>
 #include <math.h>
 #include <stdint.h>
 
@@ -201,9 +202,12 @@ __global__ void __launch_bounds__(256) ligand_prep_kernel(
 // (FFTCorrelator::correlate, docking_fft.hpp:622-633, summed over terms as
 // MolForceComp::collectTotal does in real space, docking_molforce.hpp:172-184.)
 // ---------------------------------------------------------------------------
-template <int N>
+__device__ __forceinline__ float2 spec_load(const float2* p) { return __ldg(p); }
+__device__ __forceinline__ float2 spec_load(const __nv_bfloat162* p) { return __bfloat1622float2(*p); }
+
+template <int N, typename SpecT>
 __global__ void __launch_bounds__(32 * SizeTraits<N>::G) pencil_kernel(
-    const float2* __restrict__ spec, const uint32_t* __restrict__ ent, const int32_t* __restrict__ offs,
+    const SpecT* __restrict__ spec, const uint32_t* __restrict__ ent, const int32_t* __restrict__ offs,
     const float2* __restrict__ tw, float2* __restrict__ g2, int K, int n_ent) {
     using P = LinePlan<N, SizeTraits<N>::G>;
     constexpr int G = P::G, R1 = P::R1, H = N / 2 + 1;
@@ -255,13 +259,13 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) pencil_kernel(
         __syncthreads();
         float2 F[R1];
         line_pass2<P, -1, 1, 32>(buf, w, l, tws, F);
-        const float2* sp = spec + (size_t)t * N * PP + p;
+        const SpecT* sp = spec + (size_t)t * N * PP + p;
 #pragma unroll
         for (int i = 0; i < P::NB; ++i)
 #pragma unroll
             for (int r = 0; r < G; ++r) {
                 const int kx = w + G * i + R1 * r;
-                const float2 rv = __ldg(sp + (size_t)kx * PP);
+                const float2 rv = spec_load(sp + (size_t)kx * PP);
                 const float2 f = F[i * G + r];
                 S[i * G + r].x += f.x * rv.x + f.y * rv.y;
                 S[i * G + r].y += f.y * rv.x - f.x * rv.y;
@@ -617,20 +621,25 @@ static __global__ void half_extract_kernel(const double2* __restrict__ full, dou
     half[i] = full[row * n + kz];
 }
 
-// [N][N*H] double -> [N][PP] float scaled by 1/V
-static __global__ void pack_spectrum_kernel(const double2* __restrict__ half, float2* __restrict__ spec, int n, int nh,
+__device__ __forceinline__ void spec_store(float2* p, float x, float y) { *p = make_float2(x, y); }
+__device__ __forceinline__ void spec_store(__nv_bfloat162* p, float x, float y) { *p = __floats2bfloat162_rn(x, y); }
+
+// [N][N*H] double -> [N][PP] FP32 or BF16 pairs scaled by 1/V
+template <typename SpecT>
+static __global__ void pack_spectrum_kernel(const double2* __restrict__ half, SpecT* __restrict__ spec, int n, int nh,
                                      int pp, double scale) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t tot = (size_t)n * pp;
     if (i >= tot) return;
     const size_t kx = i / pp;
     const int p = (int)(i - kx * pp);
-    float2 o = make_float2(0.f, 0.f);
+    float ox = 0.f, oy = 0.f;
     if (p < nh) {
         const double2 v = half[kx * nh + p];
-        o = make_float2((float)(v.x * scale), (float)(v.y * scale));
+        ox = (float)(v.x * scale);
+        oy = (float)(v.y * scale);
     }
-    spec[i] = o;
+    spec_store(spec + i, ox, oy);
 }
 
 }  // namespace fftdock

@@ -41,6 +41,7 @@ class ScanConfig:
     ace_cut: float = 6.0
     device: int = 0
     pencil_mode: str = "auto"       # "auto", "fft" (CUDA-core x-FFTs) or "tensor" (tcgen05 GEMM form)
+    precision: str = "fp32"         # receptor spectra: "fp32" or "bf16"
 
     @classmethod
     def from_options(cls, opts: dict, **kw):
@@ -96,6 +97,7 @@ class FFTScan:
                                                         float(config.ace_a), float(config.ace_cut))
         cfg.device = int(config.device)
         cfg.pencil_mode = PENCIL_MODES[config.pencil_mode]
+        cfg.precision = {"fp32": _lib.FFTDOCK_PREC_FP32, "bf16": _lib.FFTDOCK_PREC_BF16_SPECTRA}[config.precision]
         h = C.c_void_p()
         rc = self.lib.fftdock_create(C.byref(cfg), C.byref(h))
         self._h = h

@@ -52,6 +52,11 @@ def parse_args():
     p.add_argument("--pencil", default="auto", choices=["auto", "fft", "tensor"])
     p.add_argument("--precision", default="fp32", choices=["fp32", "bf16"],
                    help="receptor spectra storage (bf16: the precision-study mode)")
+    p.add_argument("--cluster", action="store_true",
+                   help="translational clustering of each rotation's queue (doClusterTranslations)")
+    p.add_argument("--cluster-queue", type=int, default=0,
+                   help="queue bound with --cluster (maxNTransInp; default: the reference's maxNTrans * 100)")
+    p.add_argument("--cluster-radius", type=float, default=5.0, help="clusterRadiusTrans with --cluster")
     return p.parse_args()
 
 
@@ -227,7 +232,9 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded globules, uniform quaternion rotations)",
-        "config": {"workload": workload_desc(w), "mode": "exhaustive", "sample_rotations_per_step": per_step},
+        "config": {"workload": workload_desc(w),
+                   "mode": ("exhaustive, translational clustering of a %d-cell queue per rotation (radius %g A)"
+                            % (queue, args.cluster_radius)) if args.cluster else "exhaustive", "sample_rotations_per_step": per_step},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -253,9 +260,11 @@ def run_ours(args):
         w["n_rot"] = args.n_rot
     pair = synth.make_pair(w["n_rec"], w["n_lig"], w["n_rot"], seed=1)
     n_rot = w["n_rot"]
+    queue = (args.cluster_queue or 100 * w["peaks"]) if args.cluster else 10000
     cfg = ScanConfig(grid_n=w["grid_n"], grid_step=w["grid_step"], term_set=w["term_set"], peaks_per_rot=w["peaks"],
                      rot_batch=w["rot_batch"], ace_matrix=pair.ace, device=local, pencil_mode=args.pencil,
-                     precision=args.precision)
+                     precision=args.precision, cluster_trans=args.cluster, max_trans_inp=queue,
+                     cluster_radius=args.cluster_radius)
     scan = FFTScan(cfg)
     t0 = time.perf_counter()
     scan.set_receptor(pair.receptor.xyz, pair.receptor.ace_type)
@@ -332,7 +341,10 @@ def run_ours(args):
     k_terms = info["n_terms"]
     batch = info["rot_batch"]
     avg_launch_ms = pencil_ms / max(launches, 1)
-    gpu_launches = sum(v[0] for v in kstats.values())
+    # one timed stage is one kernel, except the queue + clustering stage:
+    # init, 6 x (digit pass + pick), gather, finish
+    per_stage = {"finalize": 15 if args.cluster else 1}
+    gpu_launches = sum(v[0] * per_stage.get(k, 1) for k, v in kstats.items())
     total_kernel_ms = sum(v[1] for v in kstats.values())
     share = pencil_ms / total_kernel_ms if total_kernel_ms else None
     n = w["grid_n"]
@@ -386,7 +398,9 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32",
         "data": "synthetic (seeded globules, uniform quaternion rotations)",
-        "config": {"workload": workload_desc(w), "mode": "exhaustive",
+        "config": {"workload": workload_desc(w),
+                   "mode": ("exhaustive, translational clustering of a %d-cell queue per rotation (radius %g A)"
+                            % (queue, args.cluster_radius)) if args.cluster else "exhaustive",
                    "parallelism": "replicas" if world == 1 else "rotation sets per rank (replicas)",
                    "l2": "inputs larger than L2: %.0f MB receptor spectra + %.0f MB x-planes per batch"
                          % (k_terms * n * n * (n // 2 + 1) * 8 / 1e6, batch * n * n * (n // 2 + 1) * 8 / 1e6),

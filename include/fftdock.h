@@ -76,6 +76,24 @@ enum {
     FFTDOCK_PENCIL_TENSOR = 2   /* circular correlation as split-FP16 tcgen05 GEMMs, FP32 accumulate */
 };
 
+/* translational clustering of each rotation's queue ("doClusterTranslations",
+ * TranClust, include/PRODDL/docking_fft.hpp:30-140 over ClusterMatrix,
+ * include/PRODDL/Geom/cluster.hpp:121-477).  With clustering on, the scan
+ * keeps the exact max_trans_inp lowest cells of every rotation (at most
+ * FFTDOCK_MAX_QUEUE_CLUSTERED), walks them in the chosen order and makes a
+ * cell a cluster leader unless it lies within the neighbour radius of an
+ * earlier leader; the first peaks_per_rot leaders are the rotation's peaks,
+ * in walk order.  The reference's walk starts from the queue's worst value
+ * (its density is overridden by the weight -value and sorted ascending,
+ * cluster.hpp:238-253); BEST_FIRST walks from the best value instead.  The
+ * neighbour radius tested is sqrt(3) * cluster_radius, as in the reference
+ * (three clustered columns). */
+enum {
+    FFTDOCK_CLUSTER_ORDER_REFERENCE = 0,
+    FFTDOCK_CLUSTER_ORDER_BEST_FIRST = 1
+};
+#define FFTDOCK_MAX_QUEUE_CLUSTERED 16384
+
 typedef struct fftdock_config {
     int32_t struct_size;         /* sizeof(fftdock_config) */
     int32_t grid_n;              /* FFT grid edge N (cubic); see fftdock_supported_grid() */
@@ -94,6 +112,9 @@ typedef struct fftdock_config {
     double ace_b, ace_k, ace_a;  /* sigmoid 1/(1+exp(b(k r - a))) (potentials_inc.hpp:394-397) */
     double ace_cut;              /* cutoff of the desolvation field (A) */
     int32_t pencil_mode;         /* FFTDOCK_PENCIL_* */
+    int32_t cluster_trans;       /* 1: cluster each rotation's queue ("doClusterTranslations") */
+    int32_t cluster_order;       /* FFTDOCK_CLUSTER_ORDER_* */
+    double cluster_radius;       /* "clusterRadiusTrans" (A), reference default 5 */
 } fftdock_config;
 
 /* one selected translation; the reference's TranValue
@@ -187,7 +208,8 @@ int fftdock_get_receptor_grid(fftdock_ctx* ctx, int32_t term, double* out);
 int fftdock_correlation_grid(fftdock_ctx* ctx, const double* rot, float* out);
 
 /* Diagnostic: per-rotation FP32 candidate pool (16 smallest values and their
- * flat offsets, ascending) before FP64 rescoring. */
+ * flat offsets, ascending) before FP64 rescoring.  FFTDOCK_EUNSUPPORTED on a
+ * clustering context (cluster_trans), which keeps no such pool. */
 int fftdock_scan_candidates(fftdock_ctx* ctx, int32_t n_rot, const double* rot,
                             float* values, int32_t* offsets);
 

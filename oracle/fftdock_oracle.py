@@ -492,6 +492,90 @@ def scan_rotation(geom, rec_grids, rec_spectra, lig_xyz, lig_weights, rot, k, ma
 
 
 # ----------------------------------------------------------------------------
+# Translational clustering: TranClust (docking_fft.hpp:30-140) over
+# ClusterMatrix::cluster / getClusters (Geom/cluster.hpp:121-477)
+# ----------------------------------------------------------------------------
+CLUSTER_ORDER_REFERENCE = 0
+CLUSTER_ORDER_BEST_FIRST = 1
+
+
+def cluster_radius2(radius, n_cols=3):
+    """Squared neighbour radius the reference ends up testing against:
+    cutoff2 = r^2 * n_cols, cutoff = sqrt(cutoff2), and the sphere iterator
+    compares with cutoff * cutoff (cluster.hpp:153-156,
+    partpoints.hpp:551-562)."""
+    c2 = (radius * radius) * float(n_cols)
+    c = math.sqrt(c2)
+    return c * c
+
+
+def cluster_leaders(rows, radius, max_out, walk):
+    """``ClusterMatrix::cluster`` leader pass (cluster.hpp:268-338) over the
+    rows in ``walk`` order: a row within the neighbour radius (squared
+    distance summed column by column, ``<= cluster_radius2``) of an earlier
+    leader joins it, otherwise it becomes a leader.  Stops after ``max_out``
+    leaders (the later leaders cannot change the earlier ones).  Returns the
+    leaders' row indexes in walk order, as ``getClusters`` lists them."""
+    m = np.asarray(rows, dtype=np.float64)
+    if m.shape[0] == 0:
+        return np.zeros(0, dtype=np.int64)
+    m = m.reshape(m.shape[0], -1)
+    rad2 = cluster_radius2(radius, m.shape[1])
+    leaders = []
+    for i in walk:
+        if len(leaders) >= max_out:
+            break
+        covered = False
+        for j in leaders:
+            d2 = 0.0
+            for c in range(m.shape[1]):
+                d = m[i, c] - m[j, c]
+                d2 = d2 + d * d
+            if d2 <= rad2:
+                covered = True
+                break
+        if not covered:
+            leaders.append(int(i))
+    return np.asarray(leaders, dtype=np.int64)
+
+
+def tran_cluster(translations, values, radius, max_out, order=CLUSTER_ORDER_REFERENCE):
+    """TranClust::process on one rotation's queue output.
+
+    ``translations`` (n, 3) and ``values`` (n,) are the queue's entries in
+    ascending (value, offset) order.  The reference sets every row's weight
+    to ``-value`` and then its density to that weight (the ``dens = weights``
+    override at cluster.hpp:238), sorts rows by ascending density -- the
+    least negative value, i.e. the worst score, first -- and walks them in
+    that order (:func:`cluster_leaders`); ``getClusters`` lists the leaders
+    in walk order and ``TranClust::process`` keeps the first ``max_out``.
+    The reference's ``std::sort`` leaves the order of equal densities
+    unspecified; here equal values are walked from the higher queue position
+    down (the queue list read backwards).  ``order=CLUSTER_ORDER_BEST_FIRST``
+    walks the queue forwards instead.
+
+    Returns the indexes (into the input) of the kept leaders, in output order.
+    """
+    t = np.asarray(translations, dtype=np.float64).reshape(-1, 3)
+    n = t.shape[0]
+    walk = range(n) if order == CLUSTER_ORDER_BEST_FIRST else range(n - 1, -1, -1)
+    return cluster_leaders(t, radius, max_out, walk)
+
+
+def scan_rotation_clustered(geom, rec_grids, rec_spectra, lig_xyz, lig_weights, rot, max_trans_inp, max_out,
+                            radius, max_val=np.inf, order=CLUSTER_ORDER_REFERENCE, rot_id=0, workers=1):
+    """``findTranslationalMinima`` with ``doClusterTranslations`` on
+    (docking_app.hpp:417-447): the ``max_trans_inp`` queue, then TranClust,
+    then the first ``max_out`` entries (``getTranValuesFilled``)."""
+    res = scan_rotation(geom, rec_grids, rec_spectra, lig_xyz, lig_weights, rot, max_trans_inp, max_val,
+                        rot_id=rot_id, workers=workers)
+    if not res.in_grid:
+        return res
+    keep = tran_cluster(res.translations, res.scores, radius, max_out, order)
+    return ScanResult(rot_id, res.offsets[keep], res.cells[keep], res.scores[keep], res.translations[keep], True)
+
+
+# ----------------------------------------------------------------------------
 # Scan record format: docking_io_bin.hpp:21-76 (RotFftScanIO_Bin)
 # ----------------------------------------------------------------------------
 SCAN_SIGNATURE = 2014011401

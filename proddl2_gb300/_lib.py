@@ -32,6 +32,9 @@ FFTDOCK_PREC_BF16_SPECTRA = 1
 FFTDOCK_PENCIL_AUTO = 0
 FFTDOCK_PENCIL_FFT = 1
 FFTDOCK_PENCIL_TENSOR = 2
+FFTDOCK_CLUSTER_ORDER_REFERENCE = 0
+FFTDOCK_CLUSTER_ORDER_BEST_FIRST = 1
+FFTDOCK_MAX_QUEUE_CLUSTERED = 16384
 KC = 16
 
 
@@ -56,6 +59,9 @@ class Config(C.Structure):
         ("ace_a", C.c_double),
         ("ace_cut", C.c_double),
         ("pencil_mode", C.c_int32),
+        ("cluster_trans", C.c_int32),
+        ("cluster_order", C.c_int32),
+        ("cluster_radius", C.c_double),
     ]
 
 

@@ -96,10 +96,10 @@ template <int N> struct SizeOpsImpl {
     }
 
     template <bool PMAJOR, bool DBG>
-    static cudaError_t launch_plane(dim3 grid, size_t sm, const BatchArgs& a, cudaStream_t s) {
+    static cudaError_t launch_plane(dim3 grid, size_t sm, const BatchArgs& a, float* corr, cudaStream_t s) {
         cudaError_t e = set_smem((const void*)plane_kernel<N, PMAJOR, DBG>, sm);
         if (e != cudaSuccess) return e;
-        plane_kernel<N, PMAJOR, DBG><<<grid, 32 * G, sm, s>>>(a.g2, a.tw32, a.cand_v, a.cand_i, a.dbg_corr);
+        plane_kernel<N, PMAJOR, DBG><<<grid, 32 * G, sm, s>>>(a.g2, a.tw32, a.cand_v, a.cand_i, corr);
         return cudaGetLastError();
     }
 
@@ -134,24 +134,31 @@ template <int N> struct SizeOpsImpl {
             if (e != cudaSuccess) return e;
         }
         if (a.ev && (e = cudaEventRecord(a.ev[2], s)) != cudaSuccess) return e;
-        // K3
+        // K3 (the queue + clustering path also writes every correlation grid)
         const size_t sm3 = plane_smem();
         dim3 grid3(N, nb);
+        float* corr = a.dbg_corr ? a.dbg_corr : a.wide.corr;
         if (pmajor) {
-            if (a.dbg_corr) e = launch_plane<true, true>(grid3, sm3, a, s);
-            else e = launch_plane<true, false>(grid3, sm3, a, s);
+            if (corr) e = launch_plane<true, true>(grid3, sm3, a, corr, s);
+            else e = launch_plane<true, false>(grid3, sm3, a, nullptr, s);
         } else {
-            if (a.dbg_corr) e = launch_plane<false, true>(grid3, sm3, a, s);
-            else e = launch_plane<false, false>(grid3, sm3, a, s);
+            if (corr) e = launch_plane<false, true>(grid3, sm3, a, corr, s);
+            else e = launch_plane<false, false>(grid3, sm3, a, nullptr, s);
         }
         if (e != cudaSuccess) return e;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if (a.ev && (e = cudaEventRecord(a.ev[3], s)) != cudaSuccess) return e;
         // K4
-        finalize_kernel<N><<<nb, 256, 0, s>>>(a.cand_v, a.cand_i, a.ent, a.status, a.rgrid, a.n_ent,
-                                              a.peak_stride, a.k_out, a.max_val, a.h, a.first_rot_id, a.peaks,
-                                              a.n_peaks, a.pool_v, a.pool_i);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (a.wide.corr) {
+            BatchArgs w = a;
+            w.wide.corr = corr;
+            if ((e = wide_select_batch(w, N, s)) != cudaSuccess) return e;
+        } else {
+            finalize_kernel<N><<<nb, 256, 0, s>>>(a.cand_v, a.cand_i, a.ent, a.status, a.rgrid, a.n_ent,
+                                                  a.peak_stride, a.k_out, a.max_val, a.h, a.first_rot_id, a.peaks,
+                                                  a.n_peaks, a.pool_v, a.pool_i);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
         if (a.ev && (e = cudaEventRecord(a.ev[4], s)) != cudaSuccess) return e;
         return cudaSuccess;
     }

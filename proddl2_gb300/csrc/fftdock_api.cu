@@ -82,6 +82,9 @@ struct fftdock_ctx {
     int* err_dev = nullptr;
     int x0 = 0, W = 0;
 
+    // queue + clustering path (cfg.cluster_trans)
+    fftdock::WideArgs wide{};
+
     // kernel timing (fftdock_profile)
     bool profiling = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -174,6 +177,7 @@ BatchArgs batch_args(fftdock_ctx* ctx) {
     a.x0 = ctx->x0;
     a.W = ctx->W;
     a.err = ctx->err_dev;
+    a.wide = ctx->wide;
     return a;
 }
 
@@ -277,6 +281,9 @@ void fftdock_config_init(fftdock_config* cfg) {
     cfg->ace_k = 0.15;
     cfg->ace_a = 0.6;
     cfg->ace_cut = 6.0;
+    cfg->cluster_trans = 0;
+    cfg->cluster_order = FFTDOCK_CLUSTER_ORDER_REFERENCE;
+    cfg->cluster_radius = 5.0;
 }
 
 int fftdock_supported_grid(int32_t n) { return fftdock::size_ops(n) != nullptr ? 1 : 0; }
@@ -336,6 +343,11 @@ void fftdock_destroy(fftdock_ctx* ctx) {
     dfree(ctx->circ);
     dfree(ctx->cscale);
     dfree(ctx->err_dev);
+    dfree(ctx->wide.corr);
+    dfree(ctx->wide.hist);
+    dfree(ctx->wide.st);
+    dfree(ctx->wide.cand);
+    dfree(ctx->wide.cnt);
     for (cudaEvent_t ev : ctx->ev_pool) cudaEventDestroy(ev);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -371,6 +383,16 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
     ctx->use_tc = c.pencil_mode == FFTDOCK_PENCIL_TENSOR;
     if (!(c.shape_core_radius >= 0.0) || !(c.shape_surface_width >= 0.0))
         return fail(ctx, FFTDOCK_EINVAL, "shape radii must be >= 0");
+    if (c.cluster_trans != 0 && c.cluster_trans != 1) return fail(ctx, FFTDOCK_EINVAL, "cluster_trans must be 0 or 1");
+    if (c.cluster_trans) {
+        if (c.max_trans_inp > FFTDOCK_MAX_QUEUE_CLUSTERED)
+            return fail(ctx, FFTDOCK_EINVAL, "with cluster_trans, max_trans_inp must be <= " +
+                                                 std::to_string(FFTDOCK_MAX_QUEUE_CLUSTERED));
+        if (c.cluster_order != FFTDOCK_CLUSTER_ORDER_REFERENCE && c.cluster_order != FFTDOCK_CLUSTER_ORDER_BEST_FIRST)
+            return fail(ctx, FFTDOCK_EINVAL, "unknown cluster_order");
+        if (!(c.cluster_radius >= 0.0) || !std::isfinite(c.cluster_radius))
+            return fail(ctx, FFTDOCK_EINVAL, "cluster_radius must be finite and >= 0");
+    }
     if (c.term_set == FFTDOCK_TERMS_SHAPE) {
         ctx->K = 1;
     } else if (c.term_set == FFTDOCK_TERMS_SHAPE_ACE) {
@@ -442,6 +464,20 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
     if (ctx->use_tc) {
         CK(dalloc(&ctx->circ, (size_t)ctx->K * N * ctx->H * N));
         CK(dalloc(&ctx->cscale, (size_t)N * ctx->H));
+    }
+    if (c.cluster_trans) {
+        fftdock::WideArgs& w = ctx->wide;
+        CK(dalloc(&w.corr, (size_t)ctx->B * ctx->V));
+        CK(dalloc(&w.hist, (size_t)ctx->B * fftdock::kWideBins));
+        CK(dalloc(&w.st, (size_t)ctx->B));
+        CK(dalloc(&w.cand, (size_t)ctx->B * fftdock::kWideMax));
+        CK(dalloc(&w.cnt, (size_t)ctx->B));
+        w.m = c.max_trans_inp;
+        w.order = c.cluster_order;
+        // ClusterMatrix::cluster: cutoff2 = r^2 * 3 columns, cutoff = sqrt,
+        // compared as cutoff * cutoff (Geom/cluster.hpp:153-156)
+        const double cut = std::sqrt((c.cluster_radius * c.cluster_radius) * 3.0);
+        w.rad2 = cut * cut;
     }
     return FFTDOCK_OK;
 }
@@ -663,6 +699,8 @@ int fftdock_scan_candidates(fftdock_ctx* ctx, int32_t n_rot, const double* rot, 
     int rc = check_ready(ctx);
     if (rc) return rc;
     if (n_rot < 1 || !rot || !values || !offsets) return fail(ctx, FFTDOCK_EINVAL, "bad arguments");
+    if (ctx->wide.corr)
+        return fail(ctx, FFTDOCK_EUNSUPPORTED, "a clustering context keeps no per-plane candidate pools");
     CK(cudaSetDevice(ctx->cfg.device));
     if ((rc = grow_call_buffers(ctx, n_rot))) return rc;
     cudaStream_t s = ctx->stream;

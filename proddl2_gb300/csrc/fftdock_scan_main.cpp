@@ -13,9 +13,10 @@
 //
 // Options (JSON; keys are looked up anywhere in the file, the reference keeps
 // them in its "scan" block): gridStep, maxNTrans, maxNTransInp, maxValCorr,
-// cutOffFft, anglesFile, maxNRigidMatches, plus gridN (grid edge; default:
-// the reference's size rule over the padded receptor box), termSet ("shape"
-// or "shape_ace"), rotBatch.
+// cutOffFft, anglesFile, maxNRigidMatches, doClusterTranslations,
+// clusterRadiusTrans, plus gridN (grid edge; default: the reference's size
+// rule over the padded receptor box), termSet ("shape" or "shape_ace"),
+// rotBatch, clusterOrder ("reference" or "best_first").
 //
 // The reference reads atoms from an HDF5 molforce file built with IMP; this
 // front end reads a text pair file instead:
@@ -89,6 +90,8 @@ double num(const std::map<std::string, std::string>& o, const char* key, double 
     auto it = o.find(key);
     if (it == o.end()) return dflt;
     if (it->second == "Infinity" || it->second == "inf") return INFINITY;
+    if (it->second == "true") return 1.0;
+    if (it->second == "false") return 0.0;
     char* end = nullptr;
     const double v = std::strtod(it->second.c_str(), &end);
     if (end == it->second.c_str()) die(std::string("option ") + key + " is not a number");
@@ -200,6 +203,12 @@ int run_rot_scan(std::map<std::string, std::string>& a) {
     cfg.max_trans_inp = (int)num(opt, "maxNTransInp", cfg.peaks_per_rot * 100.0);
     cfg.max_val_corr = num(opt, "maxValCorr", 0.0);
     cfg.rot_batch = (int)num(opt, "rotBatch", 64);
+    // Worker::init (docking_app.hpp:369-382)
+    cfg.cluster_trans = num(opt, "doClusterTranslations", 0.0) != 0.0 ? 1 : 0;
+    cfg.cluster_radius = num(opt, "clusterRadiusTrans", 5.0);
+    const std::string corder = opt.count("clusterOrder") ? opt.at("clusterOrder") : "reference";
+    if (corder != "reference" && corder != "best_first") die("clusterOrder must be reference or best_first");
+    cfg.cluster_order = corder == "best_first" ? FFTDOCK_CLUSTER_ORDER_BEST_FIRST : FFTDOCK_CLUSTER_ORDER_REFERENCE;
     const std::string terms = opt.count("termSet") ? opt.at("termSet") : (p.n_types ? "shape_ace" : "shape");
     cfg.term_set = terms == "shape" ? FFTDOCK_TERMS_SHAPE : FFTDOCK_TERMS_SHAPE_ACE;
     cfg.n_types = p.n_types ? p.n_types : 18;

@@ -39,6 +39,40 @@ struct ReceptorGridArgs {
 
 cudaError_t build_receptor_grids(const ReceptorGridArgs& a, cudaStream_t s);
 
+// Exact per-rotation queue of up to kWideMax entries ("maxNTransInp") and
+// the translational clustering applied to it (TranClust,
+// include/PRODDL/docking_fft.hpp:30-140).  The correlation grid of every
+// rotation of the batch is written out; the cells at or below an upper bound
+// of the queue's last value (taken from the per-plane top-KC pools) are
+// gathered in one pass, sorted and clustered per rotation.  When the bound is
+// missing or too loose, a radix select over 64-bit keys (ordered float bits
+// << 32 | cell offset, so ties go to the lower offset) narrows the set first.
+constexpr int kWideMax = 16384;
+constexpr int kWideBins = 4096;  // 12-bit digits
+
+struct WideState {
+    unsigned long long pfx;  // resolved key prefix (radix path)
+    int nres;                // resolved key bits
+    int need;                // entries still to take from the prefix's bin
+    int below;               // entries with a key below the bin (all kept)
+    int active;              // another digit pass is needed
+    int flags;               // kWideAll | kWideRadix
+    float thr;               // upper bound of the queue's values (+inf: none)
+};
+constexpr int kWideAll = 1;    // fewer than m cells pass: keep them all
+constexpr int kWideRadix = 2;  // the bound was too loose: radix path
+
+struct WideArgs {
+    float* corr;               // [B][N^3] correlation grids (nullptr: wide path off)
+    uint32_t* hist;            // [B][kWideBins]
+    WideState* st;             // [B]
+    unsigned long long* cand;  // [B][kWideMax] gathered keys
+    int32_t* cnt;              // [B]
+    int m;                     // queue bound, 1..kWideMax
+    int order;                 // FFTDOCK_CLUSTER_ORDER_*
+    double rad2;               // squared neighbour radius of the clustering
+};
+
 // Everything one device batch of rotations needs.
 struct BatchArgs {
     // inputs
@@ -78,7 +112,12 @@ struct BatchArgs {
     const int8_t* cscale;       // [N*H] power-of-two scale exponents
     int x0, W;                  // ligand window along x
     int* err;                   // device word: nonzero after a pipeline timeout
+    WideArgs wide;              // queue + clustering path (wide.corr != nullptr)
 };
+
+// queue + clustering stage of one batch, after the correlation grids of the
+// batch are in a.wide.corr; writes a.peaks / a.n_peaks
+cudaError_t wide_select_batch(const BatchArgs& a, int N, cudaStream_t s);
 
 struct SizeOps {
     int n;

@@ -62,6 +62,10 @@ extern "C" int fftdock_scan_device_noalloc(fftdock_ctx* ctx, int32_t n_rot, cons
     if (n_rot < 0 || (n_rot > 0 && (!d_rot || !d_peaks || !d_n_peaks)))
         return fftdock::ctx_fail(ctx, FFTDOCK_EINVAL, "bad arguments");
     if (n_rot == 0) return FFTDOCK_OK;
+    if (in.args.wide.corr)
+        return fftdock::ctx_fail(ctx, FFTDOCK_EUNSUPPORTED,
+                                 "translational clustering needs a full correlation grid per rotation; the "
+                                 "no-allocation scan does not cover it");
     if (in.device < 0 || in.device >= kMaxDevices)
         return fftdock::ctx_fail(ctx, FFTDOCK_EINVAL, "device ordinal beyond the no-allocation scan's table");
     if (scratch_bytes(in, 1) > kScratchBytes) {

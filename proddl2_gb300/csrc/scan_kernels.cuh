@@ -440,11 +440,8 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
                 const float v0 = valid ? o.x : INFINITY;
                 const float v1 = valid ? o.y : INFINITY;
                 if constexpr (DBG) {
-                    if (valid) {
-                        float* d = dbg + (size_t)q * N * N * N + rowbase;
-                        d[2 * mm] = o.x;
-                        d[2 * mm + 1] = o.y;
-                    }
+                    if (valid)
+                        reinterpret_cast<float2*>(dbg + (size_t)q * N * N * N + rowbase)[mm] = o;
                 }
                 tk.offer(v0, valid ? rowbase + 2 * mm : 0x7fffffff, l);
                 tk.offer(v1, valid ? rowbase + 2 * mm + 1 : 0x7fffffff, l);

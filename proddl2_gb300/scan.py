@@ -42,12 +42,16 @@ class ScanConfig:
     device: int = 0
     pencil_mode: str = "auto"       # "auto", "fft" (CUDA-core x-FFTs) or "tensor" (tcgen05 GEMM form)
     precision: str = "fp32"         # receptor spectra: "fp32" or "bf16"
+    cluster_trans: bool = False     # doClusterTranslations
+    cluster_radius: float = 5.0     # clusterRadiusTrans
+    cluster_order: str = "reference"  # leader walk: "reference" (worst value first) or "best_first"
 
     @classmethod
     def from_options(cls, opts: dict, **kw):
         """Build from a reference-style options dict (``config/noarch/proddl.json.in``)."""
         names = {"gridStep": "grid_step", "maxNTrans": "peaks_per_rot", "maxNTransInp": "max_trans_inp",
-                 "maxValCorr": "max_val_corr"}
+                 "maxValCorr": "max_val_corr", "doClusterTranslations": "cluster_trans",
+                 "clusterRadiusTrans": "cluster_radius"}
         args = {names[k]: v for k, v in opts.items() if k in names}
         args.update(kw)
         return cls(**args)
@@ -98,6 +102,9 @@ class FFTScan:
         cfg.device = int(config.device)
         cfg.pencil_mode = PENCIL_MODES[config.pencil_mode]
         cfg.precision = {"fp32": _lib.FFTDOCK_PREC_FP32, "bf16": _lib.FFTDOCK_PREC_BF16_SPECTRA}[config.precision]
+        cfg.cluster_trans = 1 if config.cluster_trans else 0
+        cfg.cluster_radius = float(config.cluster_radius)
+        cfg.cluster_order = {"reference": 0, "best_first": 1}[config.cluster_order]
         h = C.c_void_p()
         rc = self.lib.fftdock_create(C.byref(cfg), C.byref(h))
         self._h = h

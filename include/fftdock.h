@@ -266,6 +266,67 @@ int fftdock_write_rigid(const char* path, const fftdock_pose* poses, int32_t n, 
 int fftdock_write_scan_records(const char* path, int32_t n_rot, const double* rot, int32_t peaks_per_rot,
                                const fftdock_peak* peaks, const int32_t* n_peaks, int32_t append);
 
+/* ------------------------------------------------------------------------
+ * Learned rotation proposal.  No counterpart in the reference: a small
+ * network predicts each rotation's best (lowest) scan score from a 16^3
+ * occupancy grid of the rotated ligand and a 128-value receptor descriptor,
+ * so that a caller can scan only the rotations it ranks best; the
+ * exhaustive scan (fftdock_scan) stays the fallback and the measure of its
+ * recall.  Network: three 3^3 stride-2 convolutions (16, 32, 64 channels,
+ * ReLU) -> 512 features + descriptor -> 256 ReLU -> 1.  BF16 weights and
+ * activations, FP32 accumulation, FP32 master weights trained with Adam; the
+ * training step runs as one captured CUDA graph.
+ * ------------------------------------------------------------------------ */
+#define FFTDOCK_PROPOSAL_DESC 128
+
+typedef struct fftdock_proposal fftdock_proposal;
+
+/* New network with He-normal weights drawn from `seed` on `device`. */
+int fftdock_proposal_create(int32_t device, uint64_t seed, fftdock_proposal** out);
+void fftdock_proposal_destroy(fftdock_proposal* p);
+const char* fftdock_proposal_last_error(const fftdock_proposal* p);
+
+/* Parameter count and the FP32 master weights (layout: conv1 w[16][1][27],
+ * b[16]; conv2 w[32][16][27], b[32]; conv3 w[64][32][27], b[64]; fc1
+ * w[640][256] input-major, b[256]; fc2 w[256], b).  Setting the weights
+ * resets the optimiser state. */
+int32_t fftdock_proposal_n_params(void);
+int fftdock_proposal_get_params(fftdock_proposal* p, float* out);
+int fftdock_proposal_set_params(fftdock_proposal* p, const float* in);
+
+/* Register one docking pair: the ligand's atoms (in the scan frame, rotation
+ * centre at the origin) and the receptor's descriptor; returns its id. */
+int fftdock_proposal_add_ligand(fftdock_proposal* p, int32_t n_atoms, const double* xyz, const float* rec_desc,
+                                int32_t* id);
+
+/* Training samples of a registered pair: rotations (row-major 3x3) and the
+ * regression targets (the caller's scale, e.g. standardised best scores). */
+int fftdock_proposal_add_samples(fftdock_proposal* p, int32_t lig, int32_t n, const double* rot,
+                                 const float* target);
+int fftdock_proposal_clear_samples(fftdock_proposal* p);
+
+/* `steps` Adam steps (betas 0.9 / 0.999, eps 1e-8) on minibatches of
+ * `batch` samples drawn with replacement by a hash of (seed, step); the
+ * mean squared error over the steps is returned in *mean_loss. */
+int fftdock_proposal_train(fftdock_proposal* p, int32_t steps, int32_t batch, float lr, uint64_t seed,
+                           float* mean_loss);
+
+/* Gradient of the mean squared error of the given samples with respect to
+ * every parameter (no update): the check against a CPU restatement. */
+int fftdock_proposal_gradients(fftdock_proposal* p, int32_t n, const int32_t* lig, const double* rot,
+                               const float* target, float* grads, float* loss);
+
+/* Predicted best score of pair `lig` for each rotation: host buffers, or
+ * device buffers ordered on `stream` (NULL: the library's own stream). */
+int fftdock_proposal_predict(fftdock_proposal* p, int32_t lig, int32_t n, const double* rot, float* out);
+int fftdock_proposal_predict_device(fftdock_proposal* p, int32_t lig, int32_t n, const double* d_rot, float* d_out,
+                                    void* stream);
+
+/* Receptor descriptor: per element (0 C, 1 N, 2 O, 3 S) a 32-shell radial
+ * histogram (1.5 A shells about the bounding-box centre, the last shell
+ * open-ended) divided by the atom count.  Host only. */
+int fftdock_receptor_descriptor(int32_t n, const double* xyz, const int32_t* element, float* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -128,6 +128,20 @@ SIGNATURES = {
     "fftdock_gather_list": (C.c_int, [C.c_char_p, C.c_int32, _P, C.POINTER(C.c_int32)]),
     "fftdock_write_rigid": (C.c_int, [C.c_char_p, _P, C.c_int32, _P, _P, C.c_int32]),
     "fftdock_write_scan_records": (C.c_int, [C.c_char_p, C.c_int32, _P, C.c_int32, _P, _P, C.c_int32]),
+    "fftdock_proposal_create": (C.c_int, [C.c_int32, C.c_uint64, C.POINTER(_P)]),
+    "fftdock_proposal_destroy": (None, [_P]),
+    "fftdock_proposal_last_error": (C.c_char_p, [_P]),
+    "fftdock_proposal_n_params": (C.c_int32, []),
+    "fftdock_proposal_get_params": (C.c_int, [_P, _P]),
+    "fftdock_proposal_set_params": (C.c_int, [_P, _P]),
+    "fftdock_proposal_add_ligand": (C.c_int, [_P, C.c_int32, _P, _P, C.POINTER(C.c_int32)]),
+    "fftdock_proposal_add_samples": (C.c_int, [_P, C.c_int32, C.c_int32, _P, _P]),
+    "fftdock_proposal_clear_samples": (C.c_int, [_P]),
+    "fftdock_proposal_train": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_float, C.c_uint64, C.POINTER(C.c_float)]),
+    "fftdock_proposal_gradients": (C.c_int, [_P, C.c_int32, _P, _P, _P, _P, C.POINTER(C.c_float)]),
+    "fftdock_proposal_predict": (C.c_int, [_P, C.c_int32, C.c_int32, _P, _P]),
+    "fftdock_proposal_predict_device": (C.c_int, [_P, C.c_int32, C.c_int32, _P, _P, _P]),
+    "fftdock_receptor_descriptor": (C.c_int, [C.c_int32, _P, _P, _P]),
 }
 
 _lib = None

@@ -57,6 +57,7 @@ def parse_args():
     p.add_argument("--cluster-queue", type=int, default=0,
                    help="queue bound with --cluster (maxNTransInp; default: the reference's maxNTrans * 100)")
     p.add_argument("--cluster-radius", type=float, default=5.0, help="clusterRadiusTrans with --cluster")
+    p.add_argument("--n-pairs", type=int, default=0, help="pairs of the pairs256 workload (default 256)")
     return p.parse_args()
 
 
@@ -232,9 +233,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded globules, uniform quaternion rotations)",
-        "config": {"workload": workload_desc(w),
-                   "mode": ("exhaustive, translational clustering of a %d-cell queue per rotation (radius %g A)"
-                            % (queue, args.cluster_radius)) if args.cluster else "exhaustive", "sample_rotations_per_step": per_step},
+        "config": {"workload": workload_desc(w), "mode": "exhaustive", "sample_rotations_per_step": per_step},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -423,12 +422,162 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# many uneven pairs in one CUDA graph (workload pairs256)
+# ---------------------------------------------------------------------------
+PAIRS_METRIC = "rotations/s, 256 uneven pairs (grid 48-144^3) scanned from one CUDA graph"
+
+
+def pairs_workload(args):
+    from proddl2_gb300 import synth
+    from proddl2_gb300.pairs import PairInput, pair_grid
+    w = workload(args.workload)
+    n_pairs = args.n_pairs or w["n_pairs"]
+    n_rot = args.n_rot or w["n_rot"]
+    ace = synth.ace_matrix(18, 1)
+    rot = synth.quaternion_rotations(n_rot, seed=2)
+    pairs = []
+    for rec, lig in synth.uneven_pairs(n_pairs, seed=1):
+        pairs.append(PairInput(rec.xyz, lig.xyz, rot, rec.ace_type, lig.ace_type,
+                               grid_n=pair_grid(rec.xyz, lig.xyz, w["grid_step"])))
+    return w, n_pairs, n_rot, ace, pairs
+
+
+def pairs_desc(w, n_pairs, n_rot, grids):
+    from collections import Counter
+    hist = ", ".join("%d^3 x %d" % (n, c) for n, c in sorted(Counter(grids).items()))
+    return ("%s: %d pairs, receptors 800-6000 / ligands 300-2000 atoms (log-uniform), grid edge per pair "
+            "(%s) at %.1f A, shape + 18 desolvation types, %d rotations per pair, %d peaks/rotation"
+            % (w["name"], n_pairs, hist, w["grid_step"], n_rot, w["peaks"]))
+
+
+def run_pairs(args):
+    import torch
+    from proddl2_gb300 import FFTScan, ScanConfig
+    from proddl2_gb300.pairs import scan_pairs
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    w, n_pairs, n_rot, ace, pairs = pairs_workload(args)
+    base = ScanConfig(term_set=w["term_set"], ace_matrix=ace, peaks_per_rot=w["peaks"], rot_batch=w["rot_batch"],
+                      device=local)
+    # warm-up: the tuned call fixes the plan (streams, rotations per launch)
+    t0 = time.perf_counter()
+    _, plan = scan_pairs(base, pairs, tune=True)
+    tune_call_s = time.perf_counter() - t0
+    for _ in range(max(0, args.warmup - 1)):
+        scan_pairs(base, pairs, tune=False, plan=plan)
+    gpu_index = local
+    sampler = ClockSampler(gpu_index)
+    sampler.start()
+    run_ms, call_s = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        res, rep = scan_pairs(base, pairs, tune=False, plan=plan)
+        call_s.append(time.perf_counter() - t0)
+        run_ms.append(rep["run_ms"])
+    clocks = sampler.stop()
+    rot_total = n_pairs * n_rot
+    ms_per_step = sum(run_ms) / len(run_ms)
+    value = rot_total * world / (ms_per_step / 1000.0)
+    e2e_s = sum(call_s) / len(call_s)
+
+    # per-pair sequential launches through the single-pair API (one context per grid edge, made beforehand)
+    ctxs = {}
+    for p in pairs:
+        if p.grid_n not in ctxs:
+            ctxs[p.grid_n] = FFTScan(ScanConfig(grid_n=p.grid_n, term_set=w["term_set"], ace_matrix=ace,
+                                                peaks_per_rot=w["peaks"], rot_batch=w["rot_batch"], device=local))
+    p0 = pairs[0]
+    s0 = ctxs[p0.grid_n]
+    s0.set_receptor(p0.rec_xyz, p0.rec_type)
+    s0.set_ligand(p0.lig_xyz, p0.lig_type)
+    s0.scan(p0.rotations)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    seq_n_out = 0
+    for p in pairs:
+        s = ctxs[p.grid_n]
+        s.set_receptor(p.rec_xyz, p.rec_type)
+        s.set_ligand(p.lig_xyz, p.lig_type)
+        r = s.scan(p.rotations, raise_out_of_grid=False)
+        seq_n_out += int((r.n_peaks == 0).sum())
+    seq_s = time.perf_counter() - t0
+    for s in ctxs.values():
+        s.close()
+    if rank != 0:
+        return
+    h2d = sum(p.rec_xyz.nbytes + p.lig_xyz.nbytes + p.rotations.nbytes + p.rec_type.nbytes + p.lig_type.nbytes
+              for p in pairs)
+    d2h = sum(r.peaks.nbytes + r.n_peaks.nbytes for r in res)
+    out = {
+        "metric": PAIRS_METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded globules, uniform quaternion rotations)",
+        "config": {"workload": pairs_desc(w, n_pairs, n_rot, [p.grid_n for p in pairs]),
+                   "mode": "exhaustive, all pairs in one CUDA graph",
+                   "plan": {"streams": plan["n_streams"], "rot_batch_by_grid": plan["rot_batch"]},
+                   "l2": "inputs larger than L2 (per-pair receptor spectra + x-planes rewritten every batch)"},
+        "pairs_per_s": n_pairs * world / (ms_per_step / 1000.0),
+        "e2e": {"value": rot_total * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "what": "whole fftdock_scan_pairs call: staging, capture, run, copy-out"},
+        "tune_call_s": tune_call_s,
+        "sequential_per_pair": {"value": rot_total / seq_s, "unit": UNIT, "pairs_per_s": n_pairs / seq_s,
+                                "what": "per pair: set_receptor + set_ligand + scan through the single-pair C ABI"},
+        "speedup_vs_sequential_e2e": seq_s / e2e_s,
+        # per pair: 3 receptor-grid kernels, 6 per receptor term transform, 4 per scan batch
+        "gpu_launches": sum(3 + 6 * 18 + 4 * math.ceil(n_rot / plan["rot_batch"][p.grid_n]) for p in pairs),
+        "clocks": clocks,
+    }
+    print(json.dumps(out))
+
+
+def run_pairs_reference(args):
+    rank, _, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import fftdock_oracle as O
+    w, n_pairs, n_rot, ace, pairs = pairs_workload(args)
+    threads = os.cpu_count() or 1
+    tp = O.TermParams(term_set=O.TERMS_SHAPE_ACE, ace_matrix=ace)
+    done, t_total, pi = 0, 0.0, 0
+    per_step = 2
+    # each step: the reference schedule for a few rotations of the next pair
+    for step in range(args.warmup + args.steps):
+        p = pairs[pi % len(pairs)]
+        pi += 1
+        geom = O.Geometry.centred(w["grid_step"], p.grid_n)
+        rg = O.receptor_terms(geom, p.rec_xyz, p.rec_type, tp, folded=False)
+        rs = O.receptor_spectra(rg, workers=threads)
+        wts = O.ligand_term_weights(p.lig_type, tp, folded=False)
+        t0 = time.perf_counter()
+        for i in range(per_step):
+            O.scan_rotation(geom, rg, rs, p.lig_xyz, wts, p.rotations[i], w["peaks"], workers=threads)
+        if step >= args.warmup:
+            t_total += time.perf_counter() - t0
+            done += per_step
+    value = done / t_total
+    out = {
+        "impl": "reference", "metric": PAIRS_METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_total / max(1, args.steps),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded globules, uniform quaternion rotations)",
+        "config": {"workload": pairs_desc(w, n_pairs, n_rot, [p.grid_n for p in pairs]), "mode": "exhaustive"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d rotations of one pair per step (pairs in order), FP64 oracle, 19 FFT terms "
+                                   "(reference schedule), scipy pocketfft on %d threads" % (per_step, threads)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
 def main():
     args = parse_args()
+    pairs_mode = args.workload.startswith("pairs")
     if args.impl == "reference":
-        run_reference(args)
+        (run_pairs_reference if pairs_mode else run_reference)(args)
     else:
-        run_ours(args)
+        (run_pairs if pairs_mode else run_ours)(args)
 
 
 if __name__ == "__main__":

@@ -267,6 +267,63 @@ int fftdock_write_scan_records(const char* path, int32_t n_rot, const double* ro
                                const fftdock_peak* peaks, const int32_t* n_peaks, int32_t append);
 
 /* ------------------------------------------------------------------------
+ * Many pairs in one CUDA graph.  No counterpart in the reference (it runs
+ * one pair per process).  Every pair's atoms and rotations are staged on the
+ * device once; the whole workload -- per pair the receptor grids and
+ * transforms, then the scan batches -- is captured into one CUDA graph over
+ * one or more streams and launched once.  With tune != 0 an autotuner picks
+ * the rotations per launch of each grid size and the number of streams from
+ * timed probes.  cfg supplies everything but the grid edge (term set, ACE
+ * matrix, peaks, limits, precision, device); clustering and the tensor-core
+ * pencil form are not part of the batch.
+ * ------------------------------------------------------------------------ */
+#define FFTDOCK_N_SIZES 10   /* built grid edges: 16 24 32 48 64 80 96 112 128 144 */
+
+typedef struct fftdock_pair {
+    int32_t grid_n;              /* built grid edge of this pair */
+    int32_t n_rec;
+    const double* rec_xyz;       /* [n_rec][3], grid frame */
+    const int32_t* rec_type;     /* [n_rec], shape+ACE only */
+    int32_t n_lig;
+    const double* lig_xyz;       /* [n_lig][3], rotation centre at the origin */
+    const int32_t* lig_type;     /* [n_lig], shape+ACE only */
+    int32_t n_rot;
+    const double* rot;           /* [n_rot][9] row-major */
+    int32_t first_rot_id;
+    fftdock_peak* peaks;         /* out, host: [n_rot][peaks_per_rot] */
+    int32_t* n_peaks;            /* out, host: [n_rot] */
+} fftdock_pair;
+
+typedef struct fftdock_pairs_report {
+    int32_t n_streams;                    /* streams the graph used */
+    int32_t grid_sizes[FFTDOCK_N_SIZES];  /* the edge each slot below stands for */
+    int32_t rot_batch[FFTDOCK_N_SIZES];   /* rotations per launch used per edge (0: edge unused) */
+    double setup_ms;                      /* whole call, host clock */
+    double tune_ms;                       /* autotuner probes, host clock */
+    double capture_ms;                    /* capture + instantiation, host clock */
+    double run_ms;                        /* the graph's execution, CUDA events */
+    int64_t rotations;                    /* rotations scanned */
+    int32_t n_out_of_grid;                /* rotations that left the grid (no peaks) */
+} fftdock_pairs_report;
+
+/* Scan every pair; FFTDOCK_EOUT_OF_GRID (outputs still written) if any
+ * rotation put a ligand atom outside its grid.  Errors are described by
+ * fftdock_pairs_last_error() (per calling thread).  With tune == 0, a report
+ * whose n_streams > 0 is read as the plan to use (streams and rotations per
+ * launch per edge, e.g. from an earlier tuned call); otherwise one stream
+ * and cfg->rot_batch. */
+int fftdock_scan_pairs(const fftdock_config* cfg, int32_t n_pairs, const fftdock_pair* pairs, int32_t tune,
+                       fftdock_pairs_report* report);
+const char* fftdock_pairs_last_error(void);
+
+/* Grid edge for a pair: the smallest built edge >= 48 that covers
+ * ceil((2 r_rec + 2 r_lig + 2 margin) / step) cells, r_rec the receptor's
+ * largest atom distance from its bounding-box centre and r_lig the ligand's
+ * from the origin (the rotation centre). */
+int fftdock_pair_grid(int32_t n_rec, const double* rec_xyz, int32_t n_lig, const double* lig_xyz, double step,
+                      double margin, int32_t* grid_n);
+
+/* ------------------------------------------------------------------------
  * Learned rotation proposal.  No counterpart in the reference: a small
  * network predicts each rotation's best (lowest) scan score from a 16^3
  * occupancy grid of the rotated ligand and a 128-value receptor descriptor,

@@ -65,6 +65,41 @@ class Config(C.Structure):
     ]
 
 
+N_SIZES = 10
+BUILT_SIZES = (16, 24, 32, 48, 64, 80, 96, 112, 128, 144)
+
+
+class PairDesc(C.Structure):
+    _fields_ = [
+        ("grid_n", C.c_int32),
+        ("n_rec", C.c_int32),
+        ("rec_xyz", C.c_void_p),
+        ("rec_type", C.c_void_p),
+        ("n_lig", C.c_int32),
+        ("lig_xyz", C.c_void_p),
+        ("lig_type", C.c_void_p),
+        ("n_rot", C.c_int32),
+        ("rot", C.c_void_p),
+        ("first_rot_id", C.c_int32),
+        ("peaks", C.c_void_p),
+        ("n_peaks", C.c_void_p),
+    ]
+
+
+class PairsReport(C.Structure):
+    _fields_ = [
+        ("n_streams", C.c_int32),
+        ("grid_sizes", C.c_int32 * N_SIZES),
+        ("rot_batch", C.c_int32 * N_SIZES),
+        ("setup_ms", C.c_double),
+        ("tune_ms", C.c_double),
+        ("capture_ms", C.c_double),
+        ("run_ms", C.c_double),
+        ("rotations", C.c_int64),
+        ("n_out_of_grid", C.c_int32),
+    ]
+
+
 class Peak(C.Structure):
     _fields_ = [
         ("rot_id", C.c_int32),
@@ -128,6 +163,10 @@ SIGNATURES = {
     "fftdock_gather_list": (C.c_int, [C.c_char_p, C.c_int32, _P, C.POINTER(C.c_int32)]),
     "fftdock_write_rigid": (C.c_int, [C.c_char_p, _P, C.c_int32, _P, _P, C.c_int32]),
     "fftdock_write_scan_records": (C.c_int, [C.c_char_p, C.c_int32, _P, C.c_int32, _P, _P, C.c_int32]),
+    "fftdock_scan_pairs": (C.c_int, [C.POINTER(Config), C.c_int32, C.POINTER(PairDesc), C.c_int32,
+                                     C.POINTER(PairsReport)]),
+    "fftdock_pairs_last_error": (C.c_char_p, []),
+    "fftdock_pair_grid": (C.c_int, [C.c_int32, _P, C.c_int32, _P, C.c_double, C.c_double, C.POINTER(C.c_int32)]),
     "fftdock_proposal_create": (C.c_int, [C.c_int32, C.c_uint64, C.POINTER(_P)]),
     "fftdock_proposal_destroy": (None, [_P]),
     "fftdock_proposal_last_error": (C.c_char_p, [_P]),

@@ -506,6 +506,9 @@ int fftdock_set_receptor(fftdock_ctx* ctx, int32_t n, const double* xyz, const i
     double* dens = nullptr;
     double2* cbuf = nullptr;
     double2* hbuf = nullptr;
+    int* bin_start = nullptr;
+    int* bin_atoms = nullptr;
+    int* box = nullptr;
     int rc = FFTDOCK_OK;
     auto cleanup = [&]() {
         cudaStreamSynchronize(s);
@@ -515,6 +518,9 @@ int fftdock_set_receptor(fftdock_ctx* ctx, int32_t n, const double* xyz, const i
         dfree(dens);
         dfree(cbuf);
         dfree(hbuf);
+        dfree(bin_start);
+        dfree(bin_atoms);
+        dfree(box);
     };
 #define CKR(expr)                                 \
     do {                                          \
@@ -532,12 +538,30 @@ int fftdock_set_receptor(fftdock_ctx* ctx, int32_t n, const double* xyz, const i
         CKR(cudaMemcpyAsync(d_xyz, xyz, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, s));
         if (ace) CKR(cudaMemcpyAsync(d_type, type, (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
     }
-    if (ace) CKR(dalloc(&dens, (size_t)c.n_types * V));
+    fftdock::HostAtomBins hb;
+    if (ace) {
+        CKR(dalloc(&dens, (size_t)c.n_types * V));
+        fftdock::bin_atoms(xyz, n, c.ace_cut, hb);
+        CKR(dalloc(&bin_start, hb.start.size()));
+        CKR(dalloc(&bin_atoms, hb.atoms.size()));
+        CKR(dalloc(&box, (size_t)6 * n));
+        CKR(cudaMemcpyAsync(bin_start, hb.start.data(), hb.start.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        if (n > 0)
+            CKR(cudaMemcpyAsync(bin_atoms, hb.atoms.data(), hb.atoms.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    }
     {
         fftdock::ReceptorGridArgs ra{};
         ra.xyz = d_xyz;
         ra.type = d_type;
         ra.n = n;
+        for (int d = 0; d < 3; ++d) {
+            ra.bins.lo[d] = hb.lo[d];
+            ra.bins.nb[d] = hb.nb[d];
+        }
+        ra.bins.size = hb.size;
+        ra.bins.start = bin_start;
+        ra.bins.atoms = bin_atoms;
+        ra.box = box;
         ra.geo = g;
         ra.term_set = c.term_set;
         ra.n_types = c.n_types;

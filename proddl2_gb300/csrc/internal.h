@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "fftdock.h"
 
 namespace fftdock {
@@ -21,10 +23,30 @@ struct Geo {
     int n;
 };
 
+// Receptor atoms sorted into cubic bins of edge >= the desolvation cutoff
+// (host-built counting sort, atoms in index order inside each bin), so that
+// every grid cell gathers its atoms in one fixed order.
+struct AtomBins {
+    double lo[3];          // corner of bin (0, 0, 0)
+    double size;           // bin edge
+    int nb[3];             // bins per axis
+    const int* start;      // [nbins + 1]
+    const int* atoms;      // [n] atom indexes
+};
+struct HostAtomBins {
+    double lo[3] = {0, 0, 0};
+    double size = 1.0;
+    int nb[3] = {1, 1, 1};
+    std::vector<int> start, atoms;
+};
+void bin_atoms(const double* xyz, int n, double cut, HostAtomBins& out);
+
 struct ReceptorGridArgs {
     const double* xyz;     // [n][3]
     const int32_t* type;   // [n]
     int n;
+    AtomBins bins;         // shape+ACE: cell list of the atoms (device arrays)
+    int* box;              // shape+ACE: [n][6] work (each atom's projection box)
     Geo geo;
     int term_set;
     int n_types;

@@ -2,6 +2,10 @@
 // per-type desolvation densities and their mixing into the K folded terms.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 #include "internal.h"
 #include "scan_kernels.cuh"
 
@@ -51,30 +55,59 @@ __global__ void shape_flags_kernel(const double* __restrict__ xyz, int n, Geo g,
     }
 }
 
-// per-type desolvation density G_tau(x) = sum_i g(r) (PotAce::f2,
-// potentials_inc.hpp:394-397; projection as project.hpp:143-159)
-__global__ void ace_density_kernel(const double* __restrict__ xyz, const int32_t* __restrict__ type, int n, Geo g,
-                                   double cut, double cut2, double mind2, double ab, double ak, double aa,
-                                   double* __restrict__ dens) {
-    const int a = blockIdx.x;
+// each atom's cropped projection box (project.hpp:87-98); empty boxes get
+// lo > hi
+__global__ void atom_box_kernel(const double* __restrict__ xyz, int n, Geo g, double cut, int* __restrict__ box) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= n) return;
     const double c[3] = {xyz[3 * a], xyz[3 * a + 1], xyz[3 * a + 2]};
     Box b;
-    if (!projection_box(c, cut, g, b)) return;
-    const size_t V = (size_t)g.n * g.n * g.n;
-    double* dt = dens + (size_t)type[a] * V;
-    const int nx = b.hi[0] - b.lo[0] + 1, ny = b.hi[1] - b.lo[1] + 1, nz = b.hi[2] - b.lo[2] + 1;
-    const int tot = nx * ny * nz;
-    for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-        const int ix = b.lo[0] + i / (ny * nz), iy = b.lo[1] + (i / nz) % ny, iz = b.lo[2] + i % nz;
-        double r2 = dist2(c, ix, iy, iz, g);
-        if (r2 <= cut2) {
-            if (r2 < mind2) r2 = mind2;
-            const double r = sqrt(r2);
-            const double val = __ddiv_rn(1.0, __dadd_rn(1.0, exp(__dmul_rn(ab, __dsub_rn(__dmul_rn(ak, r), aa)))));
-            atomicAdd(&dt[((size_t)ix * g.n + iy) * g.n + iz], val);
-        }
+    const bool ok = projection_box(c, cut, g, b);
+    for (int d = 0; d < 3; ++d) {
+        box[6 * a + d] = ok ? b.lo[d] : 1;
+        box[6 * a + 3 + d] = ok ? b.hi[d] : 0;
     }
+}
+
+// per-type desolvation density G_tau(x) = sum_i g(r) (PotAce::f2,
+// potentials_inc.hpp:394-397; projection as project.hpp:143-159: atom i
+// reaches cell x if x lies in i's cropped box and r^2 <= cut^2, r^2 clamped
+// to minDist^2).  Gathered per cell over the atoms of the 27 neighbouring
+// bins, bins and atoms in a fixed order: the sums do not depend on thread
+// scheduling.
+__global__ void ace_density_kernel(const double* __restrict__ xyz, const int32_t* __restrict__ type,
+                                   const int* __restrict__ box, AtomBins bins, Geo g, double cut2, double mind2,
+                                   double ab, double ak, double aa, double* __restrict__ dens) {
+    const size_t V = (size_t)g.n * g.n * g.n;
+    const size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= V) return;
+    const int ix = (int)(cell / ((size_t)g.n * g.n)), iy = (int)((cell / g.n) % g.n), iz = (int)(cell % g.n);
+    const int ic[3] = {ix, iy, iz};
+    int b0[3];
+    for (int d = 0; d < 3; ++d) {
+        const double t = floor((cell_centre(ic[d], g) - bins.lo[d]) / bins.size);
+        b0[d] = t < -2.0 ? -2 : (t > (double)bins.nb[d] + 1.0 ? bins.nb[d] + 1 : (int)t);
+    }
+    for (int bx = max(b0[0] - 1, 0); bx <= min(b0[0] + 1, bins.nb[0] - 1); ++bx)
+        for (int by = max(b0[1] - 1, 0); by <= min(b0[1] + 1, bins.nb[1] - 1); ++by)
+            for (int bz = max(b0[2] - 1, 0); bz <= min(b0[2] + 1, bins.nb[2] - 1); ++bz) {
+                const int bin = (bx * bins.nb[1] + by) * bins.nb[2] + bz;
+                for (int k = bins.start[bin]; k < bins.start[bin + 1]; ++k) {
+                    const int a = bins.atoms[k];
+                    const int* bb = box + 6 * a;
+                    if (ix < bb[0] || ix > bb[3] || iy < bb[1] || iy > bb[4] || iz < bb[2] || iz > bb[5]) continue;
+                    const double c[3] = {xyz[3 * a], xyz[3 * a + 1], xyz[3 * a + 2]};
+                    double r2 = dist2(c, ix, iy, iz, g);
+                    if (r2 <= cut2) {
+                        if (r2 < mind2) r2 = mind2;
+                        const double r = sqrt(r2);
+                        const double val =
+                            __ddiv_rn(1.0, __dadd_rn(1.0, exp(__dmul_rn(ab, __dsub_rn(__dmul_rn(ak, r), aa)))));
+                        double* dt = dens + (size_t)type[a] * V + cell;
+                        *dt = __dadd_rn(*dt, val);
+                    }
+                }
+            }
 }
 
 // R_t = sum_u E[u][t] G_u - S (shape+ACE, folded) or R_0 = -S (shape)
@@ -113,14 +146,48 @@ cudaError_t build_receptor_grids(const ReceptorGridArgs& a, cudaStream_t s) {
         if (e != cudaSuccess) return e;
         const double md = a.geo.h / 4.0;
         if (a.n > 0) {
-            ace_density_kernel<<<a.n, 256, 0, s>>>(a.xyz, a.type, a.n, a.geo, a.ace_cut, a.ace_cut * a.ace_cut,
-                                                   md * md, a.ace_b, a.ace_k, a.ace_a, a.dens);
+            atom_box_kernel<<<(a.n + 127) / 128, 128, 0, s>>>(a.xyz, a.n, a.geo, a.ace_cut, a.box);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            ace_density_kernel<<<(unsigned)((V + 255) / 256), 256, 0, s>>>(
+                a.xyz, a.type, a.box, a.bins, a.geo, a.ace_cut * a.ace_cut, md * md, a.ace_b, a.ace_k, a.ace_a,
+                a.dens);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
         }
     }
     mix_terms_kernel<<<(unsigned)((V + 255) / 256), 256, 0, s>>>(a.flags, a.dens, a.emat, a.n_types, a.K,
                                                                   a.term_set, V, a.rgrid);
     return cudaGetLastError();
+}
+
+// counting sort of the atoms into bins of edge cut * (1 + 1e-6) (at least
+// 1e-3 A), atoms in index order inside each bin
+void bin_atoms(const double* xyz, int n, double cut, HostAtomBins& out) {
+    out.size = std::max(cut * (1.0 + 1e-6), 1e-3);
+    double hi[3] = {0, 0, 0};
+    for (int d = 0; d < 3; ++d) out.lo[d] = n > 0 ? xyz[d] : 0.0;
+    for (int d = 0; d < 3; ++d) hi[d] = out.lo[d];
+    for (int i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d) {
+            out.lo[d] = std::min(out.lo[d], xyz[3 * i + d]);
+            hi[d] = std::max(hi[d], xyz[3 * i + d]);
+        }
+    for (int d = 0; d < 3; ++d) out.nb[d] = (int)std::floor((hi[d] - out.lo[d]) / out.size) + 1;
+    const int nbins = out.nb[0] * out.nb[1] * out.nb[2];
+    std::vector<int> bin(n);
+    out.start.assign(nbins + 1, 0);
+    for (int i = 0; i < n; ++i) {
+        int b[3];
+        for (int d = 0; d < 3; ++d) {
+            b[d] = (int)std::floor((xyz[3 * i + d] - out.lo[d]) / out.size);
+            b[d] = std::min(std::max(b[d], 0), out.nb[d] - 1);
+        }
+        bin[i] = (b[0] * out.nb[1] + b[1]) * out.nb[2] + b[2];
+        ++out.start[bin[i] + 1];
+    }
+    for (int k = 0; k < nbins; ++k) out.start[k + 1] += out.start[k];
+    out.atoms.assign(n, 0);
+    std::vector<int> fill(out.start.begin(), out.start.end() - 1);
+    for (int i = 0; i < n; ++i) out.atoms[fill[bin[i]]++] = i;
 }
 
 }  // namespace fftdock

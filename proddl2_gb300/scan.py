@@ -75,36 +75,42 @@ def _ptr(a):
     return C.c_void_p(a.ctypes.data) if a is not None else None
 
 
+def native_config(config: ScanConfig):
+    """The C ``fftdock_config`` of a ScanConfig (and the array it points to)."""
+    cfg = _lib.Config()
+    _lib.lib().fftdock_config_init(C.byref(cfg))
+    cfg.grid_n = int(config.grid_n)
+    cfg.grid_step = float(config.grid_step)
+    cfg.term_set = TERM_SETS[config.term_set]
+    cfg.peaks_per_rot = int(config.peaks_per_rot)
+    cfg.max_trans_inp = int(config.max_trans_inp)
+    cfg.max_val_corr = float(config.max_val_corr)
+    cfg.rot_batch = int(config.rot_batch)
+    cfg.n_types = int(config.n_types)
+    ace = None
+    if config.ace_matrix is not None:
+        ace = np.ascontiguousarray(config.ace_matrix, dtype=np.float64)
+        cfg.ace_matrix = ace.ctypes.data_as(C.POINTER(C.c_double))
+    cfg.shape_core_radius = float(config.shape_core_radius)
+    cfg.shape_surface_width = float(config.shape_surface_width)
+    cfg.ace_b, cfg.ace_k, cfg.ace_a, cfg.ace_cut = (float(config.ace_b), float(config.ace_k),
+                                                    float(config.ace_a), float(config.ace_cut))
+    cfg.device = int(config.device)
+    cfg.pencil_mode = PENCIL_MODES[config.pencil_mode]
+    cfg.precision = {"fp32": _lib.FFTDOCK_PREC_FP32, "bf16": _lib.FFTDOCK_PREC_BF16_SPECTRA}[config.precision]
+    cfg.cluster_trans = 1 if config.cluster_trans else 0
+    cfg.cluster_radius = float(config.cluster_radius)
+    cfg.cluster_order = {"reference": 0, "best_first": 1}[config.cluster_order]
+    return cfg, ace
+
+
 class FFTScan:
     """One receptor/ligand pair on one GPU (C ABI ``fftdock_ctx``)."""
 
     def __init__(self, config: ScanConfig):
         self.lib = _lib.lib()
         self.config = config
-        cfg = _lib.Config()
-        self.lib.fftdock_config_init(C.byref(cfg))
-        cfg.grid_n = int(config.grid_n)
-        cfg.grid_step = float(config.grid_step)
-        cfg.term_set = TERM_SETS[config.term_set]
-        cfg.peaks_per_rot = int(config.peaks_per_rot)
-        cfg.max_trans_inp = int(config.max_trans_inp)
-        cfg.max_val_corr = float(config.max_val_corr)
-        cfg.rot_batch = int(config.rot_batch)
-        cfg.n_types = int(config.n_types)
-        self._ace = None
-        if config.ace_matrix is not None:
-            self._ace = np.ascontiguousarray(config.ace_matrix, dtype=np.float64)
-            cfg.ace_matrix = self._ace.ctypes.data_as(C.POINTER(C.c_double))
-        cfg.shape_core_radius = float(config.shape_core_radius)
-        cfg.shape_surface_width = float(config.shape_surface_width)
-        cfg.ace_b, cfg.ace_k, cfg.ace_a, cfg.ace_cut = (float(config.ace_b), float(config.ace_k),
-                                                        float(config.ace_a), float(config.ace_cut))
-        cfg.device = int(config.device)
-        cfg.pencil_mode = PENCIL_MODES[config.pencil_mode]
-        cfg.precision = {"fp32": _lib.FFTDOCK_PREC_FP32, "bf16": _lib.FFTDOCK_PREC_BF16_SPECTRA}[config.precision]
-        cfg.cluster_trans = 1 if config.cluster_trans else 0
-        cfg.cluster_radius = float(config.cluster_radius)
-        cfg.cluster_order = {"reference": 0, "best_first": 1}[config.cluster_order]
+        cfg, self._ace = native_config(config)
         h = C.c_void_p()
         rc = self.lib.fftdock_create(C.byref(cfg), C.byref(h))
         self._h = h

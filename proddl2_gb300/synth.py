@@ -136,10 +136,29 @@ def make_pair(n_rec, n_lig, n_rot, seed, n_types=18):
     return Pair(rec, lig, rots, ace_matrix(n_types, seed * 4 + 4))
 
 
+def uneven_pairs(n_pairs, seed, rec_range=(800, 6000), lig_range=(300, 2000), n_types=18):
+    """Pairs with log-uniform receptor and ligand sizes (the batched-workload
+    generator): a list of (receptor, ligand) molecules in scan frames."""
+    rng = _rng(seed)
+    out = []
+    for i in range(n_pairs):
+        nr = int(round(math.exp(rng.uniform(math.log(rec_range[0]), math.log(rec_range[1])))))
+        nl = int(round(math.exp(rng.uniform(math.log(lig_range[0]), math.log(lig_range[1])))))
+        rec = molecule(nr, seed * 100003 + 2 * i + 1, n_types)
+        lig = molecule(nl, seed * 100003 + 2 * i + 2, n_types)
+        rec.xyz = rec.xyz - box_centre(rec.xyz)
+        lig.xyz = lig.xyz - diameter_centre(lig.xyz)
+        out.append((rec, lig))
+    return out
+
+
 # Workloads quoted by the scan benchmarks: name -> (n_rec, n_lig, N, h, terms, n_rot, batch, peaks)
 WORKLOADS = {
     "shape64": dict(n_rec=1800, n_lig=450, grid_n=64, grid_step=1.2, term_set="shape",
                     n_rot=2000, rot_batch=64, peaks=4, top=100),
     "shape_ace128": dict(n_rec=4000, n_lig=1500, grid_n=128, grid_step=1.2, term_set="shape_ace",
                          n_rot=9000, rot_batch=64, peaks=4, top=100),
+    # many uneven pairs: receptors 800-6000 / ligands 300-2000 atoms (log-uniform),
+    # grid edge per pair from pair_grid (48-144), shape + 18 desolvation terms
+    "pairs256": dict(n_pairs=256, grid_step=1.2, term_set="shape_ace", n_rot=3000, rot_batch=64, peaks=4),
 }

@@ -267,6 +267,53 @@ int fftdock_write_scan_records(const char* path, int32_t n_rot, const double* ro
                                const fftdock_peak* peaks, const int32_t* n_peaks, int32_t append);
 
 /* ------------------------------------------------------------------------
+ * Pre-scan frame set-up of a pair (host only): MolStruct::
+ * moveIntoReferencePositions (include/PRODDL/docking_molstruct.hpp:199-252)
+ * and the FFT size rule of FFTCorrelator::init (docking_fft.hpp:535-553).
+ * Spins the ligand about its centre of mass by the Euler angles (s, 3.7877 s,
+ * -4.513432 s), moves both molecules into the receptor box's frame, moves
+ * the ligand's diameter centre to the origin, pads the box by 2 h + ligand
+ * size / 2 + cutOffFft and sizes the grid per axis.  The receptor box is
+ * axis-aligned (FFTDOCK_BOX_AXES: the reference's Box with fixed
+ * directions) or given by the caller (FFTDOCK_BOX_GIVEN: e.g. the minimum-
+ * volume box the reference gets from its gdiam library: 3 direction rows and
+ * the corners (0,0,0) and (1,1,1)).  The frames written out are the ones
+ * fftdock_write_rigid undoes.
+ * ------------------------------------------------------------------------ */
+enum {
+    FFTDOCK_BOX_AXES = 0,
+    FFTDOCK_BOX_GIVEN = 1
+};
+
+typedef struct fftdock_frame_setup_in {
+    int32_t n_rec;
+    const double* rec_xyz;       /* [n_rec][3], original frame */
+    int32_t n_lig;
+    const double* lig_xyz;       /* [n_lig][3], original frame */
+    const double* lig_mass;      /* [n_lig] or NULL (unit masses) */
+    double grid_step;            /* gridStep */
+    double cut_off_fft;          /* cutOffFft */
+    double starting_spin;        /* startingSpin (radians; reference default 23.3734432) */
+    int32_t box_mode;            /* FFTDOCK_BOX_* */
+    const double* box_dirs;      /* GIVEN: [3][3] direction rows */
+    const double* box_corners;   /* GIVEN: corner (0,0,0) then corner (1,1,1), original frame */
+    const double* lig_diam;      /* optional: the ligand diameter's end points (6 doubles, frame after
+                                    step 2); NULL: the exact farthest pair */
+} fftdock_frame_setup_in;
+
+typedef struct fftdock_frame {
+    double rec_frame[12];        /* original -> scan frame (row-major rotation, then vector) */
+    double lig_frame[12];
+    double lig_size;             /* ligand diameter */
+    double min_box[6];           /* padded receptor box in the scan frame: low xyz, high xyz */
+    int32_t fft_size[3];         /* FFTW_Size::findBestSize per axis */
+    int32_t grid_n;              /* smallest built cubic edge >= the largest fft_size (0: none) */
+} fftdock_frame;
+
+/* rec_out [n_rec][3] and lig_out [n_lig][3] receive the moved atoms. */
+int fftdock_frame_setup(const fftdock_frame_setup_in* in, double* rec_out, double* lig_out, fftdock_frame* out);
+
+/* ------------------------------------------------------------------------
  * Many pairs in one CUDA graph.  No counterpart in the reference (it runs
  * one pair per process).  Every pair's atoms and rotations are staged on the
  * device once; the whole workload -- per pair the receptor grids and

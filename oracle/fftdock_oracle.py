@@ -692,3 +692,96 @@ def pack_rigid(poses, rec_frame, lig_frame):
         ang = matrix_to_euler(rr)
         out += struct.pack("<7f", v, *ang, *tt)
     return out
+
+
+# ----------------------------------------------------------------------------
+# Pre-scan frame set-up: MolStruct::moveIntoReferencePositions
+# (docking_molstruct.hpp:199-252) with Geom/bounding.hpp:27-250 and the
+# RotationTranslation algebra of Geom/transformation.hpp:135-345
+# ----------------------------------------------------------------------------
+def rt_apply(t, p):
+    """RotationTranslation::operator()(Point): product(R, p) + v."""
+    r, v = t
+    return mat_vec(r, p) + np.asarray(v)
+
+
+def centre_of_mass(xyz, mass):
+    """MolStruct::centerOfMass (:112-126): x += p_i m_i, then x /= sum(m)."""
+    x = np.zeros(3)
+    tot = 0.0
+    for m in mass:
+        tot = tot + float(m)
+    for p, m in zip(np.asarray(xyz, dtype=np.float64), mass):
+        x = x + p * float(m)
+    return x / tot
+
+
+def farthest_pair(xyz):
+    """Exact diameter end points: the first pair (i < j, row order) of
+    largest ((dx^2 + dy^2) + dz^2)."""
+    xyz = np.asarray(xyz, dtype=np.float64)
+    best, pair = -1.0, (0, 0)
+    for i in range(len(xyz)):
+        d = xyz[i + 1:] - xyz[i]
+        if len(d) == 0:
+            continue
+        d2 = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]
+        j = int(np.argmax(d2))
+        if d2[j] > best:
+            best, pair = float(d2[j]), (i, i + 1 + j)
+    return xyz[pair[0]].copy(), xyz[pair[1]].copy()
+
+
+def axis_box(xyz):
+    """Box(points, fixedDirections=true) (bounding.hpp:166-182): min/max
+    corners and identity directions."""
+    xyz = np.asarray(xyz, dtype=np.float64)
+    return np.eye(3), xyz.min(axis=0), xyz.max(axis=0)
+
+
+def frame_setup(rec_xyz, lig_xyz, lig_mass, grid_step, cut_off_fft, starting_spin=23.3734432, box=None,
+                lig_diam=None):
+    """The scan frame of a pair.  ``box`` = (directions 3x3 rows, corner
+    (0,0,0), corner (1,1,1)) in the original frame; None = axis-aligned box.
+    ``lig_diam`` = the diameter's two end points; None = exact farthest pair.
+    Returns (rec_out, lig_out, rec_frame, lig_frame, lig_size, min_box (2x3),
+    fft_size per axis)."""
+    rec = np.array(rec_xyz, dtype=np.float64).reshape(-1, 3)
+    lig = np.array(lig_xyz, dtype=np.float64).reshape(-1, 3)
+    mass = np.ones(len(lig)) if lig_mass is None else np.asarray(lig_mass, dtype=np.float64)
+    ident = (np.eye(3), np.zeros(3))
+    tr_rec, tr_lig = ident, ident
+    # randomizeLigandOrientation (:213-225)
+    s = float(starting_spin)
+    spin = euler_to_matrix((s, s * 3.7877, s * (-4.513432)))
+    cm = centre_of_mass(lig, mass)
+    t = (spin, cm)                                   # Translation(cm) * Rotation
+    t = (t[0], mat_vec(t[0], -1.0 * cm) + t[1])      # ... * Translation(-cm)
+    lig = np.array([rt_apply(t, p) for p in lig])
+    tr_lig = rt_compose(t, tr_lig)
+    # moveIntoMinBox (:199-245)
+    dirs, c0, c1 = axis_box(rec) if box is None else (np.asarray(box[0], dtype=np.float64).reshape(3, 3),
+                                                       np.asarray(box[1], dtype=np.float64),
+                                                       np.asarray(box[2], dtype=np.float64))
+    centre = -(c0 + (c1 - c0) / 2.0)
+    tb = (dirs, mat_vec(dirs, centre))               # Rotation(dirs) * Translation(-centre)
+    d0, d1 = rt_apply(tb, c0), rt_apply(tb, c1)
+    rec = np.array([rt_apply(tb, p) for p in rec])
+    lig = np.array([rt_apply(tb, p) for p in lig])
+    tr_rec = rt_compose(tb, tr_rec)
+    tr_lig = rt_compose(tb, tr_lig)
+    p, q = farthest_pair(lig) if lig_diam is None else (np.asarray(lig_diam[0], dtype=np.float64),
+                                                         np.asarray(lig_diam[1], dtype=np.float64))
+    tl = -((q + p) / 2.0)
+    lig = np.array([tl + x for x in lig])
+    tr_lig = (tr_lig[0], tr_lig[1] + tl)             # Translation * RotationTranslation
+    dd = q - p
+    lig_size = math.sqrt((dd[0] * dd[0] + dd[1] * dd[1]) + dd[2] * dd[2])
+    pad = (grid_step * 2.0 + lig_size / 2.0) + cut_off_fft
+    lo, hi = d0 - pad, d1 + pad
+    # FFTCorrelator::init (docking_fft.hpp:535-553): toLogical of the upper
+    # corner in a geometry whose zero is the lower corner, then findBestSize
+    zero_h = lo - grid_step
+    start = [int((hi[d] - zero_h[d]) / grid_step) - 1 for d in range(3)]
+    fft = [find_best_size(v) for v in start]
+    return rec, lig, tr_rec, tr_lig, lig_size, np.stack([lo, hi]), fft

@@ -65,6 +65,26 @@ class Config(C.Structure):
     ]
 
 
+FFTDOCK_BOX_AXES = 0
+FFTDOCK_BOX_GIVEN = 1
+
+
+class FrameIn(C.Structure):
+    _fields_ = [
+        ("n_rec", C.c_int32), ("rec_xyz", C.c_void_p),
+        ("n_lig", C.c_int32), ("lig_xyz", C.c_void_p), ("lig_mass", C.c_void_p),
+        ("grid_step", C.c_double), ("cut_off_fft", C.c_double), ("starting_spin", C.c_double),
+        ("box_mode", C.c_int32), ("box_dirs", C.c_void_p), ("box_corners", C.c_void_p), ("lig_diam", C.c_void_p),
+    ]
+
+
+class Frame(C.Structure):
+    _fields_ = [
+        ("rec_frame", C.c_double * 12), ("lig_frame", C.c_double * 12), ("lig_size", C.c_double),
+        ("min_box", C.c_double * 6), ("fft_size", C.c_int32 * 3), ("grid_n", C.c_int32),
+    ]
+
+
 N_SIZES = 10
 BUILT_SIZES = (16, 24, 32, 48, 64, 80, 96, 112, 128, 144)
 
@@ -163,6 +183,7 @@ SIGNATURES = {
     "fftdock_gather_list": (C.c_int, [C.c_char_p, C.c_int32, _P, C.POINTER(C.c_int32)]),
     "fftdock_write_rigid": (C.c_int, [C.c_char_p, _P, C.c_int32, _P, _P, C.c_int32]),
     "fftdock_write_scan_records": (C.c_int, [C.c_char_p, C.c_int32, _P, C.c_int32, _P, _P, C.c_int32]),
+    "fftdock_frame_setup": (C.c_int, [C.POINTER(FrameIn), _P, _P, C.POINTER(Frame)]),
     "fftdock_scan_pairs": (C.c_int, [C.POINTER(Config), C.c_int32, C.POINTER(PairDesc), C.c_int32,
                                      C.POINTER(PairsReport)]),
     "fftdock_pairs_last_error": (C.c_char_p, []),

@@ -13,7 +13,8 @@ template <int N> struct SizeOpsImpl {
     static constexpr int H = N / 2 + 1;
 
     static size_t pencil_smem(int K, int n_ent) {
-        return (size_t)2 * N * 32 * sizeof(float2) + N * sizeof(float2) + ((size_t)K * N + 1) * sizeof(int32_t) +
+        return (size_t)PencilTraits<N>::BUFS * N * 32 * sizeof(float2) + N * sizeof(float2) +
+               ((size_t)K * N + 1) * sizeof(int32_t) +
                (size_t)n_ent * sizeof(uint32_t);
     }
     static size_t plane_smem() { return (size_t)N * H * sizeof(float2) + N * sizeof(float2) + (size_t)G * KC * 8; }

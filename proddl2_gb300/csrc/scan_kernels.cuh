@@ -40,11 +40,17 @@ template <> struct SizeTraits<128> { static constexpr int G = 8, GR = 8; };
 template <> struct SizeTraits<144> { static constexpr int G = 12, GR = 6; };
 
 // Pencil kernel occupancy: exchange buffers (2: one barrier per term; 1: two
-// barriers per term but 32 KB less shared memory) and the CTAs per SM its
-// launch bounds ask for.  At 128^3 a single buffer lets three CTAs share an
-// SM (80 registers) and measured 6 % faster than two buffers at two CTAs.
+// barriers per term but N*32 complex less shared memory) and the CTAs per SM
+// its launch bounds ask for (which caps the registers).  Chosen per edge from
+// timed scans on GB300 (shape + 18 terms; pencil-kernel time against the
+// two-buffer, unbounded form): 64 -22 %, 80 -11 %, 96 -12 %, 128 -6 %,
+// 144 -25 %; 112 gained nothing.
 template <int N> struct PencilTraits { static constexpr int BUFS = 2, MINB = 1; };
+template <> struct PencilTraits<64> { static constexpr int BUFS = 1, MINB = 4; };
+template <> struct PencilTraits<80> { static constexpr int BUFS = 1, MINB = 4; };
+template <> struct PencilTraits<96> { static constexpr int BUFS = 1, MINB = 4; };
 template <> struct PencilTraits<128> { static constexpr int BUFS = 1, MINB = 3; };
+template <> struct PencilTraits<144> { static constexpr int BUFS = 2, MINB = 2; };
 
 
 // toLogical: int((x - zero_h) / h) - 1, truncation toward zero, no FMA.

@@ -309,8 +309,10 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G, PencilTraits<N>::MINB) 
 // K3: plane kernel.  CTA = one (rotation, x) plane.  Inverse transform along
 // ky (columns kz; the real DC and Nyquist columns share one complex column),
 // then the half-spectrum rows along kz are turned into N reals through one
-// N/2-point complex transform each, and every real value is offered to a warp
-// top-KC.  (FFTW c2r of FFTCorrelator::correlate + CorrelationProcessor::
+// N/2-point complex transform each; the plane's KC smallest (value, offset)
+// cells are then selected exactly: the threads' own minima give an upper
+// bound on the KC-th value and only cells at or below it reach a warp top-KC.
+// (FFTW c2r of FFTCorrelator::correlate + CorrelationProcessor::
 // selectIntoQueue, docking_fft.hpp:452-468.)
 // ---------------------------------------------------------------------------
 template <int N, bool PMAJOR, bool DBG>
@@ -332,8 +334,13 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     float2* tws = plane + N * H;                          // [N]
     float* lv_s = reinterpret_cast<float*>(tws + N);      // [G*KC]
     int* li_s = reinterpret_cast<int*>(lv_s + G * KC);    // [G*KC]
-    __shared__ float thr_v[32];                           // each warp's current KC-th value
-    __shared__ int thr_i[32];
+    constexpr int PCAND = 256;                            // candidate list capacity
+    __shared__ float tmin_v[32 * G];                      // each thread's best cell
+    __shared__ int tmin_i[32 * G];
+    __shared__ float cand_sv[PCAND];
+    __shared__ int cand_si[PCAND];
+    __shared__ float bound_v;
+    __shared__ int bound_i, n_cand;
 
     const int x = blockIdx.x;
     const int q = blockIdx.y;
@@ -392,16 +399,12 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     }
     __syncthreads();
 
-    if (l == 0) {
-        thr_v[w] = INFINITY;
-        thr_i[w] = 0x7fffffff;
-    }
-    __syncthreads();
-
-    // rows: C2R along kz via an N/2-point complex inverse DFT, then top-k
+    // rows: C2R along kz via an N/2-point complex inverse DFT.  Each row's N
+    // real outputs replace its spectrum in shared memory, and every thread
+    // keeps the smallest (value, offset) it produced.
     const int gi = w / GR, m = w % GR;
-    WarpTopK tk;
-    tk.init();
+    float bmin_v = INFINITY;
+    int bmin_i = 0x7fffffff;
 #pragma unroll 1
     for (int ro = 0; ro < ROUNDS; ++ro) {
         const int y = ro * ROWS + gi * 32 + l;
@@ -423,20 +426,6 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
             v[r] = yk;
         }
         __syncthreads();
-        // a value worse than any warp's KC-th best cannot be in the plane's
-        // top KC: filter with the best threshold published in earlier rounds
-        // (complete before the barrier above, rewritten only after the next)
-        if (ro > 0) {
-            float bv = tk.tv;
-            int bi = tk.ti;
-            for (int k = 0; k < G; ++k) {
-                const float ov = thr_v[k];
-                const int oi = thr_i[k];
-                if (better(ov, oi, bv, bi)) { bv = ov; bi = oi; }
-            }
-            tk.tv = bv;
-            tk.ti = bi;
-        }
         dft<R1R, +1>(v);
         if (valid) {
 #pragma unroll
@@ -445,6 +434,7 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
         __syncthreads();
         float2 out[R1R];
         if (valid) line_pass2<PR, +1, 2, 1>(row, m, 0, tws, out);
+        __syncthreads();  // the row's spectrum is consumed: its slots take the real outputs
         const int rowbase = (x * N + y) * N;
 #pragma unroll
         for (int i = 0; i < PR::NB; ++i)
@@ -452,19 +442,91 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
             for (int r = 0; r < GR; ++r) {
                 const int mm = m + GR * i + R1R * r;
                 const float2 o = out[i * GR + r];
-                const float v0 = valid ? o.x : INFINITY;
-                const float v1 = valid ? o.y : INFINITY;
-                if constexpr (DBG) {
-                    if (valid)
-                        reinterpret_cast<float2*>(dbg + (size_t)q * N * N * N + rowbase)[mm] = o;
+                if (valid) {
+                    row[mm] = o;
+                    if constexpr (DBG) reinterpret_cast<float2*>(dbg + (size_t)q * N * N * N + rowbase)[mm] = o;
+                    if (better(o.x, rowbase + 2 * mm, bmin_v, bmin_i)) { bmin_v = o.x; bmin_i = rowbase + 2 * mm; }
+                    if (better(o.y, rowbase + 2 * mm + 1, bmin_v, bmin_i)) { bmin_v = o.y; bmin_i = rowbase + 2 * mm + 1; }
                 }
-                tk.offer(v0, valid ? rowbase + 2 * mm : 0x7fffffff, l);
-                tk.offer(v1, valid ? rowbase + 2 * mm + 1 : 0x7fffffff, l);
             }
+    }
+
+    // Selection.  The KC-th best of the threads' minima bounds the plane's
+    // KC-th best from above (at least KC cells lie at or below it), so only
+    // cells at or below it can enter the plane's top KC.
+    tmin_v[tid] = bmin_v;
+    tmin_i[tid] = bmin_i;
+    if (tid == 0) n_cand = 0;
+    __syncthreads();
+    WarpTopK tk;
+    if (w == 0) {
+        tk.init();
+        for (int base = 0; base < 32 * G; base += 32) tk.offer(tmin_v[base + l], tmin_i[base + l], l);
         if (l == 0) {
-            thr_v[w] = tk.tv;
-            thr_i[w] = tk.ti;
+            bound_v = tk.tv;
+            bound_i = tk.ti;
         }
+    }
+    __syncthreads();
+    const float tv = bound_v;
+    const int ti = bound_i;
+    // every thread re-reads its own cells (the positions the row pass gave it)
+#pragma unroll 1
+    for (int ro = 0; ro < ROUNDS; ++ro) {
+        const int y = ro * ROWS + gi * 32 + l;
+        if (y >= N) continue;
+        const float2* row = plane + y * H;
+        const int rowbase = (x * N + y) * N;
+#pragma unroll
+        for (int i = 0; i < PR::NB; ++i)
+#pragma unroll
+            for (int r = 0; r < GR; ++r) {
+                const int mm = m + GR * i + R1R * r;
+                const float2 o = row[mm];
+                if (!better(tv, ti, o.x, rowbase + 2 * mm)) {
+                    const int at = atomicAdd(&n_cand, 1);
+                    if (at < PCAND) { cand_sv[at] = o.x; cand_si[at] = rowbase + 2 * mm; }
+                }
+                if (!better(tv, ti, o.y, rowbase + 2 * mm + 1)) {
+                    const int at = atomicAdd(&n_cand, 1);
+                    if (at < PCAND) { cand_sv[at] = o.y; cand_si[at] = rowbase + 2 * mm + 1; }
+                }
+            }
+    }
+    __syncthreads();
+    const int nc = n_cand;
+    if (nc <= PCAND) {
+        if (w == 0) {
+            tk.init();
+            for (int base = 0; base < nc; base += 32) {
+                const int e = base + l;
+                tk.offer(e < nc ? cand_sv[e] : INFINITY, e < nc ? cand_si[e] : 0x7fffffff, l);
+            }
+            if (l < KC) {
+                cand_v[((size_t)q * N + x) * KC + l] = tk.lv;
+                cand_i[((size_t)q * N + x) * KC + l] = tk.li;
+            }
+        }
+        return;
+    }
+    // many cells tie at the bound (a flat plane): every warp offers its own
+    // cells, then warp 0 merges the warps' lists
+    tk.init();
+#pragma unroll 1
+    for (int ro = 0; ro < ROUNDS; ++ro) {
+        const int y = ro * ROWS + gi * 32 + l;
+        const bool valid = y < N;
+        const float2* row = plane + (valid ? y : 0) * H;
+        const int rowbase = (x * N + y) * N;
+#pragma unroll
+        for (int i = 0; i < PR::NB; ++i)
+#pragma unroll
+            for (int r = 0; r < GR; ++r) {
+                const int mm = m + GR * i + R1R * r;
+                const float2 o = valid ? row[mm] : make_float2(INFINITY, INFINITY);
+                tk.offer(o.x, valid ? rowbase + 2 * mm : 0x7fffffff, l);
+                tk.offer(o.y, valid ? rowbase + 2 * mm + 1 : 0x7fffffff, l);
+            }
     }
     if (l < KC) {
         lv_s[w * KC + l] = tk.lv;

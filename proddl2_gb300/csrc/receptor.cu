@@ -122,16 +122,9 @@ __global__ void mix_terms_kernel(const int* __restrict__ flags, const double* __
         rgrid[cell] = -s;
         return;
     }
-    // the cell's type densities once into registers (n_types <= 32), then
-    // every term sums them in type order
-    double g[32];
-#pragma unroll
-    for (int u = 0; u < 32; ++u) g[u] = u < n_types ? dens[(size_t)u * V + cell] : 0.0;
     for (int t = 0; t < K; ++t) {
         double d = 0.0;
-#pragma unroll
-        for (int u = 0; u < 32; ++u)
-            if (u < n_types) d = __dadd_rn(d, __dmul_rn(__ldg(&emat[u * n_types + t]), g[u]));
+        for (int u = 0; u < n_types; ++u) d = __dadd_rn(d, __dmul_rn(emat[u * n_types + t], dens[(size_t)u * V + cell]));
         rgrid[(size_t)t * V + cell] = __dsub_rn(d, s);
     }
 }

@@ -52,7 +52,12 @@ enum {
  * docking_app.hpp:54-66, plus this library's shape/desolvation terms) */
 enum {
     FFTDOCK_TERMS_SHAPE = 1,     /* surface +1 / core -15 receptor grid, unit ligand weights; K = 1 */
-    FFTDOCK_TERMS_SHAPE_ACE = 2  /* shape + n_types ACE-style desolvation grids, folded to K = n_types */
+    FFTDOCK_TERMS_SHAPE_ACE = 2, /* shape + n_types ACE-style desolvation grids, folded to K = n_types */
+    FFTDOCK_TERMS_LJ_COMP = 3,   /* the reference's "ljComp": soft-core LJ repulsion + attraction
+                                    (MolForceLJComp, docking_molforce.hpp:456-600), K = 2; atoms and
+                                    parameters through fftdock_set_pair_lj */
+    FFTDOCK_TERMS_LJ_AVG = 4     /* the reference's "ljAvg": soft-core LJ with ligand-averaged
+                                    parameters (MolForceLJ, docking_molforce.hpp:375-455), K = 1 */
 };
 
 /* precision of the stored receptor spectra (FFT pencil stage): FP32 pairs,
@@ -115,6 +120,9 @@ typedef struct fftdock_config {
     int32_t cluster_trans;       /* 1: cluster each rotation's queue ("doClusterTranslations") */
     int32_t cluster_order;       /* FFTDOCK_CLUSTER_ORDER_* */
     double cluster_radius;       /* "clusterRadiusTrans" (A), reference default 5 */
+    int32_t lj_mix;              /* LJ term sets: sigma combination rule (PotentialsT::LJ_MIX_0 = 0:
+                                    arithmetic, LJ_MIX_1 = 1: geometric; ljComp requires 1) */
+    double lj_cut;               /* LJ term sets: field cutoff ("cutOffFft"), grid length units */
 } fftdock_config;
 
 /* one selected translation; the reference's TranValue
@@ -145,6 +153,18 @@ int fftdock_find_best_size(int32_t start_n, int32_t* result);
 int fftdock_create(const fftdock_config* cfg, fftdock_ctx** out);
 void fftdock_destroy(fftdock_ctx* ctx);
 const char* fftdock_last_error(const fftdock_ctx* ctx);
+
+/* The LJ term sets' inputs (the reference's MolForceParams pos/eps/sigma/
+ * alpha of both molecules): receptor atoms in the grid frame with sigma,
+ * eps, alpha; ligand atoms (rotation centre at the origin) with sigma, eps.
+ * Builds the receptor fields -- per atom SoftCoreLJRep/SoftCoreLJAttr
+ * (ljComp) or SoftCoreLJ with the force-shifted cutoff (ljAvg) against the
+ * ligand's mean sigma/eps, projected like ProjectorRadialField -- and the
+ * ligand weights (ljComp: sqrt(eps) sigma^6 and sqrt(eps) sigma^3; ljAvg:
+ * 1).  Replaces fftdock_set_receptor / fftdock_set_ligand for these sets. */
+int fftdock_set_pair_lj(fftdock_ctx* ctx, int32_t n_rec, const double* rec_xyz, const double* rec_sigma,
+                        const double* rec_eps, const double* rec_alpha, int32_t n_lig, const double* lig_xyz,
+                        const double* lig_sigma, const double* lig_eps);
 
 /* Receptor atoms in the grid frame (grid centred on the origin).  Builds the
  * K receptor term grids and keeps their spectra on the device

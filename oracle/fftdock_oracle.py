@@ -61,6 +61,8 @@ import numpy as np
 # ----------------------------------------------------------------------------
 TERMS_SHAPE = 1        # K = 1: -S correlated with all ligand atoms
 TERMS_SHAPE_ACE = 2    # K = n_types (folded): D_t - S correlated with type-t atoms
+TERMS_LJ_COMP = 3      # "ljComp": soft-core LJ repulsion + attraction, K = 2
+TERMS_LJ_AVG = 4       # "ljAvg": soft-core LJ with ligand-averaged parameters, K = 1
 
 SHAPE_SURFACE = 1.0
 SHAPE_CORE = -15.0
@@ -365,6 +367,131 @@ def ligand_term_weights(lig_type, tp: TermParams, folded=True):
     if folded:
         return w
     return np.concatenate([np.ones((n, 1)), w], axis=1)
+
+
+# ----------------------------------------------------------------------------
+# The reference's own FFT potentials: MolForceLJComp / MolForceLJ
+# (docking_molforce.hpp:375-600, docking_app.hpp:52-66) with SoftCoreLJ,
+# SoftCoreLJRep, SoftCoreLJAttr (potentials_inc.hpp:142-354)
+# ----------------------------------------------------------------------------
+@dataclass
+class LjParams:
+    rec_sigma: np.ndarray
+    rec_eps: np.ndarray
+    rec_alpha: np.ndarray
+    lig_sigma: np.ndarray
+    lig_eps: np.ndarray
+    mix: int = 1           # PotentialsT::LJ_MIX_0 / LJ_MIX_1
+    cut: float = 9.0       # cutOffFft
+
+
+def _pow3(x):
+    return (x * x) * x
+
+
+def _pow6(x):
+    t = (x * x) * x
+    return t * t
+
+
+def _mean(v):
+    t = 0.0
+    for x in np.asarray(v, dtype=np.float64):
+        t = t + float(x)
+    return t / float(len(v))
+
+
+def lj_atom_constants(lj: LjParams, term_set):
+    """Per receptor atom (as6, 4es6, 4es12, fshift, gshift), computed in the
+    reference's operation order.  ljComp: the constants shared by
+    SoftCoreLJRep and SoftCoreLJAttr (no shift); ljAvg: SoftCoreLJ with
+    CUT_POLICY_SHIFT_FORCE."""
+    sig_l = _mean(lj.lig_sigma)
+    out = []
+    cut = float(lj.cut)
+    cut2 = cut * cut
+    for si, ei, ai in zip(np.asarray(lj.rec_sigma, float), np.asarray(lj.rec_eps, float),
+                          np.asarray(lj.rec_alpha, float)):
+        if term_set == TERMS_LJ_COMP:
+            sigma = math.sqrt(si)
+            sigma_alpha = math.sqrt(si * sig_l)
+            eps = math.sqrt(ei)
+            s6 = _pow6(sigma)
+            as6 = ai * _pow6(sigma_alpha)
+            e6 = 4.0 * eps * s6
+            e12 = e6 * s6
+            out.append((as6, e6, e12, 0.0, 0.0))
+        else:
+            eps_l = _mean(lj.lig_eps)
+            sigma = (si + sig_l) / 2.0 if lj.mix == 0 else math.sqrt(si * sig_l)
+            eps = math.sqrt(ei * eps_l)
+            s6 = _pow6(sigma)
+            as6 = ai * s6
+            e6 = 4.0 * eps * s6
+            e12 = e6 * s6
+            # g2 at the cutoff with no shift yet (potentials_inc.hpp:226-234)
+            r6 = _pow3(cut2)
+            A = r6 + as6
+            B = s6 / (r6 + as6) - 1.0
+            C = -6.0 * (cut2 * cut2) * (e6 * A * B + e12) / _pow3(A)
+            gcut = cut * C + cut * (0.0 / math.sqrt(cut2))
+            fshift = -((e12 / A - e6) / A + 0.0 + 0.0 * math.sqrt(cut2))
+            gshift = -gcut
+            fshift = fshift - gshift * cut
+            out.append((as6, e6, e12, fshift, gshift))
+    return np.array(out)
+
+
+def lj_field(c, r2, term):
+    """f2(r^2) of one atom's constants c: term 0 = ljComp repulsion, 1 =
+    ljComp attraction, 'avg' = ljAvg."""
+    as6, e6, e12, fshift, gshift = c
+    A = _pow3(r2) + as6
+    if term == 0:
+        return e12 / A / A
+    if term == 1:
+        return -e6 / A
+    return (e12 / A - e6) / A + fshift + gshift * np.sqrt(r2)
+
+
+def lj_receptor_terms(geom, rec_xyz, lj: LjParams, term_set):
+    """K receptor grids of the reference's LJ potentials, projected like
+    ProjectorRadialField::projectFields (atoms in order, r^2 clamped to
+    (h/4)^2 inside the cropped box, r^2 <= cut^2)."""
+    n = geom.n
+    consts = lj_atom_constants(lj, term_set)
+    k = 2 if term_set == TERMS_LJ_COMP else 1
+    grids = np.zeros((k, n, n, n))
+    md = geom.h / 4.0
+    md2 = md * md
+    cut = float(lj.cut)
+    for c, cen in zip(consts, np.asarray(rec_xyz, dtype=np.float64)):
+        got = _cells_in_box(geom, cen, cut)
+        if got is None:
+            continue
+        sl, r2 = got
+        inside = r2 <= cut * cut
+        rr = np.where(r2 < md2, md2, r2)
+        if term_set == TERMS_LJ_COMP:
+            for t in range(2):
+                grids[t][sl] += np.where(inside, lj_field(c, rr, t), 0.0)
+        else:
+            grids[0][sl] += np.where(inside, lj_field(c, rr, "avg"), 0.0)
+    return grids
+
+
+def lj_ligand_weights(lj: LjParams, term_set):
+    """(n_atoms, K) ligand weights: ljComp sqrt(eps) sigma^6 and sqrt(eps)
+    sigma^3 (docking_molforce.hpp:503-510,569-576); ljAvg 1 (:441-445)."""
+    sig = np.asarray(lj.lig_sigma, dtype=np.float64)
+    eps = np.asarray(lj.lig_eps, dtype=np.float64)
+    if term_set == TERMS_LJ_AVG:
+        return np.ones((len(sig), 1))
+    w = np.zeros((len(sig), 2))
+    for i, (s, e) in enumerate(zip(sig, eps)):
+        w[i, 0] = math.sqrt(e) * _pow6(s)
+        w[i, 1] = math.sqrt(e) * _pow3(s)
+    return w
 
 
 # ----------------------------------------------------------------------------

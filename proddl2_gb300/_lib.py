@@ -27,6 +27,8 @@ STATUS_NAMES = {
 
 FFTDOCK_TERMS_SHAPE = 1
 FFTDOCK_TERMS_SHAPE_ACE = 2
+FFTDOCK_TERMS_LJ_COMP = 3
+FFTDOCK_TERMS_LJ_AVG = 4
 FFTDOCK_PREC_FP32 = 0
 FFTDOCK_PREC_BF16_SPECTRA = 1
 FFTDOCK_PENCIL_AUTO = 0
@@ -62,6 +64,8 @@ class Config(C.Structure):
         ("cluster_trans", C.c_int32),
         ("cluster_order", C.c_int32),
         ("cluster_radius", C.c_double),
+        ("lj_mix", C.c_int32),
+        ("lj_cut", C.c_double),
     ]
 
 
@@ -166,6 +170,7 @@ SIGNATURES = {
     "fftdock_create": (C.c_int, [C.POINTER(Config), C.POINTER(_P)]),
     "fftdock_destroy": (None, [_P]),
     "fftdock_last_error": (C.c_char_p, [_P]),
+    "fftdock_set_pair_lj": (C.c_int, [_P, C.c_int32, _P, _P, _P, _P, C.c_int32, _P, _P, _P]),
     "fftdock_set_receptor": (C.c_int, [_P, C.c_int32, _P, _P]),
     "fftdock_set_ligand": (C.c_int, [_P, C.c_int32, _P, _P]),
     "fftdock_scan": (C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, _P]),

@@ -12,6 +12,9 @@ template <int N> struct SizeOpsImpl {
     static constexpr int G = SizeTraits<N>::G;
     static constexpr int H = N / 2 + 1;
 
+    static size_t pencil_smem_w(int K, int n_ent, bool weighted) {
+        return pencil_smem(K, n_ent) + (weighted ? (size_t)n_ent * sizeof(float) : 0);
+    }
     static size_t pencil_smem(int K, int n_ent) {
         return (size_t)PencilTraits<N>::BUFS * N * 32 * sizeof(float2) + N * sizeof(float2) +
                ((size_t)K * N + 1) * sizeof(int32_t) +
@@ -86,13 +89,13 @@ template <int N> struct SizeOpsImpl {
         return cudaGetLastError();
     }
 
-    template <typename SpecT> static cudaError_t launch_pencil(const BatchArgs& a, int nb, cudaStream_t s) {
-        const size_t sm2 = pencil_smem(a.K, a.n_ent);
-        cudaError_t e = set_smem((const void*)pencil_kernel<N, SpecT>, sm2);
+    template <typename SpecT, bool W> static cudaError_t launch_pencil(const BatchArgs& a, int nb, cudaStream_t s) {
+        const size_t sm2 = pencil_smem_w(a.K, a.n_ent, W);
+        cudaError_t e = set_smem((const void*)pencil_kernel<N, SpecT, W>, sm2);
         if (e != cudaSuccess) return e;
         dim3 grid2(nb, a.PP / 32);
-        pencil_kernel<N, SpecT><<<grid2, 32 * G, sm2, s>>>(static_cast<const SpecT*>(a.spec), a.ent, a.offs,
-                                                           a.tw32, a.g2, a.K, a.n_ent);
+        pencil_kernel<N, SpecT, W><<<grid2, 32 * G, sm2, s>>>(static_cast<const SpecT*>(a.spec), a.ent, a.offs,
+                                                              a.tw32, a.g2, a.K, a.n_ent, a.ent_w);
         return cudaGetLastError();
     }
 
@@ -114,7 +117,7 @@ template <int N> struct SizeOpsImpl {
         const size_t sm1 = ((size_t)a.K * N + 1) * sizeof(int32_t) + (size_t)a.n_ent * sizeof(uint32_t);
         if ((e = set_smem((const void*)ligand_prep_kernel<N>, sm1)) != cudaSuccess) return e;
         ligand_prep_kernel<N><<<nb, 256, sm1, s>>>(a.rot, a.lig_xyz, a.lig_term, a.n_ent, a.K, geo, a.ent, a.offs,
-                                                    a.status);
+                                                    a.status, a.lig_w32, a.lig_w32 ? a.ent_w : nullptr, a.ent_idx);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if (a.ev && (e = cudaEventRecord(a.ev[1], s)) != cudaSuccess) return e;
         // K2
@@ -131,7 +134,12 @@ template <int N> struct SizeOpsImpl {
             }
         }
         if (!pmajor) {
-            e = a.spec_bf16 ? launch_pencil<__nv_bfloat162>(a, nb, s) : launch_pencil<float2>(a, nb, s);
+            if (a.lig_w32) {
+                if (a.spec_bf16) return cudaErrorNotSupported;  // weighted sets run with FP32 spectra
+                e = launch_pencil<float2, true>(a, nb, s);
+            } else {
+                e = a.spec_bf16 ? launch_pencil<__nv_bfloat162, false>(a, nb, s) : launch_pencil<float2, false>(a, nb, s);
+            }
             if (e != cudaSuccess) return e;
         }
         if (a.ev && (e = cudaEventRecord(a.ev[2], s)) != cudaSuccess) return e;
@@ -157,7 +165,8 @@ template <int N> struct SizeOpsImpl {
         } else {
             finalize_kernel<N><<<nb, 256, 0, s>>>(a.cand_v, a.cand_i, a.ent, a.status, a.rgrid, a.n_ent,
                                                   a.peak_stride, a.k_out, a.max_val, a.h, a.first_rot_id, a.peaks,
-                                                  a.n_peaks, a.pool_v, a.pool_i);
+                                                  a.n_peaks, a.pool_v, a.pool_i, a.lig_w64,
+                                                  a.lig_w64 ? a.ent_idx : nullptr);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
         }
         if (a.ev && (e = cudaEventRecord(a.ev[4], s)) != cudaSuccess) return e;

@@ -58,6 +58,12 @@ struct fftdock_ctx {
     int n_ent = 0;
     double* lig_xyz = nullptr;
     int32_t* lig_term = nullptr;
+    // weighted entries (the LJ term sets)
+    bool lj = false;
+    float* lig_w32 = nullptr;
+    double* lig_w64 = nullptr;
+    float* ent_w = nullptr;
+    int32_t* ent_idx = nullptr;
 
     // per-batch work
     uint32_t* ent = nullptr;
@@ -153,6 +159,10 @@ BatchArgs batch_args(fftdock_ctx* ctx) {
     BatchArgs a{};
     a.lig_xyz = ctx->lig_xyz;
     a.lig_term = ctx->lig_term;
+    a.lig_w32 = ctx->lig_w32;
+    a.lig_w64 = ctx->lig_w64;
+    a.ent_w = ctx->ent_w;
+    a.ent_idx = ctx->ent_idx;
     a.spec = ctx->spec;
     a.spec_bf16 = ctx->cfg.precision == FFTDOCK_PREC_BF16_SPECTRA ? 1 : 0;
     a.rgrid = ctx->rgrid;
@@ -284,6 +294,8 @@ void fftdock_config_init(fftdock_config* cfg) {
     cfg->cluster_trans = 0;
     cfg->cluster_order = FFTDOCK_CLUSTER_ORDER_REFERENCE;
     cfg->cluster_radius = 5.0;
+    cfg->lj_mix = 1;
+    cfg->lj_cut = 9.0;
 }
 
 int fftdock_supported_grid(int32_t n) { return fftdock::size_ops(n) != nullptr ? 1 : 0; }
@@ -330,6 +342,10 @@ void fftdock_destroy(fftdock_ctx* ctx) {
     dfree(ctx->emat);
     dfree(ctx->lig_xyz);
     dfree(ctx->lig_term);
+    dfree(ctx->lig_w32);
+    dfree(ctx->lig_w64);
+    dfree(ctx->ent_w);
+    dfree(ctx->ent_idx);
     dfree(ctx->ent);
     dfree(ctx->offs);
     dfree(ctx->g2);
@@ -403,6 +419,17 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
         for (double v : ctx->ace)
             if (!std::isfinite(v)) return fail(ctx, FFTDOCK_EINVAL, "ace_matrix has a non-finite entry");
         ctx->K = c.n_types;
+    } else if (c.term_set == FFTDOCK_TERMS_LJ_COMP || c.term_set == FFTDOCK_TERMS_LJ_AVG) {
+        if (c.lj_mix != 0 && c.lj_mix != 1) return fail(ctx, FFTDOCK_EINVAL, "lj_mix must be 0 or 1");
+        if (c.term_set == FFTDOCK_TERMS_LJ_COMP && c.lj_mix != 1)
+            return fail(ctx, FFTDOCK_EINVAL, "ljComp requires the geometric sigma rule (lj_mix 1)");
+        if (!(c.lj_cut > 0.0) || !std::isfinite(c.lj_cut)) return fail(ctx, FFTDOCK_EINVAL, "lj_cut must be > 0");
+        if (c.pencil_mode == FFTDOCK_PENCIL_TENSOR)
+            return fail(ctx, FFTDOCK_EUNSUPPORTED, "the LJ term sets run with the FFT pencil stage");
+        if (c.precision != FFTDOCK_PREC_FP32)
+            return fail(ctx, FFTDOCK_EUNSUPPORTED, "the LJ term sets keep FP32 receptor spectra");
+        ctx->K = c.term_set == FFTDOCK_TERMS_LJ_COMP ? 2 : 1;
+        ctx->lj = true;
     } else {
         return fail(ctx, FFTDOCK_EINVAL, "unknown term_set");
     }
@@ -485,6 +512,7 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
 int fftdock_set_receptor(fftdock_ctx* ctx, int32_t n, const double* xyz, const int32_t* type) {
     if (!ctx) return FFTDOCK_EINVAL;
     if (!ctx->ops) return fail(ctx, FFTDOCK_ESTATE, "context was not created successfully");
+    if (ctx->lj) return fail(ctx, FFTDOCK_EINVAL, "the LJ term sets take their atoms through fftdock_set_pair_lj");
     if (n < 0 || (n > 0 && !xyz)) return fail(ctx, FFTDOCK_EINVAL, "bad receptor atom arrays");
     if (!finite3(xyz, n)) return fail(ctx, FFTDOCK_EINVAL, "receptor coordinates must be finite");
     const fftdock_config& c = ctx->cfg;
@@ -598,6 +626,7 @@ int fftdock_set_receptor(fftdock_ctx* ctx, int32_t n, const double* xyz, const i
 int fftdock_set_ligand(fftdock_ctx* ctx, int32_t n, const double* xyz, const int32_t* type) {
     if (!ctx) return FFTDOCK_EINVAL;
     if (!ctx->ops) return fail(ctx, FFTDOCK_ESTATE, "context was not created successfully");
+    if (ctx->lj) return fail(ctx, FFTDOCK_EINVAL, "the LJ term sets take their atoms through fftdock_set_pair_lj");
     if (n < 1 || !xyz) return fail(ctx, FFTDOCK_EINVAL, "the ligand needs at least one atom");
     if (n > fftdock::kMaxEntries) return fail(ctx, FFTDOCK_EINVAL, "ligand has more than 32768 atoms");
     if (!finite3(xyz, n)) return fail(ctx, FFTDOCK_EINVAL, "ligand coordinates must be finite");
@@ -644,6 +673,210 @@ int fftdock_set_ligand(fftdock_ctx* ctx, int32_t n, const double* xyz, const int
     ctx->W = W;
     ctx->n_ent = n;
     ctx->have_lig = true;
+    return FFTDOCK_OK;
+}
+
+// per receptor atom (as6, 4es6, 4es12, fshift, gshift) of its LJ field, in
+// the reference's operation order (SoftCoreLJRep/SoftCoreLJAttr for ljComp,
+// potentials_inc.hpp:247-354; SoftCoreLJ with CUT_POLICY_SHIFT_FORCE for
+// ljAvg, :142-245; parameters as MolForceLJComp / MolForceLJ combine them,
+// docking_molforce.hpp:375-600)
+static double lj_pow3(double x) { return (x * x) * x; }
+static double lj_pow6(double x) {
+    const double t = (x * x) * x;
+    return t * t;
+}
+static double lj_mean(const double* v, int n) {
+    double t = 0.0;
+    for (int i = 0; i < n; ++i) t = t + v[i];
+    return t / (double)n;
+}
+
+int fftdock_set_pair_lj(fftdock_ctx* ctx, int32_t n_rec, const double* rec_xyz, const double* rec_sigma,
+                                   const double* rec_eps, const double* rec_alpha, int32_t n_lig,
+                                   const double* lig_xyz, const double* lig_sigma, const double* lig_eps) {
+    if (!ctx) return FFTDOCK_EINVAL;
+    if (!ctx->ops) return fail(ctx, FFTDOCK_ESTATE, "context was not created successfully");
+    if (!ctx->lj) return fail(ctx, FFTDOCK_EINVAL, "fftdock_set_pair_lj needs an LJ term set");
+    if (n_rec < 0 || (n_rec > 0 && (!rec_xyz || !rec_sigma || !rec_eps || !rec_alpha)))
+        return fail(ctx, FFTDOCK_EINVAL, "bad receptor arrays");
+    if (n_lig < 1 || !lig_xyz || !lig_sigma || !lig_eps) return fail(ctx, FFTDOCK_EINVAL, "bad ligand arrays");
+    if (!finite3(rec_xyz, n_rec) || !finite3(lig_xyz, n_lig))
+        return fail(ctx, FFTDOCK_EINVAL, "coordinates must be finite");
+    for (int i = 0; i < n_rec; ++i)
+        if (!(rec_sigma[i] > 0.0) || !(rec_eps[i] >= 0.0) || !(rec_alpha[i] >= 0.0) || !std::isfinite(rec_sigma[i]) ||
+            !std::isfinite(rec_eps[i]) || !std::isfinite(rec_alpha[i]))
+            return fail(ctx, FFTDOCK_EINVAL, "receptor sigma must be > 0, eps and alpha >= 0, all finite");
+    for (int i = 0; i < n_lig; ++i)
+        if (!(lig_sigma[i] > 0.0) || !(lig_eps[i] >= 0.0) || !std::isfinite(lig_sigma[i]) || !std::isfinite(lig_eps[i]))
+            return fail(ctx, FFTDOCK_EINVAL, "ligand sigma must be > 0, eps >= 0, all finite");
+    const fftdock_config& c = ctx->cfg;
+    const bool comp = c.term_set == FFTDOCK_TERMS_LJ_COMP;
+    const int n_ent = comp ? 2 * n_lig : n_lig;
+    if (n_ent > fftdock::kMaxEntries) return fail(ctx, FFTDOCK_EINVAL, "too many ligand entries (2 per atom for ljComp)");
+    if (ctx->ops->pencil_smem(ctx->K, n_ent) + (comp ? (size_t)n_ent * sizeof(float) : 0) > fftdock::kMaxSmem)
+        return fail(ctx, FFTDOCK_EINVAL, "ligand too large for the pencil kernel's shared memory");
+
+    // receptor field constants
+    const double sig_l = lj_mean(lig_sigma, n_lig);
+    const double eps_l = lj_mean(lig_eps, n_lig);
+    const double cut = c.lj_cut, cut2 = cut * cut;
+    std::vector<double> lc((size_t)5 * n_rec);
+    for (int i = 0; i < n_rec; ++i) {
+        double* p = &lc[(size_t)5 * i];
+        if (comp) {
+            const double sigma = std::sqrt(rec_sigma[i]);
+            const double sigma_alpha = std::sqrt(rec_sigma[i] * sig_l);
+            const double eps = std::sqrt(rec_eps[i]);
+            const double s6 = lj_pow6(sigma);
+            p[0] = rec_alpha[i] * lj_pow6(sigma_alpha);
+            p[1] = 4. * eps * s6;
+            p[2] = p[1] * s6;
+            p[3] = 0.0;
+            p[4] = 0.0;
+        } else {
+            const double sigma = c.lj_mix == 0 ? (rec_sigma[i] + sig_l) / 2. : std::sqrt(rec_sigma[i] * sig_l);
+            const double eps = std::sqrt(rec_eps[i] * eps_l);
+            const double s6 = lj_pow6(sigma);
+            const double as6 = rec_alpha[i] * s6;
+            const double e6 = 4. * eps * s6;
+            const double e12 = e6 * s6;
+            const double r6 = lj_pow3(cut2);
+            const double A = r6 + as6;
+            const double B = s6 / (r6 + as6) - 1.;
+            const double C = -6. * (cut2 * cut2) * (e6 * A * B + e12) / lj_pow3(A);
+            const double gcut = cut * C + cut * (0.0 / std::sqrt(cut2));
+            double fshift = -((e12 / A - e6) / A + 0.0 + 0.0 * std::sqrt(cut2));
+            const double gshift = -gcut;
+            fshift = fshift - gshift * cut;
+            p[0] = as6;
+            p[1] = e6;
+            p[2] = e12;
+            p[3] = fshift;
+            p[4] = gshift;
+        }
+    }
+    CK(cudaSetDevice(c.device));
+    ctx->have_rec = ctx->have_lig = false;
+    CK(cudaStreamSynchronize(ctx->stream));
+    const int N = ctx->N;
+    const size_t V = ctx->V;
+    cudaStream_t s = ctx->stream;
+    double* d_xyz = nullptr;
+    double* d_lc = nullptr;
+    int* bin_start = nullptr;
+    int* bin_atoms = nullptr;
+    int* box = nullptr;
+    double2* cbuf = nullptr;
+    double2* hbuf = nullptr;
+    int rc = FFTDOCK_OK;
+    auto cleanup = [&]() {
+        cudaStreamSynchronize(s);
+        dfree(d_xyz);
+        dfree(d_lc);
+        dfree(bin_start);
+        dfree(bin_atoms);
+        dfree(box);
+        dfree(cbuf);
+        dfree(hbuf);
+    };
+#define CKR(expr)                                 \
+    do {                                          \
+        cudaError_t e_ = (expr);                  \
+        if (e_ != cudaSuccess) {                  \
+            rc = cuda_fail(ctx, e_, #expr);       \
+            cleanup();                            \
+            return rc;                            \
+        }                                         \
+    } while (0)
+    fftdock::HostAtomBins hb;
+    fftdock::bin_atoms(rec_xyz, n_rec, cut, hb);
+    CKR(dalloc(&d_xyz, (size_t)n_rec * 3));
+    CKR(dalloc(&d_lc, lc.size()));
+    CKR(dalloc(&bin_start, hb.start.size()));
+    CKR(dalloc(&bin_atoms, hb.atoms.size()));
+    CKR(dalloc(&box, (size_t)6 * n_rec));
+    CKR(cudaMemcpyAsync(bin_start, hb.start.data(), hb.start.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    if (n_rec > 0) {
+        CKR(cudaMemcpyAsync(d_xyz, rec_xyz, (size_t)n_rec * 3 * sizeof(double), cudaMemcpyHostToDevice, s));
+        CKR(cudaMemcpyAsync(d_lc, lc.data(), lc.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+        CKR(cudaMemcpyAsync(bin_atoms, hb.atoms.data(), hb.atoms.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    }
+    {
+        fftdock::ReceptorGridArgs ra{};
+        ra.xyz = d_xyz;
+        ra.n = n_rec;
+        ra.geo = fftdock::Geo{ctx->h, ctx->zero_h, ctx->center0, N};
+        ra.term_set = c.term_set;
+        ra.K = ctx->K;
+        for (int d = 0; d < 3; ++d) {
+            ra.bins.lo[d] = hb.lo[d];
+            ra.bins.nb[d] = hb.nb[d];
+        }
+        ra.bins.size = hb.size;
+        ra.bins.start = bin_start;
+        ra.bins.atoms = bin_atoms;
+        ra.box = box;
+        ra.lj_c = d_lc;
+        ra.lj_cut = cut;
+        ra.rgrid = ctx->rgrid;
+        CKR(fftdock::build_receptor_grids(ra, s));
+    }
+    CKR(dalloc(&cbuf, V));
+    CKR(dalloc(&hbuf, (size_t)N * N * ctx->H));
+    for (int t = 0; t < ctx->K; ++t)
+        CKR(ctx->ops->receptor_fft(ctx->rgrid + (size_t)t * V, cbuf, hbuf, ctx->tw64,
+                                   static_cast<unsigned char*>(ctx->spec) + (size_t)t * N * ctx->PP * 8, 0, ctx->PP,
+                                   nullptr, s));
+    CKR(cudaStreamSynchronize(s));
+    cleanup();
+#undef CKR
+
+    // ligand entries: one per (atom, term); ljComp weighs each atom into both
+    // terms, ljAvg has unit weights (the unweighted path)
+    std::vector<double> exyz((size_t)3 * n_ent), w64;
+    std::vector<float> w32;
+    std::vector<int32_t> term(n_ent, 0);
+    for (int k = 0; k < (comp ? 2 : 1); ++k)
+        for (int i = 0; i < n_lig; ++i) {
+            const int e = k * n_lig + i;
+            std::memcpy(&exyz[(size_t)3 * e], lig_xyz + (size_t)3 * i, 3 * sizeof(double));
+            term[e] = k;
+        }
+    if (comp) {
+        w64.resize(n_ent);
+        w32.resize(n_ent);
+        for (int i = 0; i < n_lig; ++i) {
+            const double se = std::sqrt(lig_eps[i]);
+            w64[i] = se * lj_pow6(lig_sigma[i]);
+            w64[n_lig + i] = se * lj_pow3(lig_sigma[i]);
+        }
+        for (int e = 0; e < n_ent; ++e) w32[e] = (float)w64[e];
+    }
+    dfree(ctx->lig_xyz);
+    dfree(ctx->lig_term);
+    dfree(ctx->lig_w32);
+    dfree(ctx->lig_w64);
+    dfree(ctx->ent);
+    dfree(ctx->ent_w);
+    dfree(ctx->ent_idx);
+    CK(dalloc(&ctx->lig_xyz, exyz.size()));
+    CK(dalloc(&ctx->lig_term, (size_t)n_ent));
+    CK(dalloc(&ctx->ent, (size_t)ctx->B * n_ent));
+    CK(cudaMemcpy(ctx->lig_xyz, exyz.data(), exyz.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->lig_term, term.data(), (size_t)n_ent * sizeof(int32_t), cudaMemcpyHostToDevice));
+    if (comp) {
+        CK(dalloc(&ctx->lig_w32, (size_t)n_ent));
+        CK(dalloc(&ctx->lig_w64, (size_t)n_ent));
+        CK(dalloc(&ctx->ent_w, (size_t)ctx->B * n_ent));
+        CK(dalloc(&ctx->ent_idx, (size_t)ctx->B * n_ent));
+        CK(cudaMemcpy(ctx->lig_w32, w32.data(), (size_t)n_ent * sizeof(float), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(ctx->lig_w64, w64.data(), (size_t)n_ent * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    ctx->n_ent = n_ent;
+    ctx->x0 = 0;
+    ctx->W = N;
+    ctx->have_rec = ctx->have_lig = true;
     return FFTDOCK_OK;
 }
 

@@ -45,8 +45,10 @@ struct ReceptorGridArgs {
     const double* xyz;     // [n][3]
     const int32_t* type;   // [n]
     int n;
-    AtomBins bins;         // shape+ACE: cell list of the atoms (device arrays)
-    int* box;              // shape+ACE: [n][6] work (each atom's projection box)
+    AtomBins bins;         // shape+ACE and LJ: cell list of the atoms (device arrays)
+    int* box;              // shape+ACE and LJ: [n][6] work (each atom's projection box)
+    const double* lj_c;    // LJ: [n][5] per-atom field constants (as6, 4es6, 4es12, fshift, gshift)
+    double lj_cut;         // LJ: field cutoff
     Geo geo;
     int term_set;
     int n_types;
@@ -101,6 +103,8 @@ struct BatchArgs {
     const double* rot;          // [B][9]
     const double* lig_xyz;      // [n_ent][3]
     const int32_t* lig_term;    // [n_ent]
+    const float* lig_w32;       // optional [n_ent] entry weights (weighted term sets), FP32 for the sums
+    const double* lig_w64;      // optional [n_ent] the same weights in FP64 for the rescoring
     const void* spec;           // [K][N][PP] float2, or __nv_bfloat162 when spec_bf16
     int spec_bf16;
     const double* rgrid;        // [K][N^3]
@@ -112,6 +116,8 @@ struct BatchArgs {
     double h, zero_h, center0;
     // work
     uint32_t* ent;              // [B][n_ent]
+    float* ent_w;               // weighted: [B][n_ent] weights in sorted order
+    int32_t* ent_idx;           // weighted: [B][n_ent] entry index in sorted order
     int32_t* offs;              // [B][K*N+1]
     int32_t* status;            // [B]
     float2* g2;                 // [B][N][PP]

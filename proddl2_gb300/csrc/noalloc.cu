@@ -62,6 +62,9 @@ extern "C" int fftdock_scan_device_noalloc(fftdock_ctx* ctx, int32_t n_rot, cons
     if (n_rot < 0 || (n_rot > 0 && (!d_rot || !d_peaks || !d_n_peaks)))
         return fftdock::ctx_fail(ctx, FFTDOCK_EINVAL, "bad arguments");
     if (n_rot == 0) return FFTDOCK_OK;
+    if (in.args.lig_w32)
+        return fftdock::ctx_fail(ctx, FFTDOCK_EUNSUPPORTED,
+                                 "weighted ligand entries (ljComp) are not covered by the no-allocation scan");
     if (in.args.wide.corr)
         return fftdock::ctx_fail(ctx, FFTDOCK_EUNSUPPORTED,
                                  "translational clustering needs a full correlation grid per rotation; the "

@@ -570,6 +570,8 @@ int fftdock_scan_pairs(const fftdock_config* cfg, int32_t n_pairs, const fftdock
     if (!(c.grid_step > 0.0) || std::isnan(c.max_val_corr)) return fail(FFTDOCK_EINVAL, "bad grid_step or max_val_corr");
     if (c.precision != FFTDOCK_PREC_FP32 && c.precision != FFTDOCK_PREC_BF16_SPECTRA)
         return fail(FFTDOCK_EUNSUPPORTED, "precision mode not built");
+    if (c.term_set == FFTDOCK_TERMS_LJ_COMP || c.term_set == FFTDOCK_TERMS_LJ_AVG)
+        return fail(FFTDOCK_EUNSUPPORTED, "the LJ term sets are not part of the pair batch");
     if (c.term_set == FFTDOCK_TERMS_SHAPE) {
         r.K = 1;
     } else if (c.term_set == FFTDOCK_TERMS_SHAPE_ACE) {

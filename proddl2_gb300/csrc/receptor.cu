@@ -110,6 +110,57 @@ __global__ void ace_density_kernel(const double* __restrict__ xyz, const int32_t
             }
 }
 
+// The reference's LJ fields (SoftCoreLJRep / SoftCoreLJAttr for ljComp,
+// SoftCoreLJ with the force-shifted cutoff for ljAvg; potentials_inc.hpp:
+// 142-354), projected like ProjectorRadialField::projectFields
+// (project.hpp:143-176): each cell gathers, in a fixed bin and atom order,
+// f2(max(r^2, minDist^2)) of every atom whose cropped box holds it and with
+// r^2 <= cut^2.  K = 2 (ljComp: repulsion, attraction) or 1 (ljAvg).
+template <int K>
+__global__ void lj_field_kernel(const double* __restrict__ xyz, const double* __restrict__ lc,
+                                const int* __restrict__ box, AtomBins bins, Geo g, double cut2, double mind2,
+                                double* __restrict__ rgrid) {
+    const size_t V = (size_t)g.n * g.n * g.n;
+    const size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= V) return;
+    const int ix = (int)(cell / ((size_t)g.n * g.n)), iy = (int)((cell / g.n) % g.n), iz = (int)(cell % g.n);
+    const int ic[3] = {ix, iy, iz};
+    int b0[3];
+    for (int d = 0; d < 3; ++d) {
+        const double t = floor((cell_centre(ic[d], g) - bins.lo[d]) / bins.size);
+        b0[d] = t < -2.0 ? -2 : (t > (double)bins.nb[d] + 1.0 ? bins.nb[d] + 1 : (int)t);
+    }
+    double acc0 = 0.0, acc1 = 0.0;
+    for (int bx = max(b0[0] - 1, 0); bx <= min(b0[0] + 1, bins.nb[0] - 1); ++bx)
+        for (int by = max(b0[1] - 1, 0); by <= min(b0[1] + 1, bins.nb[1] - 1); ++by)
+            for (int bz = max(b0[2] - 1, 0); bz <= min(b0[2] + 1, bins.nb[2] - 1); ++bz) {
+                const int bin = (bx * bins.nb[1] + by) * bins.nb[2] + bz;
+                for (int k = bins.start[bin]; k < bins.start[bin + 1]; ++k) {
+                    const int a = bins.atoms[k];
+                    const int* bb = box + 6 * a;
+                    if (ix < bb[0] || ix > bb[3] || iy < bb[1] || iy > bb[4] || iz < bb[2] || iz > bb[5]) continue;
+                    const double c[3] = {xyz[3 * a], xyz[3 * a + 1], xyz[3 * a + 2]};
+                    double r2 = dist2(c, ix, iy, iz, g);
+                    if (r2 <= cut2) {
+                        if (r2 < mind2) r2 = mind2;
+                        const double* p = lc + 5 * a;  // as6, 4es6, 4es12, fshift, gshift
+                        const double A = __dadd_rn(__dmul_rn(__dmul_rn(r2, r2), r2), p[0]);
+                        if constexpr (K == 2) {
+                            acc0 = __dadd_rn(acc0, __ddiv_rn(__ddiv_rn(p[2], A), A));
+                            acc1 = __dadd_rn(acc1, __ddiv_rn(-p[1], A));
+                        } else {
+                            const double f = __dadd_rn(
+                                __dadd_rn(__ddiv_rn(__dsub_rn(__ddiv_rn(p[2], A), p[1]), A), p[3]),
+                                __dmul_rn(p[4], sqrt(r2)));
+                            acc0 = __dadd_rn(acc0, f);
+                        }
+                    }
+                }
+            }
+    rgrid[cell] = acc0;
+    if constexpr (K == 2) rgrid[V + cell] = acc1;
+}
+
 // R_t = sum_u E[u][t] G_u - S (shape+ACE, folded) or R_0 = -S (shape)
 __global__ void mix_terms_kernel(const int* __restrict__ flags, const double* __restrict__ dens,
                                  const double* __restrict__ emat, int n_types, int K, int term_set, size_t V,
@@ -133,6 +184,22 @@ __global__ void mix_terms_kernel(const int* __restrict__ flags, const double* __
 
 cudaError_t build_receptor_grids(const ReceptorGridArgs& a, cudaStream_t s) {
     const size_t V = (size_t)a.geo.n * a.geo.n * a.geo.n;
+    if (a.term_set == FFTDOCK_TERMS_LJ_COMP || a.term_set == FFTDOCK_TERMS_LJ_AVG) {
+        const double md = a.geo.h / 4.0;
+        cudaError_t e = cudaSuccess;
+        if (a.n > 0) {
+            atom_box_kernel<<<(a.n + 127) / 128, 128, 0, s>>>(a.xyz, a.n, a.geo, a.lj_cut, a.box);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
+        const unsigned blocks = (unsigned)((V + 255) / 256);
+        if (a.term_set == FFTDOCK_TERMS_LJ_COMP)
+            lj_field_kernel<2><<<blocks, 256, 0, s>>>(a.xyz, a.lj_c, a.box, a.bins, a.geo, a.lj_cut * a.lj_cut,
+                                                       md * md, a.rgrid);
+        else
+            lj_field_kernel<1><<<blocks, 256, 0, s>>>(a.xyz, a.lj_c, a.box, a.bins, a.geo, a.lj_cut * a.lj_cut,
+                                                       md * md, a.rgrid);
+        return cudaGetLastError();
+    }
     cudaError_t e = cudaMemsetAsync(a.flags, 0, V * sizeof(int), s);
     if (e != cudaSuccess) return e;
     if (a.n > 0) {

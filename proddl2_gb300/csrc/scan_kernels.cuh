@@ -122,7 +122,8 @@ template <int N>
 __global__ void __launch_bounds__(256) ligand_prep_kernel(
     const double* __restrict__ rot, const double* __restrict__ lig_xyz, const int32_t* __restrict__ lig_term,
     int n_ent, int K, Geo geo, uint32_t* __restrict__ ent_out, int32_t* __restrict__ offs_out,
-    int32_t* __restrict__ status) {
+    int32_t* __restrict__ status, const float* __restrict__ w_in, float* __restrict__ w_out,
+    int32_t* __restrict__ idx_out) {
     extern __shared__ unsigned char smem_raw[];
     int32_t* cnt = reinterpret_cast<int32_t*>(smem_raw);          // [K*N + 1]
     uint32_t* keys = reinterpret_cast<uint32_t*>(cnt + K * N + 1);  // [n_ent]
@@ -198,6 +199,10 @@ __global__ void __launch_bounds__(256) ligand_prep_kernel(
             if (act) dst = cnt[bin] + rank;
             __syncwarp();
             if (act) ent[dst] = key;
+            if (act && w_out) {
+                w_out[(size_t)q * n_ent + dst] = w_in[i];
+                idx_out[(size_t)q * n_ent + dst] = i;
+            }
             if (act && tid == leader) cnt[bin] += __popc(peers);
             __syncwarp();
         }
@@ -218,10 +223,10 @@ __global__ void __launch_bounds__(256) ligand_prep_kernel(
 __device__ __forceinline__ float2 spec_load(const float2* p) { return __ldg(p); }
 __device__ __forceinline__ float2 spec_load(const __nv_bfloat162* p) { return __bfloat1622float2(*p); }
 
-template <int N, typename SpecT>
+template <int N, typename SpecT, bool WEIGHTED = false>
 __global__ void __launch_bounds__(32 * SizeTraits<N>::G, PencilTraits<N>::MINB) pencil_kernel(
     const SpecT* __restrict__ spec, const uint32_t* __restrict__ ent, const int32_t* __restrict__ offs,
-    const float2* __restrict__ tw, float2* __restrict__ g2, int K, int n_ent) {
+    const float2* __restrict__ tw, float2* __restrict__ g2, int K, int n_ent, const float* __restrict__ ent_w) {
     using P = LinePlan<N, SizeTraits<N>::G>;
     constexpr int G = P::G, R1 = P::R1, H = N / 2 + 1;
     constexpr int PP = pencil_pitch(N);
@@ -231,6 +236,7 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G, PencilTraits<N>::MINB) 
     float2* tws = xbuf + BUFS * N * 32;                  // [N]
     int32_t* offs_s = reinterpret_cast<int32_t*>(tws + N);  // [K*N+1]
     uint32_t* ent_s = reinterpret_cast<uint32_t*>(offs_s + K * N + 1);  // [n_ent]
+    float* w_s = reinterpret_cast<float*>(ent_s + n_ent);                 // [n_ent] (weighted)
 
     const int q = blockIdx.x;
     const int tile = blockIdx.y;
@@ -244,6 +250,10 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G, PencilTraits<N>::MINB) 
     for (int i = tid; i <= K * N; i += blockDim.x) offs_s[i] = offs_g[i];
     const uint32_t* ent_g = ent + (size_t)q * n_ent;
     for (int i = tid; i < n_ent; i += blockDim.x) ent_s[i] = ent_g[i];
+    if constexpr (WEIGHTED) {
+        const float* w_g = ent_w + (size_t)q * n_ent;
+        for (int i = tid; i < n_ent; i += blockDim.x) w_s[i] = w_g[i];
+    }
     __syncthreads();
 
     float2 S[R1];
@@ -261,8 +271,14 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G, PencilTraits<N>::MINB) 
                 const uint32_t u = ent_s[j];
                 const unsigned ph = (ky * ((u >> 8) & 255u) + kz * (u & 255u)) % (unsigned)N;
                 const float2 z = tws[ph];
-                acc.x += z.x;
-                acc.y += z.y;
+                if constexpr (WEIGHTED) {
+                    const float wj = w_s[j];
+                    acc.x = fmaf(wj, z.x, acc.x);
+                    acc.y = fmaf(wj, z.y, acc.y);
+                } else {
+                    acc.x += z.x;
+                    acc.y += z.y;
+                }
             }
             v[r] = acc;
         }
@@ -553,7 +569,8 @@ __global__ void __launch_bounds__(256) finalize_kernel(
     const float* __restrict__ cand_v, const int32_t* __restrict__ cand_i, const uint32_t* __restrict__ ent,
     const int32_t* __restrict__ status, const double* __restrict__ rgrid, int n_ent, int peak_stride, int k_out,
     double max_val, double h, int first_rot_id, fftdock_peak* __restrict__ peaks, int32_t* __restrict__ n_peaks,
-    float* __restrict__ pool_v, int32_t* __restrict__ pool_i) {
+    float* __restrict__ pool_v, int32_t* __restrict__ pool_i, const double* __restrict__ w64,
+    const int32_t* __restrict__ ent_idx) {
     __shared__ float lv_s[8 * KC];
     __shared__ int li_s[8 * KC];
     __shared__ double score_s[KC];
@@ -602,7 +619,8 @@ __global__ void __launch_bounds__(256) finalize_kernel(
                 const int gx = ax - sx < 0 ? ax - sx + N : ax - sx;
                 const int gy = ay - sy < 0 ? ay - sy + N : ay - sy;
                 const int gz = az - sz < 0 ? az - sz + N : az - sz;
-                sum = __dadd_rn(sum, rgrid[(size_t)t * V + ((size_t)gx * N + gy) * N + gz]);
+                const double rv = rgrid[(size_t)t * V + ((size_t)gx * N + gy) * N + gz];
+                sum = __dadd_rn(sum, w64 ? __dmul_rn(w64[ent_idx[(size_t)q * n_ent + j]], rv) : rv);
             }
             for (int o = 16; o > 0; o >>= 1) sum = __dadd_rn(sum, __shfl_xor_sync(0xffffffffu, sum, o));
         }

@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(kFinishThreads) wide_finish_kernel(
     const u64* __restrict__ cand, const int32_t* __restrict__ cnt, const uint32_t* __restrict__ ent,
     const int32_t* __restrict__ status, const double* __restrict__ rgrid, int n_ent, int N, int m, int order,
     double rad2, int max_out, int peak_stride, double h, int first_rot_id, fftdock_peak* __restrict__ peaks,
-    int32_t* __restrict__ n_peaks) {
+    int32_t* __restrict__ n_peaks, const double* __restrict__ w64, const int32_t* __restrict__ ent_idx) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     u64* keys = reinterpret_cast<u64*>(smem_raw);  // [kWideMax]
     __shared__ int lead_pos[kMaxLeaders];
@@ -387,7 +387,8 @@ __global__ void __launch_bounds__(kFinishThreads) wide_finish_kernel(
             const int gx = ax - sx < 0 ? ax - sx + N : ax - sx;
             const int gy = ay - sy < 0 ? ay - sy + N : ay - sy;
             const int gz = az - sz < 0 ? az - sz + N : az - sz;
-            sum = __dadd_rn(sum, rgrid[(size_t)t * V + ((size_t)gx * N + gy) * N + gz]);
+            const double rv = rgrid[(size_t)t * V + ((size_t)gx * N + gy) * N + gz];
+            sum = __dadd_rn(sum, w64 ? __dmul_rn(w64[ent_idx[(size_t)q * n_ent + j]], rv) : rv);
         }
         for (int o = 16; o > 0; o >>= 1) sum = __dadd_rn(sum, __shfl_xor_sync(0xffffffffu, sum, o));
         if (l == 0) score_s[w] = sum;
@@ -442,7 +443,7 @@ cudaError_t wide_select_batch(const BatchArgs& a, int N, cudaStream_t s) {
     const int max_out = a.k_out < kMaxLeaders ? a.k_out : kMaxLeaders;
     wide_finish_kernel<<<nb, kFinishThreads, sm, s>>>(w.cand, w.cnt, a.ent, a.status, a.rgrid, a.n_ent, N, w.m,
                                                       w.order, w.rad2, max_out, a.peak_stride, a.h, a.first_rot_id,
-                                                      a.peaks, a.n_peaks);
+                                                      a.peaks, a.n_peaks, a.lig_w64, a.lig_w64 ? a.ent_idx : nullptr);
     return cudaGetLastError();
 }
 

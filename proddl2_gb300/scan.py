@@ -18,7 +18,10 @@ import numpy as np
 from . import _lib
 from ._lib import FFTDockError
 
-TERM_SETS = {"shape": _lib.FFTDOCK_TERMS_SHAPE, "shape_ace": _lib.FFTDOCK_TERMS_SHAPE_ACE}
+TERM_SETS = {"shape": _lib.FFTDOCK_TERMS_SHAPE, "shape_ace": _lib.FFTDOCK_TERMS_SHAPE_ACE,
+             "lj_comp": _lib.FFTDOCK_TERMS_LJ_COMP, "lj_avg": _lib.FFTDOCK_TERMS_LJ_AVG}
+# the reference's potentialName values
+POTENTIAL_NAMES = {"ljComp": "lj_comp", "ljAvg": "lj_avg"}
 PENCIL_MODES = {"auto": _lib.FFTDOCK_PENCIL_AUTO, "fft": _lib.FFTDOCK_PENCIL_FFT, "tensor": _lib.FFTDOCK_PENCIL_TENSOR}
 
 
@@ -45,6 +48,8 @@ class ScanConfig:
     cluster_trans: bool = False     # doClusterTranslations
     cluster_radius: float = 5.0     # clusterRadiusTrans
     cluster_order: str = "reference"  # leader walk: "reference" (worst value first) or "best_first"
+    lj_mix: int = 1                 # LJ sets: sigma rule (0 arithmetic, 1 geometric; ljComp needs 1)
+    lj_cut: float = 9.0             # LJ sets: cutOffFft
 
     @classmethod
     def from_options(cls, opts: dict, **kw):
@@ -53,6 +58,10 @@ class ScanConfig:
                  "maxValCorr": "max_val_corr", "doClusterTranslations": "cluster_trans",
                  "clusterRadiusTrans": "cluster_radius"}
         args = {names[k]: v for k, v in opts.items() if k in names}
+        if "potentialName" in opts and opts["potentialName"] in POTENTIAL_NAMES:
+            args["term_set"] = POTENTIAL_NAMES[opts["potentialName"]]
+        if "cutOffFft" in opts:
+            args["lj_cut"] = opts["cutOffFft"]
         args.update(kw)
         return cls(**args)
 
@@ -101,6 +110,8 @@ def native_config(config: ScanConfig):
     cfg.cluster_trans = 1 if config.cluster_trans else 0
     cfg.cluster_radius = float(config.cluster_radius)
     cfg.cluster_order = {"reference": 0, "best_first": 1}[config.cluster_order]
+    cfg.lj_mix = int(config.lj_mix)
+    cfg.lj_cut = float(config.lj_cut)
     return cfg, ace
 
 
@@ -166,6 +177,15 @@ class FFTScan:
         xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
         t = None if types is None else np.ascontiguousarray(types, dtype=np.int32)
         self._check(self.lib.fftdock_set_receptor(self._h, xyz.shape[0], _ptr(xyz), _ptr(t)))
+
+    def set_pair_lj(self, rec_xyz, rec_sigma, rec_eps, rec_alpha, lig_xyz, lig_sigma, lig_eps):
+        """Both molecules with their LJ parameters (the LJ term sets)."""
+        r = np.ascontiguousarray(rec_xyz, dtype=np.float64).reshape(-1, 3)
+        l_ = np.ascontiguousarray(lig_xyz, dtype=np.float64).reshape(-1, 3)
+        arr = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+               for a in (rec_sigma, rec_eps, rec_alpha, lig_sigma, lig_eps)]
+        self._check(self.lib.fftdock_set_pair_lj(self._h, len(r), _ptr(r), _ptr(arr[0]), _ptr(arr[1]), _ptr(arr[2]),
+                                                 len(l_), _ptr(l_), _ptr(arr[3]), _ptr(arr[4])))
 
     def set_ligand(self, xyz, types=None):
         xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)

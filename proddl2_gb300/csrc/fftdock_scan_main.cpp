@@ -16,13 +16,17 @@
 // cutOffFft, anglesFile, maxNRigidMatches, doClusterTranslations,
 // clusterRadiusTrans, plus gridN (grid edge; default: the reference's size
 // rule over the padded receptor box), termSet ("shape" or "shape_ace"),
-// rotBatch, clusterOrder ("reference" or "best_first").
+// rotBatch, clusterOrder ("reference" or "best_first"), potentialName
+// ("ljComp" / "ljAvg": the reference's LJ potentials, with cutOffFft and
+// ljMix).
 //
 // The reference reads atoms from an HDF5 molforce file built with IMP; this
 // front end reads a text pair file instead:
 //   receptor <n>          then n lines "x y z type"
 //   ligand <m>            then m lines "x y z type"
 //   ace <T>               then T lines of T numbers (desolvation matrix)
+//   receptor_lj <n>       then n lines "sigma eps alpha" (LJ potentials)
+//   ligand_lj <m>         then m lines "sigma eps"
 //   receptor_frame / ligand_frame  12 numbers each (optional; row-major
 //                         rotation then vector, mapping original to scan frame)
 // Lines starting with '#' are comments.
@@ -100,6 +104,7 @@ double num(const std::map<std::string, std::string>& o, const char* key, double 
 
 struct Pair {
     std::vector<double> rec_xyz, lig_xyz, ace;
+    std::vector<double> rec_lj, lig_lj;  // per atom (sigma, eps, alpha) / (sigma, eps)
     std::vector<int32_t> rec_type, lig_type;
     int n_types = 0;
     bool has_rec_frame = false, has_lig_frame = false;
@@ -131,6 +136,14 @@ Pair read_pair(const std::string& path) {
             if (!(in >> n) || n < 0) die("bad atom count in " + path);
             if (word == "receptor") atoms(n, p.rec_xyz, p.rec_type);
             else atoms(n, p.lig_xyz, p.lig_type);
+        } else if (word == "receptor_lj" || word == "ligand_lj") {
+            int n;
+            if (!(in >> n) || n < 0) die("bad atom count in " + path);
+            const int per = word == "receptor_lj" ? 3 : 2;
+            std::vector<double>& v = word == "receptor_lj" ? p.rec_lj : p.lig_lj;
+            v.resize((size_t)n * per);
+            for (double& x : v)
+                if (!(in >> x)) die("truncated LJ parameters in " + path);
         } else if (word == "ace") {
             if (!(in >> p.n_types) || p.n_types < 1) die("bad ace size in " + path);
             p.ace.resize((size_t)p.n_types * p.n_types);
@@ -209,8 +222,18 @@ int run_rot_scan(std::map<std::string, std::string>& a) {
     const std::string corder = opt.count("clusterOrder") ? opt.at("clusterOrder") : "reference";
     if (corder != "reference" && corder != "best_first") die("clusterOrder must be reference or best_first");
     cfg.cluster_order = corder == "best_first" ? FFTDOCK_CLUSTER_ORDER_BEST_FIRST : FFTDOCK_CLUSTER_ORDER_REFERENCE;
+    // potentialName "ljComp" / "ljAvg" select the reference's own potentials
+    // (docking_app.hpp:52-66); termSet selects this library's shape terms
+    const std::string pot = opt.count("potentialName") ? opt.at("potentialName") : "";
     const std::string terms = opt.count("termSet") ? opt.at("termSet") : (p.n_types ? "shape_ace" : "shape");
     cfg.term_set = terms == "shape" ? FFTDOCK_TERMS_SHAPE : FFTDOCK_TERMS_SHAPE_ACE;
+    if (pot == "ljComp") cfg.term_set = FFTDOCK_TERMS_LJ_COMP;
+    if (pot == "ljAvg") cfg.term_set = FFTDOCK_TERMS_LJ_AVG;
+    const bool lj = cfg.term_set == FFTDOCK_TERMS_LJ_COMP || cfg.term_set == FFTDOCK_TERMS_LJ_AVG;
+    cfg.lj_cut = num(opt, "cutOffFft", 9.0);
+    cfg.lj_mix = (int)num(opt, "ljMix", 1.0);
+    if (lj && (p.rec_lj.size() != 3 * p.rec_type.size() || p.lig_lj.size() != 2 * p.lig_type.size()))
+        die("the LJ potentials need receptor_lj and ligand_lj sections for every atom");
     cfg.n_types = p.n_types ? p.n_types : 18;
     cfg.ace_matrix = p.ace.empty() ? nullptr : p.ace.data();
     int n = (int)num(opt, "gridN", 0);
@@ -247,8 +270,24 @@ int run_rot_scan(std::map<std::string, std::string>& a) {
     fftdock_ctx* ctx = nullptr;
     int rc = fftdock_create(&cfg, &ctx);
     if (rc) die(std::string("create: ") + fftdock_last_error(ctx), 2);
-    rc = fftdock_set_receptor(ctx, (int32_t)p.rec_type.size(), p.rec_xyz.data(), p.rec_type.data());
-    if (!rc) rc = fftdock_set_ligand(ctx, (int32_t)p.lig_type.size(), p.lig_xyz.data(), p.lig_type.data());
+    if (lj) {
+        const size_t nr = p.rec_type.size(), nl = p.lig_type.size();
+        std::vector<double> rs(nr), re(nr), ra(nr), ls(nl), le(nl);
+        for (size_t i = 0; i < nr; ++i) {
+            rs[i] = p.rec_lj[3 * i];
+            re[i] = p.rec_lj[3 * i + 1];
+            ra[i] = p.rec_lj[3 * i + 2];
+        }
+        for (size_t i = 0; i < nl; ++i) {
+            ls[i] = p.lig_lj[2 * i];
+            le[i] = p.lig_lj[2 * i + 1];
+        }
+        rc = fftdock_set_pair_lj(ctx, (int32_t)nr, p.rec_xyz.data(), rs.data(), re.data(), ra.data(), (int32_t)nl,
+                                 p.lig_xyz.data(), ls.data(), le.data());
+    } else {
+        rc = fftdock_set_receptor(ctx, (int32_t)p.rec_type.size(), p.rec_xyz.data(), p.rec_type.data());
+        if (!rc) rc = fftdock_set_ligand(ctx, (int32_t)p.lig_type.size(), p.lig_xyz.data(), p.lig_type.data());
+    }
     const int nr = end - start;
     std::vector<fftdock_peak> peaks((size_t)std::max(nr, 1) * cfg.peaks_per_rot);
     std::vector<int32_t> npk(std::max(nr, 1));

@@ -12,7 +12,10 @@ def _frame_line(name, frame):
     return "%s %s\n" % (name, " ".join("%.17g" % x for x in vals))
 
 
-def write_pair(path, rec_xyz, rec_type, lig_xyz, lig_type, ace=None, rec_frame=None, lig_frame=None):
+def write_pair(path, rec_xyz, rec_type, lig_xyz, lig_type, ace=None, rec_frame=None, lig_frame=None,
+               rec_lj=None, lig_lj=None):
+    """``rec_lj`` (n, 3) sigma, eps, alpha and ``lig_lj`` (m, 2) sigma, eps: the
+    per-atom parameters of the reference's LJ potentials (ljComp, ljAvg)."""
     out = ["# fftdock pair file\n"]
     for name, xyz, typ in (("receptor", rec_xyz, rec_type), ("ligand", lig_xyz, lig_type)):
         xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
@@ -23,6 +26,11 @@ def write_pair(path, rec_xyz, rec_type, lig_xyz, lig_type, ace=None, rec_frame=N
         ace = np.asarray(ace, dtype=np.float64)
         out.append("ace %d\n" % ace.shape[0])
         out.extend(" ".join("%.17g" % x for x in row) + "\n" for row in ace)
+    for name, arr in (("receptor_lj", rec_lj), ("ligand_lj", lig_lj)):
+        if arr is not None:
+            arr = np.asarray(arr, dtype=np.float64)
+            out.append("%s %d\n" % (name, arr.shape[0]))
+            out.extend(" ".join("%.17g" % x for x in row) + "\n" for row in arr)
     if rec_frame is not None:
         out.append(_frame_line("receptor_frame", rec_frame))
     if lig_frame is not None:

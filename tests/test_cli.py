@@ -93,3 +93,34 @@ def test_cli_rot_scan_ranges_match_the_c_abi(tmp_path):
         assert np.array_equal(rot, rots[i])
         _, tt, sc = res.rotation(i)
         assert np.array_equal(t, tt) and np.array_equal(v, sc)
+
+
+@pytest.mark.gpu
+def test_cli_rot_scan_with_the_reference_ljcomp_potential(tmp_path):
+    """potentialName "ljComp" with per-atom sigma/eps/alpha in the pair file
+    gives the records of the C ABI's fftdock_set_pair_lj scan."""
+    from proddl2_gb300 import FFTScan, ScanConfig, synth
+    from proddl2_gb300.pairfile import write_angles, write_pair
+    pair = synth.make_pair(300, 60, 1, seed=77)
+    rng = np.random.default_rng(5)
+    rl = np.stack([rng.uniform(3.0, 3.9, 300), rng.uniform(0.05, 0.6, 300), np.full(300, 0.4)], axis=1)
+    ll = np.stack([rng.uniform(3.0, 3.9, 60), rng.uniform(0.05, 0.6, 60)], axis=1)
+    pf = tmp_path / "pair.txt"
+    write_pair(pf, pair.receptor.xyz, pair.receptor.ace_type, pair.ligand.xyz, pair.ligand.ace_type,
+               rec_lj=rl, lig_lj=ll)
+    ang = rng.uniform(-180, 180, size=(5, 3))
+    write_angles(tmp_path / "ang.dat", ang)
+    opts = _opts(tmp_path, gridN=48, anglesFile=str(tmp_path / "ang.dat"), potentialName="ljComp", cutOffFft=9.0)
+    out = tmp_path / "o.dat"
+    r = subprocess.run([str(CLI), "--task", "rot-scan", "--options", str(opts), "--molforce-params", str(pf),
+                        "--fft-rot-grid-start", "0", "--fft-rot-grid-end", "5", "--fft-rot-scan-res", str(out)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    recs = O.unpack_records(out.read_bytes())
+    rots = np.stack([O.euler_to_matrix(np.asarray(a) * (math.pi / 180.0)) for a in ang])
+    with FFTScan(ScanConfig(grid_n=48, term_set="lj_comp", lj_cut=9.0, peaks_per_rot=4, max_val_corr=1e300)) as s:
+        s.set_pair_lj(pair.receptor.xyz, rl[:, 0], rl[:, 1], rl[:, 2], pair.ligand.xyz, ll[:, 0], ll[:, 1])
+        res = s.scan(rots)
+    for i, (rot, t, v) in enumerate(recs):
+        _, tt, sc = res.rotation(i)
+        assert np.array_equal(t, tt) and np.array_equal(v, sc)

@@ -73,7 +73,9 @@ def workload(name):
 
 
 def workload_desc(w):
-    terms = "shape + 18 desolvation types (18 folded terms)" if w["term_set"] == "shape_ace" else "shape (1 term)"
+    terms = {"shape_ace": "shape + 18 desolvation types (18 folded terms)", "shape": "shape (1 term)",
+             "lj_comp": "the reference's ljComp soft-core LJ (2 terms, weighted ligand entries)",
+             "lj_avg": "the reference's ljAvg soft-core LJ (1 term)"}[w["term_set"]]
     return ("%s: receptor %d / ligand %d atoms, %d^3 at %.1f A, %s, %d rotations, %d per batch, %d peaks/rotation"
             % (w["name"], w["n_rec"], w["n_lig"], w["grid_n"], w["grid_step"], terms, w["n_rot"], w["rot_batch"],
                w["peaks"]))
@@ -178,12 +180,20 @@ class CpuReference:
         self.pair = pair
         self.threads = threads
         self.geom = O.Geometry.centred(w["grid_step"], w["grid_n"])
-        ts = O.TERMS_SHAPE_ACE if w["term_set"] == "shape_ace" else O.TERMS_SHAPE
-        tp = O.TermParams(term_set=ts, ace_matrix=pair.ace)
-        # the reference runs one FFTCorrelator per term: shape + each type
-        self.rg = O.receptor_terms(self.geom, pair.receptor.xyz, pair.receptor.ace_type, tp, folded=False)
+        if w["term_set"].startswith("lj"):
+            from proddl2_gb300 import synth
+            ts = O.TERMS_LJ_COMP if w["term_set"] == "lj_comp" else O.TERMS_LJ_AVG
+            rl, ll = synth.lj_params(w["n_rec"], 11), synth.lj_params(w["n_lig"], 12)
+            lj = O.LjParams(rl[0], rl[1], rl[2], ll[0], ll[1], mix=1, cut=9.0)
+            self.rg = O.lj_receptor_terms(self.geom, pair.receptor.xyz, lj, ts)
+            self.wts = O.lj_ligand_weights(lj, ts)
+        else:
+            ts = O.TERMS_SHAPE_ACE if w["term_set"] == "shape_ace" else O.TERMS_SHAPE
+            tp = O.TermParams(term_set=ts, ace_matrix=pair.ace)
+            # the reference runs one FFTCorrelator per term: shape + each type
+            self.rg = O.receptor_terms(self.geom, pair.receptor.xyz, pair.receptor.ace_type, tp, folded=False)
+            self.wts = O.ligand_term_weights(pair.ligand.ace_type, tp, folded=False)
         self.rs = O.receptor_spectra(self.rg, workers=threads)
-        self.wts = O.ligand_term_weights(pair.ligand.ace_type, tp, folded=False)
         self.k = w["peaks"]
 
     def rotations(self, idx):
@@ -266,9 +276,14 @@ def run_ours(args):
                      cluster_radius=args.cluster_radius)
     scan = FFTScan(cfg)
     t0 = time.perf_counter()
-    scan.set_receptor(pair.receptor.xyz, pair.receptor.ace_type)
+    if w["term_set"].startswith("lj"):
+        rl, ll = synth.lj_params(w["n_rec"], 11), synth.lj_params(w["n_lig"], 12)
+        scan.set_pair_lj(pair.receptor.xyz, rl[0], rl[1], rl[2], pair.ligand.xyz, ll[0], ll[1])
+    else:
+        scan.set_receptor(pair.receptor.xyz, pair.receptor.ace_type)
     receptor_ms = 1000.0 * (time.perf_counter() - t0)
-    scan.set_ligand(pair.ligand.xyz, pair.ligand.ace_type)
+    if not w["term_set"].startswith("lj"):
+        scan.set_ligand(pair.ligand.xyz, pair.ligand.ace_type)
 
     rot_host = np.ascontiguousarray(pair.rotations.reshape(n_rot, 9))
     d_rot = torch.from_numpy(rot_host).to(dev)

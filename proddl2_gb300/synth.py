@@ -136,6 +136,14 @@ def make_pair(n_rec, n_lig, n_rot, seed, n_types=18):
     return Pair(rec, lig, rots, ace_matrix(n_types, seed * 4 + 4))
 
 
+def lj_params(n, seed, alpha=0.4):
+    """Per-atom (sigma, eps, alpha) for the LJ potentials: sigma uniform in
+    [3.0, 3.9] A, eps in [0.05, 0.6], alpha constant (the reference's option
+    generator uses alpha 0.4)."""
+    rng = _rng(seed)
+    return rng.uniform(3.0, 3.9, n), rng.uniform(0.05, 0.6, n), np.full(n, float(alpha))
+
+
 def uneven_pairs(n_pairs, seed, rec_range=(800, 6000), lig_range=(300, 2000), n_types=18):
     """Pairs with log-uniform receptor and ligand sizes (the batched-workload
     generator): a list of (receptor, ligand) molecules in scan frames."""
@@ -158,6 +166,9 @@ WORKLOADS = {
                     n_rot=2000, rot_batch=64, peaks=4, top=100),
     "shape_ace128": dict(n_rec=4000, n_lig=1500, grid_n=128, grid_step=1.2, term_set="shape_ace",
                          n_rot=9000, rot_batch=64, peaks=4, top=100),
+    # the reference's default potential (ljComp, K = 2) at the same size
+    "ljcomp128": dict(n_rec=4000, n_lig=1500, grid_n=128, grid_step=1.2, term_set="lj_comp",
+                      n_rot=9000, rot_batch=64, peaks=4, top=100),
     # many uneven pairs: receptors 800-6000 / ligands 300-2000 atoms (log-uniform),
     # grid edge per pair from pair_grid (48-144), shape + 18 desolvation terms
     "pairs256": dict(n_pairs=256, grid_step=1.2, term_set="shape_ace", n_rot=3000, rot_batch=64, peaks=4),

@@ -356,8 +356,8 @@ def run_ours(args):
     batch = info["rot_batch"]
     avg_launch_ms = pencil_ms / max(launches, 1)
     # one timed stage is one kernel, except the queue + clustering stage:
-    # init, 6 x (digit pass + pick), gather, finish
-    per_stage = {"finalize": 15 if args.cluster else 1}
+    # bound, gather, check, 6 x (digit pass + pick), gather, finish
+    per_stage = {"finalize": 17 if args.cluster else 1}
     gpu_launches = sum(v[0] * per_stage.get(k, 1) for k, v in kstats.items())
     total_kernel_ms = sum(v[1] for v in kstats.values())
     share = pencil_ms / total_kernel_ms if total_kernel_ms else None

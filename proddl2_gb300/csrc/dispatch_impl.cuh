@@ -107,20 +107,27 @@ template <int N> struct SizeOpsImpl {
         return cudaGetLastError();
     }
 
-    static cudaError_t scan_batch(const BatchArgs& a, cudaStream_t s) {
+    // K1 over a.n_rot rotations
+    static cudaError_t prep(const BatchArgs& a, cudaStream_t s) {
+        const int nb = a.n_rot;
+        if (nb <= 0) return cudaSuccess;
         Geo geo{a.h, a.zero_h, a.center0, N};
+        const size_t sm1 = ((size_t)a.K * N + 1) * sizeof(int32_t) + (size_t)a.n_ent * sizeof(uint32_t);
+        cudaError_t e = set_smem((const void*)ligand_prep_kernel<N>, sm1);
+        if (e != cudaSuccess) return e;
+        ligand_prep_kernel<N><<<nb, 256, sm1, s>>>(a.rot, a.lig_xyz, a.lig_term, a.n_ent, a.K, geo, a.ent, a.offs,
+                                                    a.status, a.lig_w32, a.lig_w32 ? a.ent_w : nullptr, a.ent_idx);
+        return cudaGetLastError();
+    }
+
+    // K2 + K3 over a.n_rot rotations (and, on the queue + clustering path,
+    // the selection that writes the peaks).  a.ev (optional): events recorded
+    // before K2, between K2 and K3, after K3 and after the clustering stage.
+    static cudaError_t middle(const BatchArgs& a, cudaStream_t s) {
         const int nb = a.n_rot;
         if (nb <= 0) return cudaSuccess;
         cudaError_t e;
         if (a.ev && (e = cudaEventRecord(a.ev[0], s)) != cudaSuccess) return e;
-        // K1
-        const size_t sm1 = ((size_t)a.K * N + 1) * sizeof(int32_t) + (size_t)a.n_ent * sizeof(uint32_t);
-        if ((e = set_smem((const void*)ligand_prep_kernel<N>, sm1)) != cudaSuccess) return e;
-        ligand_prep_kernel<N><<<nb, 256, sm1, s>>>(a.rot, a.lig_xyz, a.lig_term, a.n_ent, a.K, geo, a.ent, a.offs,
-                                                    a.status, a.lig_w32, a.lig_w32 ? a.ent_w : nullptr, a.ent_idx);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        if (a.ev && (e = cudaEventRecord(a.ev[1], s)) != cudaSuccess) return e;
-        // K2
         bool pmajor = false;
         if constexpr (kHasTc) {
             if (a.use_tc) {
@@ -142,7 +149,7 @@ template <int N> struct SizeOpsImpl {
             }
             if (e != cudaSuccess) return e;
         }
-        if (a.ev && (e = cudaEventRecord(a.ev[2], s)) != cudaSuccess) return e;
+        if (a.ev && (e = cudaEventRecord(a.ev[1], s)) != cudaSuccess) return e;
         // K3 (the queue + clustering path also writes every correlation grid)
         const size_t sm3 = plane_smem();
         dim3 grid3(N, nb);
@@ -156,25 +163,39 @@ template <int N> struct SizeOpsImpl {
         }
         if (e != cudaSuccess) return e;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        if (a.ev && (e = cudaEventRecord(a.ev[3], s)) != cudaSuccess) return e;
-        // K4
+        if (a.ev && (e = cudaEventRecord(a.ev[2], s)) != cudaSuccess) return e;
         if (a.wide.corr) {
             BatchArgs w = a;
             w.wide.corr = corr;
             if ((e = wide_select_batch(w, N, s)) != cudaSuccess) return e;
-        } else {
-            finalize_kernel<N><<<nb, 256, 0, s>>>(a.cand_v, a.cand_i, a.ent, a.status, a.rgrid, a.n_ent,
-                                                  a.peak_stride, a.k_out, a.max_val, a.h, a.first_rot_id, a.peaks,
-                                                  a.n_peaks, a.pool_v, a.pool_i, a.lig_w64,
-                                                  a.lig_w64 ? a.ent_idx : nullptr);
-            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            if (a.ev && (e = cudaEventRecord(a.ev[3], s)) != cudaSuccess) return e;
         }
-        if (a.ev && (e = cudaEventRecord(a.ev[4], s)) != cudaSuccess) return e;
         return cudaSuccess;
     }
 
+    // K4 over a.n_rot rotations (not on the queue + clustering path)
+    static cudaError_t finish(const BatchArgs& a, cudaStream_t s) {
+        const int nb = a.n_rot;
+        if (nb <= 0 || a.wide.corr) return cudaSuccess;
+        finalize_kernel<N><<<nb, 256, 0, s>>>(a.cand_v, a.cand_i, a.ent, a.status, a.rgrid, a.n_ent, a.peak_stride,
+                                              a.k_out, a.max_val, a.h, a.first_rot_id, a.peaks, a.n_peaks,
+                                              a.pool_v, a.pool_i, a.lig_w64, a.lig_w64 ? a.ent_idx : nullptr);
+        return cudaGetLastError();
+    }
+
+    // the whole pipeline for one batch (work buffers sized for a.n_rot)
+    static cudaError_t scan_batch(const BatchArgs& a, cudaStream_t s) {
+        cudaError_t e = prep(a, s);
+        if (e != cudaSuccess) return e;
+        BatchArgs m = a;
+        m.ev = nullptr;
+        if ((e = middle(m, s)) != cudaSuccess) return e;
+        return finish(a, s);
+    }
+
     static const SizeOps* ops() {
-        static const SizeOps o{N, &receptor_fft, &circ_scales, kHasTc, &scan_batch, &pencil_smem};
+        static const SizeOps o{N, &receptor_fft, &circ_scales, kHasTc, &scan_batch, &pencil_smem, &prep, &middle,
+                               &finish};
         return &o;
     }
 };

@@ -65,7 +65,9 @@ struct fftdock_ctx {
     float* ent_w = nullptr;
     int32_t* ent_idx = nullptr;
 
-    // per-batch work
+    // work: ent/offs/cand (and ent_w/ent_idx) per group of G rotations,
+    // g2 per batch of B
+    int G = 0;
     uint32_t* ent = nullptr;
     int32_t* offs = nullptr;
     float2* g2 = nullptr;
@@ -91,10 +93,16 @@ struct fftdock_ctx {
     // queue + clustering path (cfg.cluster_trans)
     fftdock::WideArgs wide{};
 
-    // kernel timing (fftdock_profile)
+    // kernel timing (fftdock_profile): event pool and (stage, from, to)
+    // records of pool indices
     bool profiling = false;
     std::vector<cudaEvent_t> ev_pool;
     size_t ev_used = 0;
+    struct EvRec {
+        int stage;
+        size_t from, to;
+    };
+    std::vector<EvRec> ev_recs;
 };
 
 namespace {
@@ -203,35 +211,93 @@ int check_pipeline(fftdock_ctx* ctx) {
     return FFTDOCK_OK;
 }
 
+// n events from the profiling pool; returns the index of the first
+int take_events(fftdock_ctx* ctx, size_t n, size_t* first) {
+    while (ctx->ev_pool.size() < ctx->ev_used + n) {
+        cudaEvent_t ev;
+        cudaError_t e = cudaEventCreate(&ev);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaEventCreate");
+        ctx->ev_pool.push_back(ev);
+    }
+    *first = ctx->ev_used;
+    ctx->ev_used += n;
+    return FFTDOCK_OK;
+}
+
+// Rotations per group: ligand prep and finalize run once per group (full-GPU
+// launches), pencil and plane once per batch of B.
+int group_size(int B) { return B * std::max(1, 1024 / B); }
+
 // queue every batch of a call; rot/peaks/npeaks/status are device arrays
 // covering the whole call
 int run_batches(fftdock_ctx* ctx, int n_rot, const double* rot, int first_id, fftdock_peak* peaks,
                 int32_t* npeaks, int32_t* status, cudaStream_t s, float* dbg, float* pool_v, int32_t* pool_i) {
-    BatchArgs a = batch_args(ctx);
-    for (int b0 = 0; b0 < n_rot; b0 += ctx->B) {
-        a.ev = nullptr;
+    const BatchArgs a = batch_args(ctx);
+    const int N = ctx->N, stride = ctx->cfg.peaks_per_rot;
+    int rc;
+    size_t ev = 0;
+    for (int g0 = 0; g0 < n_rot; g0 += ctx->G) {
+        BatchArgs ga = a;
+        ga.ev = nullptr;
+        ga.n_rot = std::min(ctx->G, n_rot - g0);
+        ga.rot = rot + (size_t)g0 * 9;
+        ga.status = status + g0;
+        ga.peaks = peaks + (size_t)g0 * stride;
+        ga.n_peaks = npeaks + g0;
+        ga.first_rot_id = first_id + g0;
+        ga.dbg_corr = dbg ? dbg + (size_t)g0 * ctx->V : nullptr;
+        ga.pool_v = pool_v ? pool_v + (size_t)g0 * fftdock::kKC : nullptr;
+        ga.pool_i = pool_i ? pool_i + (size_t)g0 * fftdock::kKC : nullptr;
+        cudaError_t e;
         if (ctx->profiling) {
-            while (ctx->ev_pool.size() < ctx->ev_used + 5) {
-                cudaEvent_t ev;
-                cudaError_t e = cudaEventCreate(&ev);
-                if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaEventCreate");
-                ctx->ev_pool.push_back(ev);
-            }
-            a.ev = ctx->ev_pool.data() + ctx->ev_used;
-            ctx->ev_used += 5;
+            if ((rc = take_events(ctx, 2, &ev))) return rc;
+            if ((e = cudaEventRecord(ctx->ev_pool[ev], s)) != cudaSuccess) return cuda_fail(ctx, e, "event");
         }
-        const int nb = std::min(ctx->B, n_rot - b0);
-        a.rot = rot + (size_t)b0 * 9;
-        a.n_rot = nb;
-        a.status = status + b0;
-        a.peaks = peaks + (size_t)b0 * ctx->cfg.peaks_per_rot;
-        a.n_peaks = npeaks + b0;
-        a.first_rot_id = first_id + b0;
-        a.dbg_corr = dbg ? dbg + (size_t)b0 * ctx->V : nullptr;
-        a.pool_v = pool_v ? pool_v + (size_t)b0 * fftdock::kKC : nullptr;
-        a.pool_i = pool_i ? pool_i + (size_t)b0 * fftdock::kKC : nullptr;
-        cudaError_t e = ctx->ops->scan_batch(a, s);
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "scan batch launch");
+        if ((e = ctx->ops->prep(ga, s)) != cudaSuccess) return cuda_fail(ctx, e, "ligand prep launch");
+        if (ctx->profiling) {
+            if ((e = cudaEventRecord(ctx->ev_pool[ev + 1], s)) != cudaSuccess) return cuda_fail(ctx, e, "event");
+            ctx->ev_recs.push_back({0, ev, ev + 1});
+        }
+        for (int j = 0; j < ga.n_rot; j += ctx->B) {
+            BatchArgs b = ga;
+            b.n_rot = std::min(ctx->B, ga.n_rot - j);
+            b.rot += (size_t)j * 9;
+            b.status += j;
+            b.peaks += (size_t)j * stride;
+            b.n_peaks += j;
+            b.first_rot_id += j;
+            if (b.dbg_corr) b.dbg_corr += (size_t)j * ctx->V;
+            if (b.pool_v) b.pool_v += (size_t)j * fftdock::kKC;
+            if (b.pool_i) b.pool_i += (size_t)j * fftdock::kKC;
+            b.ent += (size_t)j * ctx->n_ent;
+            b.offs += (size_t)j * (ctx->K * N + 1);
+            b.cand_v += (size_t)j * N * fftdock::kKC;
+            b.cand_i += (size_t)j * N * fftdock::kKC;
+            if (b.ent_w) b.ent_w += (size_t)j * ctx->n_ent;
+            if (b.ent_idx) b.ent_idx += (size_t)j * ctx->n_ent;
+            cudaEvent_t evs[4];
+            const bool wide = b.wide.corr != nullptr;
+            if (ctx->profiling) {
+                const size_t n_ev = wide ? 4 : 3;
+                if ((rc = take_events(ctx, n_ev, &ev))) return rc;
+                for (size_t k = 0; k < n_ev; ++k) evs[k] = ctx->ev_pool[ev + k];
+                b.ev = evs;
+                ctx->ev_recs.push_back({1, ev, ev + 1});
+                ctx->ev_recs.push_back({2, ev + 1, ev + 2});
+                if (wide) ctx->ev_recs.push_back({3, ev + 2, ev + 3});
+            }
+            if ((e = ctx->ops->middle(b, s)) != cudaSuccess) return cuda_fail(ctx, e, "scan batch launch");
+        }
+        if (ga.wide.corr) continue;
+        if (ctx->profiling) {
+            if ((rc = take_events(ctx, 2, &ev))) return rc;
+            if ((e = cudaEventRecord(ctx->ev_pool[ev], s)) != cudaSuccess) return cuda_fail(ctx, e, "event");
+        }
+        if ((e = ctx->ops->finish(ga, s)) != cudaSuccess) return cuda_fail(ctx, e, "finalize launch");
+        if (ctx->profiling) {
+            if ((e = cudaEventRecord(ctx->ev_pool[ev + 1], s)) != cudaSuccess) return cuda_fail(ctx, e, "event");
+            ctx->ev_recs.push_back({3, ev, ev + 1});
+        }
     }
     return FFTDOCK_OK;
 }
@@ -440,6 +506,7 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
     ctx->PP = fftdock::pencil_pitch(N);
     ctx->V = (size_t)N * N * N;
     ctx->B = c.rot_batch;
+    ctx->G = group_size(ctx->B);
     // centred geometry exactly as UniformCubicGeometry(step, logicalSize)
     const double h = c.grid_step;
     const double s_size = h + h * (double)(N - 1);
@@ -482,10 +549,10 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
         ctx->spec = sp;
     }
     CK(dalloc(&ctx->rgrid, (size_t)ctx->K * ctx->V));
-    CK(dalloc(&ctx->offs, (size_t)ctx->B * (ctx->K * N + 1)));
+    CK(dalloc(&ctx->offs, (size_t)ctx->G * (ctx->K * N + 1)));
     CK(dalloc(&ctx->g2, (size_t)ctx->B * N * ctx->PP));
-    CK(dalloc(&ctx->cand_v, (size_t)ctx->B * N * fftdock::kKC));
-    CK(dalloc(&ctx->cand_i, (size_t)ctx->B * N * fftdock::kKC));
+    CK(dalloc(&ctx->cand_v, (size_t)ctx->G * N * fftdock::kKC));
+    CK(dalloc(&ctx->cand_i, (size_t)ctx->G * N * fftdock::kKC));
     CK(dalloc(&ctx->err_dev, 1));
     CK(cudaMemset(ctx->err_dev, 0, sizeof(int)));
     if (ctx->use_tc) {
@@ -649,7 +716,7 @@ int fftdock_set_ligand(fftdock_ctx* ctx, int32_t n, const double* xyz, const int
     dfree(ctx->ent);
     CK(dalloc(&ctx->lig_xyz, (size_t)n * 3));
     CK(dalloc(&ctx->lig_term, (size_t)n));
-    CK(dalloc(&ctx->ent, (size_t)ctx->B * n));
+    CK(dalloc(&ctx->ent, (size_t)ctx->G * n));
     CK(cudaMemcpy(ctx->lig_xyz, xyz, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->lig_term, term.data(), (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice));
     // window of x cells that holds the ligand under every rotation about the
@@ -862,14 +929,14 @@ int fftdock_set_pair_lj(fftdock_ctx* ctx, int32_t n_rec, const double* rec_xyz, 
     dfree(ctx->ent_idx);
     CK(dalloc(&ctx->lig_xyz, exyz.size()));
     CK(dalloc(&ctx->lig_term, (size_t)n_ent));
-    CK(dalloc(&ctx->ent, (size_t)ctx->B * n_ent));
+    CK(dalloc(&ctx->ent, (size_t)ctx->G * n_ent));
     CK(cudaMemcpy(ctx->lig_xyz, exyz.data(), exyz.size() * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->lig_term, term.data(), (size_t)n_ent * sizeof(int32_t), cudaMemcpyHostToDevice));
     if (comp) {
         CK(dalloc(&ctx->lig_w32, (size_t)n_ent));
         CK(dalloc(&ctx->lig_w64, (size_t)n_ent));
-        CK(dalloc(&ctx->ent_w, (size_t)ctx->B * n_ent));
-        CK(dalloc(&ctx->ent_idx, (size_t)ctx->B * n_ent));
+        CK(dalloc(&ctx->ent_w, (size_t)ctx->G * n_ent));
+        CK(dalloc(&ctx->ent_idx, (size_t)ctx->G * n_ent));
         CK(cudaMemcpy(ctx->lig_w32, w32.data(), (size_t)n_ent * sizeof(float), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(ctx->lig_w64, w64.data(), (size_t)n_ent * sizeof(double), cudaMemcpyHostToDevice));
     }
@@ -989,7 +1056,10 @@ int fftdock_scan_candidates(fftdock_ctx* ctx, int32_t n_rot, const double* rot, 
 int fftdock_profile(fftdock_ctx* ctx, int32_t enable) {
     if (!ctx) return FFTDOCK_EINVAL;
     ctx->profiling = enable != 0;
-    if (enable) ctx->ev_used = 0;
+    if (enable) {
+        ctx->ev_used = 0;
+        ctx->ev_recs.clear();
+    }
     return FFTDOCK_OK;
 }
 
@@ -999,13 +1069,11 @@ int fftdock_get_kernel_stats(fftdock_ctx* ctx, fftdock_kernel_stats* out) {
     if (ctx->ev_used == 0) return FFTDOCK_OK;
     CK(cudaSetDevice(ctx->cfg.device));
     CK(cudaEventSynchronize(ctx->ev_pool[ctx->ev_used - 1]));
-    for (size_t b = 0; b + 5 <= ctx->ev_used; b += 5) {
-        for (int k = 0; k < 4; ++k) {
-            float ms = 0.f;
-            CK(cudaEventElapsedTime(&ms, ctx->ev_pool[b + k], ctx->ev_pool[b + k + 1]));
-            out->launches[k] += 1;
-            out->total_ms[k] += ms;
-        }
+    for (const auto& r : ctx->ev_recs) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, ctx->ev_pool[r.from], ctx->ev_pool[r.to]));
+        out->launches[r.stage] += 1;
+        out->total_ms[r.stage] += ms;
     }
     return FFTDOCK_OK;
 }

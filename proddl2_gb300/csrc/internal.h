@@ -133,7 +133,7 @@ struct BatchArgs {
     float* dbg_corr;            // optional [B][N^3]
     float* pool_v;              // optional [B][KC]
     int32_t* pool_i;
-    cudaEvent_t* ev;            // optional: 5 events recorded around the 4 kernels
+    cudaEvent_t* ev;            // optional: events recorded by the middle stage (see SizeOps::middle)
     // tensor-core pencil stage (use_tc): g2 is then [B][N*H][N] (x fastest)
     int use_tc;
     const float2* circ;         // [K][N*H][N] receptor circulant samples
@@ -158,6 +158,11 @@ struct SizeOps {
     cudaError_t (*scan_batch)(const BatchArgs& a, cudaStream_t s);
     // shared-memory bytes of the pencil kernel for (K, n_ent)
     size_t (*pencil_smem)(int K, int n_ent);
+    // the pipeline's stages: ligand prep, pencil + plane (+ clustering
+    // selection), finalize; scan_batch = all three for one batch
+    cudaError_t (*prep)(const BatchArgs& a, cudaStream_t s);
+    cudaError_t (*middle)(const BatchArgs& a, cudaStream_t s);
+    cudaError_t (*finish)(const BatchArgs& a, cudaStream_t s);
 };
 
 const SizeOps* size_ops(int n);

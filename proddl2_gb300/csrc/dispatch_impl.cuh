@@ -42,7 +42,6 @@ template <int N> struct SizeOpsImpl {
 
     static constexpr bool kHasTc = N <= 128;
 
-    static size_t tc_smem() { return (size_t)TC_STAGES * TC_STAGE_BYTES + N * sizeof(TcPair) + N * sizeof(float2); }
 
     static cudaError_t circ_scales(const float2* circ, int K, int8_t* cscale, cudaStream_t s) {
         if constexpr (kHasTc) {
@@ -99,11 +98,11 @@ template <int N> struct SizeOpsImpl {
         return cudaGetLastError();
     }
 
-    template <bool PMAJOR, bool DBG>
+    template <bool DBG>
     static cudaError_t launch_plane(dim3 grid, size_t sm, const BatchArgs& a, float* corr, cudaStream_t s) {
-        cudaError_t e = set_smem((const void*)plane_kernel<N, PMAJOR, DBG>, sm);
+        cudaError_t e = set_smem((const void*)plane_kernel<N, DBG>, sm);
         if (e != cudaSuccess) return e;
-        plane_kernel<N, PMAJOR, DBG><<<grid, 32 * G, sm, s>>>(a.g2, a.tw32, a.cand_v, a.cand_i, corr);
+        plane_kernel<N, DBG><<<grid, 32 * G, sm, s>>>(a.g2, a.tw32, a.cand_v, a.cand_i, corr);
         return cudaGetLastError();
     }
 
@@ -116,7 +115,8 @@ template <int N> struct SizeOpsImpl {
         cudaError_t e = set_smem((const void*)ligand_prep_kernel<N>, sm1);
         if (e != cudaSuccess) return e;
         ligand_prep_kernel<N><<<nb, 256, sm1, s>>>(a.rot, a.lig_xyz, a.lig_term, a.n_ent, a.K, geo, a.ent, a.offs,
-                                                    a.status, a.lig_w32, a.lig_w32 ? a.ent_w : nullptr, a.ent_idx);
+                                                    a.status, a.lig_w32, a.lig_w32 ? a.ent_w : nullptr, a.ent_idx,
+                                                    a.use_tc ? a.ent_t : nullptr, a.tpad, a.n_pad, a.x0);
         return cudaGetLastError();
     }
 
@@ -128,19 +128,20 @@ template <int N> struct SizeOpsImpl {
         if (nb <= 0) return cudaSuccess;
         cudaError_t e;
         if (a.ev && (e = cudaEventRecord(a.ev[0], s)) != cudaSuccess) return e;
-        bool pmajor = false;
+        bool tc = false;
         if constexpr (kHasTc) {
             if (a.use_tc) {
-                pmajor = true;
-                const size_t smt = tc_smem();
+                tc = true;
+                const size_t smt = tc_smem_bytes(N, a.W / 8, a.n_tc_terms);
                 if ((e = set_smem((const void*)pencil_tc_kernel<N>, smt)) != cudaSuccess) return e;
                 dim3 gridt(N * H, (nb + TC_ROT - 1) / TC_ROT);
-                pencil_tc_kernel<N><<<gridt, 160, smt, s>>>(a.circ, a.cscale, a.ent, a.offs, a.tw32, a.g2, a.K,
-                                                           a.n_ent, nb, a.x0, a.W, a.err);
+                pencil_tc_kernel<N><<<gridt, TC_THREADS, smt, s>>>(a.circ, a.cscale, a.ent_t, a.tinfo,
+                                                                  a.n_tc_terms, a.tw32, a.g2, a.n_pad, nb, a.x0,
+                                                                  a.W, a.err);
                 if ((e = cudaGetLastError()) != cudaSuccess) return e;
             }
         }
-        if (!pmajor) {
+        if (!tc) {
             if (a.lig_w32) {
                 if (a.spec_bf16) return cudaErrorNotSupported;  // weighted sets run with FP32 spectra
                 e = launch_pencil<float2, true>(a, nb, s);
@@ -154,13 +155,8 @@ template <int N> struct SizeOpsImpl {
         const size_t sm3 = plane_smem();
         dim3 grid3(N, nb);
         float* corr = a.dbg_corr ? a.dbg_corr : a.wide.corr;
-        if (pmajor) {
-            if (corr) e = launch_plane<true, true>(grid3, sm3, a, corr, s);
-            else e = launch_plane<true, false>(grid3, sm3, a, nullptr, s);
-        } else {
-            if (corr) e = launch_plane<false, true>(grid3, sm3, a, corr, s);
-            else e = launch_plane<false, false>(grid3, sm3, a, nullptr, s);
-        }
+        if (corr) e = launch_plane<true>(grid3, sm3, a, corr, s);
+        else e = launch_plane<false>(grid3, sm3, a, nullptr, s);
         if (e != cudaSuccess) return e;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if (a.ev && (e = cudaEventRecord(a.ev[2], s)) != cudaSuccess) return e;

@@ -89,6 +89,11 @@ struct fftdock_ctx {
     int8_t* cscale = nullptr;
     int* err_dev = nullptr;
     int x0 = 0, W = 0;
+    bool tc_ready = false;       // the ligand fits the tensor stage (window, terms, unweighted)
+    uint32_t* ent_t = nullptr;   // [G/128][n_pad][128]
+    int32_t* tinfo = nullptr;    // non-empty terms: padded entry starts, then term ids
+    int32_t* tpad = nullptr;     // [K] padded start - start per term
+    int n_tc_terms = 0, n_pad = 0;
 
     // queue + clustering path (cfg.cluster_trans)
     fftdock::WideArgs wide{};
@@ -189,11 +194,16 @@ BatchArgs batch_args(fftdock_ctx* ctx) {
     a.peak_stride = ctx->cfg.peaks_per_rot;
     a.k_out = std::min(ctx->cfg.peaks_per_rot, ctx->cfg.max_trans_inp);
     a.max_val = ctx->cfg.max_val_corr;
-    a.use_tc = ctx->use_tc ? 1 : 0;
     a.circ = ctx->circ;
     a.cscale = ctx->cscale;
     a.x0 = ctx->x0;
     a.W = ctx->W;
+    a.use_tc = ctx->use_tc && ctx->tc_ready ? 1 : 0;
+    a.ent_t = ctx->ent_t;
+    a.tinfo = ctx->tinfo;
+    a.tpad = ctx->tpad;
+    a.n_tc_terms = ctx->n_tc_terms;
+    a.n_pad = ctx->n_pad;
     a.err = ctx->err_dev;
     a.wide = ctx->wide;
     return a;
@@ -275,6 +285,7 @@ int run_batches(fftdock_ctx* ctx, int n_rot, const double* rot, int first_id, ff
             b.cand_i += (size_t)j * N * fftdock::kKC;
             if (b.ent_w) b.ent_w += (size_t)j * ctx->n_ent;
             if (b.ent_idx) b.ent_idx += (size_t)j * ctx->n_ent;
+            if (b.ent_t) b.ent_t += (size_t)j * ctx->n_pad;  // j is a multiple of 128 on the tensor path
             cudaEvent_t evs[4];
             const bool wide = b.wide.corr != nullptr;
             if (ctx->profiling) {
@@ -390,7 +401,7 @@ int fftdock_get_scan_info(const fftdock_ctx* ctx, fftdock_scan_info* out) {
     if (!ctx || !out) return FFTDOCK_EINVAL;
     out->grid_n = ctx->N;
     out->n_terms = ctx->K;
-    out->pencil_path = ctx->use_tc ? FFTDOCK_PENCIL_TENSOR : FFTDOCK_PENCIL_FFT;
+    out->pencil_path = ctx->use_tc && ctx->tc_ready ? FFTDOCK_PENCIL_TENSOR : FFTDOCK_PENCIL_FFT;
     out->rot_batch = ctx->B;
     out->n_entries = ctx->have_lig ? ctx->n_ent : 0;
     out->window_x0 = ctx->x0;
@@ -424,6 +435,9 @@ void fftdock_destroy(fftdock_ctx* ctx) {
     dfree(ctx->status_dev);
     dfree(ctx->circ);
     dfree(ctx->cscale);
+    dfree(ctx->ent_t);
+    dfree(ctx->tinfo);
+    dfree(ctx->tpad);
     dfree(ctx->err_dev);
     dfree(ctx->wide.corr);
     dfree(ctx->wide.hist);
@@ -506,6 +520,8 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
     ctx->PP = fftdock::pencil_pitch(N);
     ctx->V = (size_t)N * N * N;
     ctx->B = c.rot_batch;
+    // the tensor stage takes rotations in groups of 128
+    if (ctx->use_tc) ctx->B = (ctx->B + fftdock::kTcRot - 1) / fftdock::kTcRot * fftdock::kTcRot;
     ctx->G = group_size(ctx->B);
     // centred geometry exactly as UniformCubicGeometry(step, logicalSize)
     const double h = c.grid_step;
@@ -739,6 +755,43 @@ int fftdock_set_ligand(fftdock_ctx* ctx, int32_t n, const double* xyz, const int
     ctx->x0 = (int)x0;
     ctx->W = W;
     ctx->n_ent = n;
+    // tensor stage: entry ranges of the non-empty terms (the same in every
+    // rotation: entries are sorted by term first)
+    ctx->tc_ready = false;
+    dfree(ctx->ent_t);
+    dfree(ctx->tinfo);
+    dfree(ctx->tpad);
+    if (ctx->use_tc) {
+        std::vector<int32_t> cnt(ctx->K, 0);
+        for (int i = 0; i < n; ++i) ++cnt[term[i]];
+        // rows of the transposed entries: each term's range padded to 16
+        std::vector<int32_t> starts, ids, tpad(ctx->K, 0);
+        int run = 0, prun = 0;
+        for (int t = 0; t < ctx->K; ++t) {
+            if (cnt[t] == 0) continue;
+            starts.push_back(prun);
+            ids.push_back(t);
+            tpad[t] = prun - run;
+            run += cnt[t];
+            prun += (cnt[t] + 15) / 16 * 16;
+        }
+        starts.push_back(prun);
+        const int ka = (int)ids.size();
+        if (W / 8 <= fftdock::kTcMaxChunks && ka <= fftdock::kTcMaxTerms) {
+            std::vector<int32_t> info(starts);
+            info.insert(info.end(), ids.begin(), ids.end());
+            CK(dalloc(&ctx->ent_t, (size_t)ctx->G * prun));
+            // the padding rows are never written: 0xffffffff marks them
+            CK(cudaMemset(ctx->ent_t, 0xff, (size_t)ctx->G * prun * sizeof(uint32_t)));
+            CK(dalloc(&ctx->tinfo, info.size()));
+            CK(dalloc(&ctx->tpad, tpad.size()));
+            CK(cudaMemcpy(ctx->tinfo, info.data(), info.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(ctx->tpad, tpad.data(), tpad.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+            ctx->n_tc_terms = ka;
+            ctx->n_pad = prun;
+            ctx->tc_ready = true;
+        }
+    }
     ctx->have_lig = true;
     return FFTDOCK_OK;
 }

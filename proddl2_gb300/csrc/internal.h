@@ -71,6 +71,12 @@ cudaError_t build_receptor_grids(const ReceptorGridArgs& a, cudaStream_t s);
 // gathered in one pass, sorted and clustered per rotation.  When the bound is
 // missing or too loose, a radix select over 64-bit keys (ordered float bits
 // << 32 | cell offset, so ties go to the lower offset) narrows the set first.
+// tensor pencil stage: rotations per CTA (the MMA's N), largest window in
+// 8-cell chunks, most non-empty terms
+constexpr int kTcRot = 128;
+constexpr int kTcMaxChunks = 16;  // the whole x range at N = 128
+constexpr int kTcMaxTerms = 64;
+
 constexpr int kWideMax = 16384;
 constexpr int kWideBins = 4096;  // 12-bit digits
 
@@ -134,11 +140,16 @@ struct BatchArgs {
     float* pool_v;              // optional [B][KC]
     int32_t* pool_i;
     cudaEvent_t* ev;            // optional: events recorded by the middle stage (see SizeOps::middle)
-    // tensor-core pencil stage (use_tc): g2 is then [B][N*H][N] (x fastest)
+    // tensor-core pencil stage (use_tc); it writes g2 in the same [B][N][PP] layout
     int use_tc;
     const float2* circ;         // [K][N*H][N] receptor circulant samples
     const int8_t* cscale;       // [N*H] power-of-two scale exponents
     int x0, W;                  // ligand window along x
+    uint32_t* ent_t;            // [B/128][n_pad][128] entries transposed per group of 128 rotations
+    const int32_t* tinfo;       // padded entry starts of the n_tc_terms non-empty terms, then their term ids
+    const int32_t* tpad;        // [K] padded start - start of each term's entries
+    int n_tc_terms;
+    int n_pad;                  // entries per rotation with every term padded to a multiple of 16
     int* err;                   // device word: nonzero after a pipeline timeout
     WideArgs wide;              // queue + clustering path (wide.corr != nullptr)
 };

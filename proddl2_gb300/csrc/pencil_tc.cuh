@@ -11,29 +11,50 @@
 //   D[x][r] = sum_k C[x][k] F[r][k],  k = (t, n, re/im)
 // run on the tensor cores as real M = 128 (x) x N = 128 (r) x K = 16 MMAs,
 // D_re and D_im in tensor memory.  FP32 accuracy comes from splitting each
-// operand into FP16 hi + lo parts and accumulating hi*hi + hi*lo + lo*hi in
-// FP32; per-pencil power-of-two scales keep both parts in the normal range.
+// operand into FP16 hi + lo parts and accumulating hi*hi + hi*lo + lo*hi;
+// per-pencil power-of-two scales keep both parts in the normal range.
 //
-// CTA: warps 0-3 produce (thread = rotation of the group) and run the
-// epilogue, warp 4 issues the MMAs.  A ring of STAGES shared-memory stages,
-// each one chunk = 8 window bins of one term, is handed over with mbarriers;
-// every wait is bounded and a timeout is reported through *err.
+// Operands.  C is Toeplitz: the tile of window chunk n0 = 8c is
+//   C_c[x][i] = c_t((x0 + 8c + i - x) mod N) = E[x + W - 8 - 8c][i],
+//   E[e][i]   = c_t((x0 + W - 8 + i - e) mod N),  e < 120 + W,
+// so one extended tile E of 120 + W rows per term serves every chunk: chunk
+// c's descriptor starts (W/8 - 1 - c) 8-row groups into E.  F comes from the
+// ligand entries of the term, which ligand prep writes transposed per group
+// of 128 rotations ([entry][rotation], sorted by (term, x) per rotation, each
+// term's range padded to a multiple of 16 with 0xffffffff, x relative to x0).
+// A term's entries occupy the same index range in every rotation; two threads
+// per rotation walk the two halves of the range with coalesced loads.  Each
+// keeps the running sum of its current x bin and stores it after every entry
+// into an FP32 staging row (the last store of a bin holds its sum: the
+// entries are sorted by x), which needs no branch.  The second half's first
+// bin may continue the first half's last one: its partial sum goes to a side
+// slot and is added after both halves are done.  The staging rows, laid over
+// the F tiles, are then converted in place into the hi/lo tiles.  The phase
+// table (scaled by the F scale) is replicated per lane ([phase][lane]) so
+// that the 32 lanes' lookups never share a bank.
+//
+// CTA (288 threads): eight producer warps (two threads per rotation) and an
+// MMA-issuing warp; the producers fill the next term's tiles only after the
+// tensor core has read the current ones, so two CTAs share an SM (shared
+// memory and 2 x 256 TMEM columns permitting) and overlap each other's MMAs
+// and production.  All waits are bounded; a timeout is reported through *err.
 #pragma once
 
 #include <cuda_fp16.h>
 
 #include "fft_core.cuh"
+#include "internal.h"
 #include "tc05.cuh"
 
 namespace fftdock {
 
-constexpr int TC_STAGES = 4;
-constexpr int TC_ROT = 128;                 // rotations per CTA (MMA N)
-constexpr int TC_TILE = 128 * 16 * 2;       // bytes of one 128 x 16 FP16 operand tile
-constexpr int TC_STAGE_BYTES = 6 * TC_TILE; // C_re hi/lo, C_im hi/lo, F hi/lo
+constexpr int TC_ROT = kTcRot;              // rotations per CTA (MMA N)
+constexpr int TC_THREADS = 288;             // 8 producer warps + the MMA warp
 constexpr uint32_t TC_LBO = 128, TC_SBO = 256;
-constexpr uint64_t TC_WAIT_NS = 2000000000ull;  // 2 s per wait
-constexpr float TC_F_SCALE = 16.0f;         // scale of the ligand sums before the FP16 split
+constexpr uint32_t TC_FTILE = 128 * 16 * 2;       // one 128 x 16 FP16 tile (hi or lo)
+constexpr uint32_t TC_FCHUNK = 2 * TC_FTILE;      // hi + lo of one window chunk
+constexpr uint64_t TC_WAIT_NS = 2000000000ull;    // 2 s per wait
+constexpr float TC_F_SCALE = 16.0f;               // scale of the ligand sums before the FP16 split
 
 struct TcPair {      // one receptor circulant sample d, as FP16 pairs
     __half2 re_h;    // (Re c, -Im c) hi: multiplies (F_re, F_im) into the real output
@@ -48,215 +69,293 @@ __device__ __forceinline__ void split_h2(float a, float b, __half2& hi, __half2&
     lo = __floats2half2_rn(a - back.x, b - back.y);
 }
 
+// Shared-memory accesses to the operand tiles and staging rows.  Volatile:
+// they keep their order among themselves and against the fences and barriers
+// (volatile, with memory clobbers); without a clobber of their own, ordinary
+// loads of other shared arrays may move across them.
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
-    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d)
-                 : "memory");
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d));
+}
+__device__ __forceinline__ void st_shared_f2(uint32_t addr, float a, float b) {
+    asm volatile("st.shared.v2.f32 [%0], {%1, %2};" ::"r"(addr), "f"(a), "f"(b));
+}
+__device__ __forceinline__ float2 ld_shared_f2(uint32_t addr) {
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+    return v;
+}
+// load from a table that no longer changes: not volatile, so the compiler
+// may schedule it freely
+__device__ __forceinline__ float2 ld_shared_f2_const(uint32_t addr) {
+    float2 v;
+    asm("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+    return v;
 }
 __device__ __forceinline__ uint32_t h2u(__half2 h) { return *reinterpret_cast<uint32_t*>(&h); }
 
+// 8-row groups of the extended circulant tile E for a window of 8 n_chunks cells
+__host__ __device__ constexpr int tc_ext_groups(int n_chunks) { return 15 + n_chunks; }
+
+// dynamic shared memory of pencil_tc_kernel: F tiles / staging rows
+// [chunks][hi|lo], E tiles [4 parts][groups][256 B], phase table [N][32]
+// float2, staged samples [N], side slots [128] float2, term table; at least
+// 76 KB so that no more than two CTAs (2 x 256 TMEM columns) share an SM
+__host__ __device__ inline size_t tc_smem_bytes(int N, int n_chunks, int n_terms) {
+    size_t b = (size_t)n_chunks * TC_FCHUNK + (size_t)4 * tc_ext_groups(n_chunks) * 256 + (size_t)N * 32 * 8 +
+               (size_t)N * sizeof(TcPair) + (size_t)TC_ROT * 8 + (size_t)(2 * n_terms + 1) * 4;
+    b = (b + 15) & ~(size_t)15;
+    return b < 76 * 1024 ? 76 * 1024 : b;
+}
+
+// tinfo: [0, Ka] padded entry starts (multiples of 16) of the Ka non-empty
+// terms, [Ka + 1, 2 Ka] their term ids; n_pad = entry rows per rotation group
 template <int N>
-__global__ void __launch_bounds__(160, 1) pencil_tc_kernel(
-    const float2* __restrict__ circ, const int8_t* __restrict__ cscale, const uint32_t* __restrict__ ent,
-    const int32_t* __restrict__ offs, const float2* __restrict__ tw, float2* __restrict__ g2, int K, int n_ent,
+__global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
+    const float2* __restrict__ circ, const int8_t* __restrict__ cscale, const uint32_t* __restrict__ ent_t,
+    const int32_t* __restrict__ tinfo, int Ka, const float2* __restrict__ tw, float2* __restrict__ g2, int n_pad,
     int n_rot, int x0, int W, int* __restrict__ err) {
     static_assert(N <= 128, "the tensor pencil stage covers x in one 128-row tile");
     constexpr int H = N / 2 + 1;
     constexpr int NH = N * H;
+    constexpr int PP = pencil_pitch(N);
+    const int NC = W >> 3;
+    const int RG = tc_ext_groups(NC);
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    unsigned char* stages = smem_raw;                                               // [STAGES][6 tiles]
-    TcPair* pairs = reinterpret_cast<TcPair*>(smem_raw + TC_STAGES * TC_STAGE_BYTES);  // [N]
-    float2* tws = reinterpret_cast<float2*>(pairs + N);                             // [N]
-    __shared__ __align__(8) uint64_t full_bar[TC_STAGES];
-    __shared__ __align__(8) uint64_t empty_bar[TC_STAGES];
+    unsigned char* fbuf = smem_raw;                                            // [NC][hi | lo]
+    unsigned char* abuf = fbuf + NC * TC_FCHUNK;                               // [4][RG][256]
+    float2* twr = reinterpret_cast<float2*>(abuf + 4 * RG * 256);              // [N][32]
+    TcPair* pr = reinterpret_cast<TcPair*>(twr + N * 32);                      // [N]
+    float2* side = reinterpret_cast<float2*>(pr + N);                          // [128]
+    int32_t* tinf = reinterpret_cast<int32_t*>(side + TC_ROT);                 // [2 Ka + 1]
+    __shared__ __align__(8) uint64_t full_bar;
+    __shared__ __align__(8) uint64_t empty_bar;
     __shared__ __align__(8) uint64_t done_bar;
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
 
-    // a timeout elsewhere in this launch already failed the scan: do nothing
-    if (*(volatile int*)err != 0) return;
     const int p = blockIdx.x;           // pencil
     const int g = blockIdx.y;           // rotation group
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
     const unsigned ky = (unsigned)(p / H), kz = (unsigned)(p - (p / H) * H);
-    const int n_chunks = K * (W / 8);
     const float c_scale = ldexpf(1.0f, (int)cscale[p]);
 
-    for (int i = tid; i < N; i += blockDim.x) tws[i] = tw[i];
+    if (tid == 0) abort_flag = *(volatile int*)err;
+    __syncthreads();
+    // a timeout elsewhere in this launch already failed the scan: do nothing
+    if (abort_flag) return;
+
+    for (int i = tid; i < N * 32; i += blockDim.x) {
+        const float2 v = tw[i >> 5];
+        twr[i] = make_float2(v.x * TC_F_SCALE, v.y * TC_F_SCALE);
+    }
+    for (int i = tid; i <= 2 * Ka; i += blockDim.x) tinf[i] = tinfo[i];
     if (warp == 0) {
         tc::tmem_alloc(&tmem_base, 256);
         tc::tmem_relinquish();
     }
     if (tid == 0) {
-        for (int s = 0; s < TC_STAGES; ++s) {
-            tc::mbar_init(&full_bar[s], 128);
-            tc::mbar_init(&empty_bar[s], 1);
-        }
+        tc::mbar_init(&full_bar, 256);
+        tc::mbar_init(&empty_bar, 1);
         tc::mbar_init(&done_bar, 1);
-        abort_flag = 0;
         tc::fence_barrier_init();
     }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = tmem_base;
-    const uint32_t sbase = tc::smem_u32(stages);
+    const uint32_t fb = tc::smem_u32(fbuf);
+    const uint32_t ab = tc::smem_u32(abuf);
 
-    if (warp == 4) {
+    if (warp == 8) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
             const uint32_t idesc = tc::idesc_f16_f32(128, TC_ROT);
-            for (int q = 0; q < n_chunks; ++q) {
-                const int s = q % TC_STAGES;
-                if (*(volatile int*)&abort_flag ||
-                    !tc::mbar_wait(&full_bar[s], (uint32_t)((q / TC_STAGES) & 1), TC_WAIT_NS)) {
+            const uint32_t d_re = tmem, d_im = tmem + TC_ROT;
+            for (int k = 0; k < Ka; ++k) {
+                if (*(volatile int*)&abort_flag) break;
+                if (!tc::mbar_wait(&full_bar, (uint32_t)(k & 1), TC_WAIT_NS)) {
                     atomicOr(err, 1);
                     abort_flag = 1;
                     break;
                 }
                 tc::fence_after_sync();
-                const uint32_t st = sbase + s * TC_STAGE_BYTES;
-                const uint64_t cre_h = tc::smem_desc(st + 0 * TC_TILE, TC_LBO, TC_SBO);
-                const uint64_t cre_l = tc::smem_desc(st + 1 * TC_TILE, TC_LBO, TC_SBO);
-                const uint64_t cim_h = tc::smem_desc(st + 2 * TC_TILE, TC_LBO, TC_SBO);
-                const uint64_t cim_l = tc::smem_desc(st + 3 * TC_TILE, TC_LBO, TC_SBO);
-                const uint64_t f_h = tc::smem_desc(st + 4 * TC_TILE, TC_LBO, TC_SBO);
-                const uint64_t f_l = tc::smem_desc(st + 5 * TC_TILE, TC_LBO, TC_SBO);
-                const uint32_t acc = q > 0 ? 1u : 0u;
-                tc::mma_f16(tmem, cre_h, f_h, idesc, acc);
-                tc::mma_f16(tmem, cre_h, f_l, idesc, 1u);
-                tc::mma_f16(tmem, cre_l, f_h, idesc, 1u);
-                tc::mma_f16(tmem + TC_ROT, cim_h, f_h, idesc, acc);
-                tc::mma_f16(tmem + TC_ROT, cim_h, f_l, idesc, 1u);
-                tc::mma_f16(tmem + TC_ROT, cim_l, f_h, idesc, 1u);
-                tc::mma_commit(&empty_bar[s]);
+                for (int c = 0; c < NC; ++c) {
+                    const uint32_t ao = (uint32_t)(NC - 1 - c) * TC_SBO;
+                    const uint64_t cre_h = tc::smem_desc(ab + 0 * RG * 256 + ao, TC_LBO, TC_SBO);
+                    const uint64_t cre_l = tc::smem_desc(ab + 1 * RG * 256 + ao, TC_LBO, TC_SBO);
+                    const uint64_t cim_h = tc::smem_desc(ab + 2 * RG * 256 + ao, TC_LBO, TC_SBO);
+                    const uint64_t cim_l = tc::smem_desc(ab + 3 * RG * 256 + ao, TC_LBO, TC_SBO);
+                    const uint64_t f_h = tc::smem_desc(fb + c * TC_FCHUNK, TC_LBO, TC_SBO);
+                    const uint64_t f_l = tc::smem_desc(fb + c * TC_FCHUNK + TC_FTILE, TC_LBO, TC_SBO);
+                    const uint32_t acc = (k == 0 && c == 0) ? 0u : 1u;
+                    tc::mma_f16(d_re, cre_h, f_h, idesc, acc);
+                    tc::mma_f16(d_re, cre_h, f_l, idesc, 1u);
+                    tc::mma_f16(d_re, cre_l, f_h, idesc, 1u);
+                    tc::mma_f16(d_im, cim_h, f_h, idesc, acc);
+                    tc::mma_f16(d_im, cim_h, f_l, idesc, 1u);
+                    tc::mma_f16(d_im, cim_l, f_h, idesc, 1u);
+                }
+                tc::mma_commit(&empty_bar);
             }
+            // arrives when every MMA issued above has completed
             tc::mma_commit(&done_bar);
         }
         __syncwarp();
     } else {
-        // ---------------- producers: thread r = rotation of the group ----------------
-        const int r = tid;
-        const int rot = g * TC_ROT + r;
-        const bool live = rot < n_rot;
-        const uint32_t* ent_r = ent + (size_t)(live ? rot : 0) * n_ent;
-        const int32_t* offs_r = offs + (size_t)(live ? rot : 0) * (K * N + 1);
-        const int x = r;  // output row of the circulant tiles this thread expands
-        for (int q = 0; q < n_chunks; ++q) {
-            const int t = q / (W / 8);
-            const int n0 = (q - t * (W / 8)) * 8;
-            if (n0 == 0) {
-                // receptor circulant samples of term t, scaled and split
-                asm volatile("bar.sync 1, 128;" ::: "memory");
-                for (int d = r; d < N; d += 128) {
-                    const float2 c = circ[((size_t)t * NH + p) * N + d];
-                    const float cr = c.x * c_scale, ci = c.y * c_scale;
-                    TcPair pr;
-                    split_h2(cr, -ci, pr.re_h, pr.re_l);
-                    split_h2(ci, cr, pr.im_h, pr.im_l);
-                    pairs[d] = pr;
-                }
-                asm volatile("bar.sync 1, 128;" ::: "memory");
-            }
-            // ligand sums of 8 window bins for this thread's rotation
-            float2 f[8];
-            if (live) {
-                const int32_t* ob = offs_r + t * N;
-                int xb = x0 + n0;
-                int b = xb < N ? ob[xb] : 0;
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const int xi = xb + i;
-                    float2 acc = make_float2(0.f, 0.f);
-                    if (xi < N) {
-                        const int e = ob[xi + 1];
-                        for (int j = b; j < e; ++j) {
-                            const uint32_t u = __ldg(ent_r + j);
-                            const unsigned ph = (ky * ((u >> 8) & 255u) + kz * (u & 255u)) % (unsigned)N;
-                            const float2 z = tws[ph];
-                            acc.x += z.x;
-                            acc.y += z.y;
-                        }
-                        b = e;
-                    }
-                    f[i] = acc;
-                }
-            } else {
-#pragma unroll
-                for (int i = 0; i < 8; ++i) f[i] = make_float2(0.f, 0.f);
-            }
-            const int s = q % TC_STAGES;
-            // after a timeout anywhere, keep iterating (the named barriers
-            // above need every producer) but stop handing stages over
-            if (*(volatile int*)&abort_flag) continue;
-            if (!tc::mbar_wait(&empty_bar[s], (uint32_t)(((q / TC_STAGES) & 1) ^ 1), TC_WAIT_NS)) {
+        // ---------------- producers: thread (r, half) ----------------
+        const int r = tid & 127;
+        const int half = tid >> 7;
+        const uint32_t* ent_g = ent_t + (size_t)g * n_pad * TC_ROT + r;
+        const uint32_t twl = tc::smem_u32(twr) + (uint32_t)lane * 8u;  // this lane's copy of the phase table
+        const uint32_t stg = fb + (uint32_t)r * 8u;                     // staging row x' at stg + 1024 x'
+        const uint32_t sd = tc::smem_u32(side) + (uint32_t)r * 8u;
+        const uint32_t r0 = tc::kmajor_offset((uint32_t)r, 0, TC_LBO, TC_SBO);
+        const uint32_t r1 = tc::kmajor_offset((uint32_t)r, 8, TC_LBO, TC_SBO);
+        for (int k = 0; k < Ka; ++k) {
+            // the tensor core has read the previous term's tiles
+            if (k >= 1 && !*(volatile int*)&abort_flag &&
+                !tc::mbar_wait(&empty_bar, (uint32_t)((k - 1) & 1), TC_WAIT_NS)) {
                 atomicOr(err, 2);
                 abort_flag = 1;
-                continue;
             }
-            const uint32_t st = sbase + s * TC_STAGE_BYTES;
-            // F tile row r: k = 2i + {re, im}
-            {
-                __half2 hi[8], lo[8];
-#pragma unroll
-                for (int i = 0; i < 8; ++i) split_h2(f[i].x * TC_F_SCALE, f[i].y * TC_F_SCALE, hi[i], lo[i]);
-                const uint32_t o0 = tc::kmajor_offset(r, 0, TC_LBO, TC_SBO);
-                const uint32_t o1 = tc::kmajor_offset(r, 8, TC_LBO, TC_SBO);
-                st_shared_v4(st + 4 * TC_TILE + o0, h2u(hi[0]), h2u(hi[1]), h2u(hi[2]), h2u(hi[3]));
-                st_shared_v4(st + 4 * TC_TILE + o1, h2u(hi[4]), h2u(hi[5]), h2u(hi[6]), h2u(hi[7]));
-                st_shared_v4(st + 5 * TC_TILE + o0, h2u(lo[0]), h2u(lo[1]), h2u(lo[2]), h2u(lo[3]));
-                st_shared_v4(st + 5 * TC_TILE + o1, h2u(lo[4]), h2u(lo[5]), h2u(lo[6]), h2u(lo[7]));
+            const int t = tinf[Ka + 1 + k];
+            // receptor circulant samples of term t, scaled and split
+            if (tid < N) {
+                const float2 c = circ[((size_t)t * NH + p) * N + tid];
+                const float cr = c.x * c_scale, ci = c.y * c_scale;
+                TcPair v;
+                split_h2(cr, -ci, v.re_h, v.re_l);
+                split_h2(ci, cr, v.im_h, v.im_l);
+                pr[tid] = v;
             }
-            // circulant tile row x: k = 2i + {re, im} -> c((x0 + n0 + i - x) mod N)
-            {
+            // zero the staging rows (W x 128 float2, the F tile bytes)
+            for (uint32_t off = (uint32_t)tid * 16u; off < (uint32_t)W * 1024u; off += 256u * 16u)
+                st_shared_v4(fb + off, 0u, 0u, 0u, 0u);
+            asm volatile("bar.sync 1, 256;" ::: "memory");
+            // extended circulant tile E: row e, k = 2i + {re, im} -> c((x0 + W - 8 + i - e) mod N)
+            for (int e = tid; e < 8 * RG; e += 256) {
+                int d0 = (x0 + W - 8 - e) % N;
+                if (d0 < 0) d0 += N;
                 TcPair v[8];
 #pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    if (x < N) {
-                        int d = (x0 + n0 + i - x) % N;
-                        if (d < 0) d += N;
-                        v[i] = pairs[d];
-                    } else {
-                        const __half2 z = __floats2half2_rn(0.f, 0.f);
-                        v[i] = TcPair{z, z, z, z};
-                    }
+                for (int i2 = 0; i2 < 8; ++i2) {
+                    const int d = d0 + i2;
+                    v[i2] = pr[d < N ? d : d - N];
                 }
-                const uint32_t o0 = tc::kmajor_offset(x, 0, TC_LBO, TC_SBO);
-                const uint32_t o1 = tc::kmajor_offset(x, 8, TC_LBO, TC_SBO);
-                st_shared_v4(st + 0 * TC_TILE + o0, h2u(v[0].re_h), h2u(v[1].re_h), h2u(v[2].re_h), h2u(v[3].re_h));
-                st_shared_v4(st + 0 * TC_TILE + o1, h2u(v[4].re_h), h2u(v[5].re_h), h2u(v[6].re_h), h2u(v[7].re_h));
-                st_shared_v4(st + 1 * TC_TILE + o0, h2u(v[0].re_l), h2u(v[1].re_l), h2u(v[2].re_l), h2u(v[3].re_l));
-                st_shared_v4(st + 1 * TC_TILE + o1, h2u(v[4].re_l), h2u(v[5].re_l), h2u(v[6].re_l), h2u(v[7].re_l));
-                st_shared_v4(st + 2 * TC_TILE + o0, h2u(v[0].im_h), h2u(v[1].im_h), h2u(v[2].im_h), h2u(v[3].im_h));
-                st_shared_v4(st + 2 * TC_TILE + o1, h2u(v[4].im_h), h2u(v[5].im_h), h2u(v[6].im_h), h2u(v[7].im_h));
-                st_shared_v4(st + 3 * TC_TILE + o0, h2u(v[0].im_l), h2u(v[1].im_l), h2u(v[2].im_l), h2u(v[3].im_l));
-                st_shared_v4(st + 3 * TC_TILE + o1, h2u(v[4].im_l), h2u(v[5].im_l), h2u(v[6].im_l), h2u(v[7].im_l));
+                const uint32_t o0 = tc::kmajor_offset((uint32_t)e, 0, TC_LBO, TC_SBO);
+                const uint32_t o1 = tc::kmajor_offset((uint32_t)e, 8, TC_LBO, TC_SBO);
+                const uint32_t pre = ab, prl = ab + RG * 256, pie = ab + 2 * RG * 256, pil = ab + 3 * RG * 256;
+                st_shared_v4(pre + o0, h2u(v[0].re_h), h2u(v[1].re_h), h2u(v[2].re_h), h2u(v[3].re_h));
+                st_shared_v4(pre + o1, h2u(v[4].re_h), h2u(v[5].re_h), h2u(v[6].re_h), h2u(v[7].re_h));
+                st_shared_v4(prl + o0, h2u(v[0].re_l), h2u(v[1].re_l), h2u(v[2].re_l), h2u(v[3].re_l));
+                st_shared_v4(prl + o1, h2u(v[4].re_l), h2u(v[5].re_l), h2u(v[6].re_l), h2u(v[7].re_l));
+                st_shared_v4(pie + o0, h2u(v[0].im_h), h2u(v[1].im_h), h2u(v[2].im_h), h2u(v[3].im_h));
+                st_shared_v4(pie + o1, h2u(v[4].im_h), h2u(v[5].im_h), h2u(v[6].im_h), h2u(v[7].im_h));
+                st_shared_v4(pil + o0, h2u(v[0].im_l), h2u(v[1].im_l), h2u(v[2].im_l), h2u(v[3].im_l));
+                st_shared_v4(pil + o1, h2u(v[4].im_l), h2u(v[5].im_l), h2u(v[6].im_l), h2u(v[7].im_l));
+            }
+            // this thread's half of the term's rows, in blocks of 8
+            const int jt0 = tinf[k], n8 = (tinf[k + 1] - jt0) >> 3;
+            const int na = (n8 + 1) >> 1;
+            const int b0 = half ? na : 0, nb8 = half ? n8 - na : na;
+            const uint32_t* ep = ent_g + (size_t)(jt0 + 8 * b0) * TC_ROT;
+            // the second half's first bin goes to the side slot
+            const unsigned first = half && nb8 > 0 ? (__ldg(ep) >> 16) : 0xfffffffeu;
+            unsigned cur = 0xffffffffu;
+            float2 acc = make_float2(0.f, 0.f);
+            uint32_t u[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) u[q] = nb8 > 0 ? __ldg(ep + q * TC_ROT) : 0xffffffffu;
+            for (int blk = 0; blk < nb8; ++blk) {
+                uint32_t un[8];
+                const bool more = blk + 1 < nb8;
+                const uint32_t* en = ep + (size_t)(blk + 1) * 8 * TC_ROT;
+#pragma unroll
+                for (int q = 0; q < 8; ++q) un[q] = more ? __ldg(en + q * TC_ROT) : 0xffffffffu;
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const uint32_t e = u[q];
+                    // x relative to the window start; padding 0xffffffff gives
+                    // 0xffff, outside every window
+                    const unsigned xr = e >> 16;
+                    const unsigned ph = (ky * ((e >> 8) & 255u) + kz * (e & 255u)) % (unsigned)N;
+                    const float2 z = ld_shared_f2_const(twl + ph * 256u);
+                    const bool nb = xr != cur;
+                    acc.x = nb ? z.x : acc.x + z.x;
+                    acc.y = nb ? z.y : acc.y + z.y;
+                    cur = xr;
+                    const uint32_t dst = xr == first ? sd : stg + xr * 1024u;
+                    if (xr < (unsigned)W) st_shared_f2(dst, acc.x, acc.y);
+                }
+#pragma unroll
+                for (int q = 0; q < 8; ++q) u[q] = un[q];
+            }
+            asm volatile("bar.sync 1, 256;" ::: "memory");
+            // the second half's first bin: add its partial sum
+            if (half && first < (unsigned)W) {
+                const float2 a = ld_shared_f2(stg + first * 1024u), b = ld_shared_f2(sd);
+                st_shared_f2(stg + first * 1024u, a.x + b.x, a.y + b.y);
+            }
+            asm volatile("bar.sync 1, 256;" ::: "memory");
+            // staging rows -> F tiles (hi, lo): thread half h converts chunks
+            // c = 2 s + h; chunk c's staging rows and tiles occupy the same
+            // bytes, so every thread reads its chunk before any thread writes
+            for (int s2 = 0; 2 * s2 < NC; ++s2) {
+                const int c = 2 * s2 + half;
+                float2 v[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) v[i] = c < NC ? ld_shared_f2(stg + (uint32_t)(8 * c + i) * 1024u)
+                                                          : make_float2(0.f, 0.f);
+                asm volatile("bar.sync 1, 256;" ::: "memory");
+                if (c < NC) {
+                    uint32_t hi[8], lo[8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        __half2 a, b;
+                        split_h2(v[i].x, v[i].y, a, b);
+                        hi[i] = h2u(a);
+                        lo[i] = h2u(b);
+                    }
+                    const uint32_t fc = fb + (uint32_t)c * TC_FCHUNK;
+                    st_shared_v4(fc + r0, hi[0], hi[1], hi[2], hi[3]);
+                    st_shared_v4(fc + r1, hi[4], hi[5], hi[6], hi[7]);
+                    st_shared_v4(fc + TC_FTILE + r0, lo[0], lo[1], lo[2], lo[3]);
+                    st_shared_v4(fc + TC_FTILE + r1, lo[4], lo[5], lo[6], lo[7]);
+                }
             }
             tc::fence_proxy_async_smem();
-            tc::mbar_arrive(&full_bar[s]);
+            tc::mbar_arrive(&full_bar);
         }
-        // ---------------- epilogue: TMEM -> g2[rot][p][x] ----------------
-        if (!tc::mbar_wait(&done_bar, 0, TC_WAIT_NS)) atomicOr(err, 4);
+        // ---------------- epilogue: TMEM -> g2[rot][x][PP] (the layout the plane stage reads) ----------------
+        if (!*(volatile int*)&abort_flag && !tc::mbar_wait(&done_bar, 0, TC_WAIT_NS)) {
+            atomicOr(err, 4);
+            abort_flag = 1;
+        }
         tc::fence_after_sync();
         const float inv = 1.0f / (c_scale * TC_F_SCALE);
-        const int xo = 32 * warp + lane;  // TMEM lane = output row x
+        const int xo = 32 * (warp & 3) + lane;  // TMEM lane = output row x
+        const uint32_t trow = (uint32_t)(32 * (warp & 3)) << 16;
 #pragma unroll 1
-        for (int cb = 0; cb < TC_ROT / 32; ++cb) {
+        for (int cb = 0; cb < 2; ++cb) {
+            const int c0 = half * 64 + cb * 32;  // this warp's rotations [c0, c0 + 32)
             uint32_t dre[32], dim[32];
-            tc::tmem_ld_32x32b_x32(tmem + ((uint32_t)(32 * warp) << 16) + cb * 32, dre);
-            tc::tmem_ld_32x32b_x32(tmem + ((uint32_t)(32 * warp) << 16) + TC_ROT + cb * 32, dim);
+            tc::tmem_ld_32x32b_x32(tmem + trow + c0, dre);
+            tc::tmem_ld_32x32b_x32(tmem + trow + TC_ROT + c0, dim);
             tc::tmem_wait_ld();
             if (xo < N) {
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
-                    const int rr = g * TC_ROT + cb * 32 + j;
+                    const int rr = g * TC_ROT + c0 + j;
                     if (rr < n_rot)
-                        g2[((size_t)rr * NH + p) * N + xo] =
+                        g2[((size_t)rr * N + xo) * PP + p] =
                             make_float2(__uint_as_float(dre[j]) * inv, __uint_as_float(dim[j]) * inv);
                 }
             }
         }
     }
+    // the MMA issuer's done barrier covers every MMA before TMEM is released
+    if (warp == 8 && lane == 0 && !tc::mbar_wait(&done_bar, 0, TC_WAIT_NS)) atomicOr(err, 16);
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, 256);

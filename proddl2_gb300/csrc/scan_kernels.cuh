@@ -123,7 +123,8 @@ __global__ void __launch_bounds__(256) ligand_prep_kernel(
     const double* __restrict__ rot, const double* __restrict__ lig_xyz, const int32_t* __restrict__ lig_term,
     int n_ent, int K, Geo geo, uint32_t* __restrict__ ent_out, int32_t* __restrict__ offs_out,
     int32_t* __restrict__ status, const float* __restrict__ w_in, float* __restrict__ w_out,
-    int32_t* __restrict__ idx_out) {
+    int32_t* __restrict__ idx_out, uint32_t* __restrict__ ent_t, const int32_t* __restrict__ tpad, int n_pad,
+    int x0) {
     extern __shared__ unsigned char smem_raw[];
     int32_t* cnt = reinterpret_cast<int32_t*>(smem_raw);          // [K*N + 1]
     uint32_t* keys = reinterpret_cast<uint32_t*>(cnt + K * N + 1);  // [n_ent]
@@ -199,6 +200,13 @@ __global__ void __launch_bounds__(256) ligand_prep_kernel(
             if (act) dst = cnt[bin] + rank;
             __syncwarp();
             if (act) ent[dst] = key;
+            // transposed copy for the tensor pencil stage, [q / 128][row][q % 128]
+            // with each term's rows padded to a multiple of 16; the term is
+            // implied by the row and x is stored relative to the window start
+            // x0 (mod 256: cells outside the window stay outside it)
+            if (act && ent_t)
+                ent_t[((size_t)(q >> 7) * n_pad + dst + __ldg(tpad + (key >> 24))) * 128 + (q & 127)] =
+                    ((((key >> 16) - (uint32_t)x0) & 255u) << 16) | (key & 0xffffu);
             if (act && w_out) {
                 w_out[(size_t)q * n_ent + dst] = w_in[i];
                 idx_out[(size_t)q * n_ent + dst] = i;
@@ -331,7 +339,7 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G, PencilTraits<N>::MINB) 
 // (FFTW c2r of FFTCorrelator::correlate + CorrelationProcessor::
 // selectIntoQueue, docking_fft.hpp:452-468.)
 // ---------------------------------------------------------------------------
-template <int N, bool PMAJOR, bool DBG>
+template <int N, bool DBG>
 __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     const float2* __restrict__ g2, const float2* __restrict__ tw, float* __restrict__ cand_v,
     int32_t* __restrict__ cand_i, float* __restrict__ dbg) {
@@ -363,10 +371,8 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     const int tid = threadIdx.x;
     const int w = tid >> 5, l = tid & 31;
     for (int i = tid; i < N; i += blockDim.x) tws[i] = tw[i];
-    // element (ky, kz) of plane x: [B][N][PP] (x-planes contiguous) or, after
-    // the tensor pencil stage, [B][N*H][N] (x fastest)
-    const float2* src = PMAJOR ? g2 + (size_t)q * N * H * N + x : g2 + ((size_t)q * N + x) * PP;
-    constexpr int ES = PMAJOR ? N : 1;
+    // element (ky, kz) of plane x: [B][N][PP], x-planes contiguous
+    const float2* src = g2 + ((size_t)q * N + x) * PP;
     __syncthreads();
 
     // columns: inverse DFT along ky
@@ -381,10 +387,10 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
             float2 a = make_float2(0.f, 0.f);
             if (valid) {
                 if (s == 0) {
-                    const float2 d = src[(size_t)(ky * H) * ES], ny = src[(size_t)(ky * H + NS) * ES];
+                    const float2 d = src[(size_t)(ky * H)], ny = src[(size_t)(ky * H + NS)];
                     a = make_float2(d.x - ny.y, d.y + ny.x);
                 } else {
-                    a = src[(size_t)(ky * H + s) * ES];
+                    a = src[(size_t)(ky * H + s)];
                 }
             }
             v[r] = a;

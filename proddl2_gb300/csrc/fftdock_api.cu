@@ -780,9 +780,12 @@ int fftdock_set_ligand(fftdock_ctx* ctx, int32_t n, const double* xyz, const int
         if (W / 8 <= fftdock::kTcMaxChunks && ka <= fftdock::kTcMaxTerms) {
             std::vector<int32_t> info(starts);
             info.insert(info.end(), ids.begin(), ids.end());
-            CK(dalloc(&ctx->ent_t, (size_t)ctx->G * prun));
+            // 16 spare rows of 128 at the end: the tensor stage's loads run up
+            // to 16 rows past a range
+            const size_t n_t = (size_t)ctx->G * prun + 16 * fftdock::kTcRot;
+            CK(dalloc(&ctx->ent_t, n_t));
             // the padding rows are never written: 0xffffffff marks them
-            CK(cudaMemset(ctx->ent_t, 0xff, (size_t)ctx->G * prun * sizeof(uint32_t)));
+            CK(cudaMemset(ctx->ent_t, 0xff, n_t * sizeof(uint32_t)));
             CK(dalloc(&ctx->tinfo, info.size()));
             CK(dalloc(&ctx->tpad, tpad.size()));
             CK(cudaMemcpy(ctx->tinfo, info.data(), info.size() * sizeof(int32_t), cudaMemcpyHostToDevice));

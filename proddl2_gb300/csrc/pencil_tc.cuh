@@ -20,8 +20,9 @@
 // so one extended tile E of 120 + W rows per term serves every chunk: chunk
 // c's descriptor starts (W/8 - 1 - c) 8-row groups into E.  F comes from the
 // ligand entries of the term, which ligand prep writes transposed per group
-// of 128 rotations ([entry][rotation], sorted by (term, x) per rotation, each
-// term's range padded to a multiple of 16 with 0xffffffff, x relative to x0).
+// of 128 rotations ([entry / 4][rotation][entry % 4], sorted by (term, x) per
+// rotation, each term's range padded to a multiple of 16 with 0xffffffff, x
+// relative to x0).
 // A term's entries occupy the same index range in every rotation; two threads
 // per rotation walk the two halves of the range with coalesced loads.  Each
 // keeps the running sum of its current x bin and stores it after every entry
@@ -105,6 +106,64 @@ __host__ __device__ inline size_t tc_smem_bytes(int N, int n_chunks, int n_terms
                (size_t)N * sizeof(TcPair) + (size_t)TC_ROT * 8 + (size_t)(2 * n_terms + 1) * 4;
     b = (b + 15) & ~(size_t)15;
     return b < 76 * 1024 ? 76 * 1024 : b;
+}
+
+// One entry e of a rotation's sorted walk: add its phase to the running sum
+// of its x bin (restarted when x changes) and store the sum into the bin's
+// staging row, or, for SIDE and the walk's first bin, into the side slot.
+template <bool SIDE, int N>
+__device__ __forceinline__ void tc_entry(uint32_t e, unsigned ky, unsigned kz, uint32_t twl, uint32_t stg,
+                                         uint32_t sd, unsigned first, unsigned W, unsigned& cur, float2& acc) {
+    // x relative to the window start; padding 0xffffffff gives 0xffff, outside every window
+    const unsigned xr = e >> 16;
+    const unsigned ph = (ky * ((e >> 8) & 255u) + kz * (e & 255u)) % (unsigned)N;
+    const float2 z = ld_shared_f2_const(twl + ph * 256u);
+    const float keep = xr != cur ? 0.f : 1.f;
+    acc.x = fmaf(acc.x, keep, z.x);
+    acc.y = fmaf(acc.y, keep, z.y);
+    cur = xr;
+    uint32_t dst = stg + xr * 1024u;
+    if (SIDE) dst = xr == first ? sd : dst;
+    if (xr < W) st_shared_f2(dst, acc.x, acc.y);
+}
+
+// Walk nblk blocks of 8 rows from eq (this rotation's quads of rows: one
+// uint4 per 4 rows, consecutive quads 128 uint4 apart), blocks 0 and 1
+// already loaded into (a0, a1) and (b0, b1).  Two blocks are in flight while
+// one is summed; the loads may run up to 16 rows past the range, which the
+// entry buffer provides.
+template <bool SIDE, int N>
+__device__ __forceinline__ void tc_walk(const uint4* eq, int nblk, unsigned ky, unsigned kz, uint32_t twl,
+                                        uint32_t stg, uint32_t sd, unsigned first, unsigned W, uint4 a0, uint4 a1,
+                                        uint4 b0, uint4 b1) {
+    unsigned cur = 0xffffffffu;
+    float2 acc = make_float2(0.f, 0.f);
+    if (nblk <= 0) return;
+    uint4 c0, c1;
+    auto ld = [&](int blk, uint4& x0, uint4& x1) {
+        x0 = __ldg(eq + (size_t)(2 * blk) * TC_ROT);
+        x1 = __ldg(eq + (size_t)(2 * blk + 1) * TC_ROT);
+    };
+    auto sum = [&](const uint4& x0, const uint4& x1) {
+        tc_entry<SIDE, N>(x0.x, ky, kz, twl, stg, sd, first, W, cur, acc);
+        tc_entry<SIDE, N>(x0.y, ky, kz, twl, stg, sd, first, W, cur, acc);
+        tc_entry<SIDE, N>(x0.z, ky, kz, twl, stg, sd, first, W, cur, acc);
+        tc_entry<SIDE, N>(x0.w, ky, kz, twl, stg, sd, first, W, cur, acc);
+        tc_entry<SIDE, N>(x1.x, ky, kz, twl, stg, sd, first, W, cur, acc);
+        tc_entry<SIDE, N>(x1.y, ky, kz, twl, stg, sd, first, W, cur, acc);
+        tc_entry<SIDE, N>(x1.z, ky, kz, twl, stg, sd, first, W, cur, acc);
+        tc_entry<SIDE, N>(x1.w, ky, kz, twl, stg, sd, first, W, cur, acc);
+    };
+    for (int blk = 0; blk < nblk; blk += 3) {
+        ld(blk + 2, c0, c1);
+        sum(a0, a1);
+        if (blk + 1 >= nblk) break;
+        ld(blk + 3, a0, a1);
+        sum(b0, b1);
+        if (blk + 2 >= nblk) break;
+        ld(blk + 4, b0, b1);
+        sum(c0, c1);
+    }
 }
 
 // tinfo: [0, Ka] padded entry starts (multiples of 16) of the Ka non-empty
@@ -206,12 +265,29 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
         // ---------------- producers: thread (r, half) ----------------
         const int r = tid & 127;
         const int half = tid >> 7;
-        const uint32_t* ent_g = ent_t + (size_t)g * n_pad * TC_ROT + r;
+        // this rotation's quads of rows of the group ([g][row / 4][rotation][4])
+        const uint4* ent_g = reinterpret_cast<const uint4*>(ent_t) + (size_t)g * (n_pad / 4) * TC_ROT + r;
         const uint32_t twl = tc::smem_u32(twr) + (uint32_t)lane * 8u;  // this lane's copy of the phase table
         const uint32_t stg = fb + (uint32_t)r * 8u;                     // staging row x' at stg + 1024 x'
         const uint32_t sd = tc::smem_u32(side) + (uint32_t)r * 8u;
         const uint32_t r0 = tc::kmajor_offset((uint32_t)r, 0, TC_LBO, TC_SBO);
         const uint32_t r1 = tc::kmajor_offset((uint32_t)r, 8, TC_LBO, TC_SBO);
+        // the loads a term starts with (its circulant sample, this thread's
+        // first two entry blocks) are issued before the wait for the tensor
+        // core, so that they land while it reads the previous term's tiles
+        float2 cpre = make_float2(0.f, 0.f);
+        uint4 pa0, pa1, pb0, pb1;
+        auto preload = [&](int kk) {
+            const int jt = tinf[kk], m8 = (tinf[kk + 1] - jt) >> 3;
+            const int bb = half ? (m8 + 1) >> 1 : 0;
+            const uint4* q = ent_g + (size_t)((jt >> 2) + 2 * bb) * TC_ROT;
+            pa0 = __ldg(q);
+            pa1 = __ldg(q + TC_ROT);
+            pb0 = __ldg(q + 2 * TC_ROT);
+            pb1 = __ldg(q + 3 * TC_ROT);
+            if (tid < N) cpre = circ[((size_t)tinf[Ka + 1 + kk] * NH + p) * N + tid];
+        };
+        preload(0);
         for (int k = 0; k < Ka; ++k) {
             // the tensor core has read the previous term's tiles
             if (k >= 1 && !*(volatile int*)&abort_flag &&
@@ -219,10 +295,9 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
                 atomicOr(err, 2);
                 abort_flag = 1;
             }
-            const int t = tinf[Ka + 1 + k];
-            // receptor circulant samples of term t, scaled and split
+            // receptor circulant samples of the term, scaled and split
             if (tid < N) {
-                const float2 c = circ[((size_t)t * NH + p) * N + tid];
+                const float2 c = cpre;
                 const float cr = c.x * c_scale, ci = c.y * c_scale;
                 TcPair v;
                 split_h2(cr, -ci, v.re_h, v.re_l);
@@ -259,38 +334,13 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
             const int jt0 = tinf[k], n8 = (tinf[k + 1] - jt0) >> 3;
             const int na = (n8 + 1) >> 1;
             const int b0 = half ? na : 0, nb8 = half ? n8 - na : na;
-            const uint32_t* ep = ent_g + (size_t)(jt0 + 8 * b0) * TC_ROT;
+            const uint4* eq = ent_g + (size_t)((jt0 >> 2) + 2 * b0) * TC_ROT;
             // the second half's first bin goes to the side slot
-            const unsigned first = half && nb8 > 0 ? (__ldg(ep) >> 16) : 0xfffffffeu;
-            unsigned cur = 0xffffffffu;
-            float2 acc = make_float2(0.f, 0.f);
-            uint32_t u[8];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) u[q] = nb8 > 0 ? __ldg(ep + q * TC_ROT) : 0xffffffffu;
-            for (int blk = 0; blk < nb8; ++blk) {
-                uint32_t un[8];
-                const bool more = blk + 1 < nb8;
-                const uint32_t* en = ep + (size_t)(blk + 1) * 8 * TC_ROT;
-#pragma unroll
-                for (int q = 0; q < 8; ++q) un[q] = more ? __ldg(en + q * TC_ROT) : 0xffffffffu;
-#pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    const uint32_t e = u[q];
-                    // x relative to the window start; padding 0xffffffff gives
-                    // 0xffff, outside every window
-                    const unsigned xr = e >> 16;
-                    const unsigned ph = (ky * ((e >> 8) & 255u) + kz * (e & 255u)) % (unsigned)N;
-                    const float2 z = ld_shared_f2_const(twl + ph * 256u);
-                    const bool nb = xr != cur;
-                    acc.x = nb ? z.x : acc.x + z.x;
-                    acc.y = nb ? z.y : acc.y + z.y;
-                    cur = xr;
-                    const uint32_t dst = xr == first ? sd : stg + xr * 1024u;
-                    if (xr < (unsigned)W) st_shared_f2(dst, acc.x, acc.y);
-                }
-#pragma unroll
-                for (int q = 0; q < 8; ++q) u[q] = un[q];
-            }
+            const unsigned first = half && nb8 > 0 ? (pa0.x >> 16) : 0xfffffffeu;
+            if (half)
+                tc_walk<true, N>(eq, nb8, ky, kz, twl, stg, sd, first, (unsigned)W, pa0, pa1, pb0, pb1);
+            else
+                tc_walk<false, N>(eq, nb8, ky, kz, twl, stg, sd, first, (unsigned)W, pa0, pa1, pb0, pb1);
             asm volatile("bar.sync 1, 256;" ::: "memory");
             // the second half's first bin: add its partial sum
             if (half && first < (unsigned)W) {
@@ -326,6 +376,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
             }
             tc::fence_proxy_async_smem();
             tc::mbar_arrive(&full_bar);
+            if (k + 1 < Ka) preload(k + 1);
         }
         // ---------------- epilogue: TMEM -> g2[rot][x][PP] (the layout the plane stage reads) ----------------
         if (!*(volatile int*)&abort_flag && !tc::mbar_wait(&done_bar, 0, TC_WAIT_NS)) {

@@ -200,13 +200,16 @@ __global__ void __launch_bounds__(256) ligand_prep_kernel(
             if (act) dst = cnt[bin] + rank;
             __syncwarp();
             if (act) ent[dst] = key;
-            // transposed copy for the tensor pencil stage, [q / 128][row][q % 128]
-            // with each term's rows padded to a multiple of 16; the term is
-            // implied by the row and x is stored relative to the window start
-            // x0 (mod 256: cells outside the window stay outside it)
-            if (act && ent_t)
-                ent_t[((size_t)(q >> 7) * n_pad + dst + __ldg(tpad + (key >> 24))) * 128 + (q & 127)] =
+            // transposed copy for the tensor pencil stage,
+            // [q / 128][row / 4][q % 128][row % 4], with each term's rows
+            // padded to a multiple of 16; the term is implied by the row and
+            // x is stored relative to the window start x0 (mod 256: cells
+            // outside the window stay outside it)
+            if (act && ent_t) {
+                const size_t row = (size_t)(dst + __ldg(tpad + (key >> 24)));
+                ent_t[(((size_t)(q >> 7) * (n_pad >> 2) + (row >> 2)) * 128 + (q & 127)) * 4 + (row & 3)] =
                     ((((key >> 16) - (uint32_t)x0) & 255u) << 16) | (key & 0xffffu);
+            }
             if (act && w_out) {
                 w_out[(size_t)q * n_ent + dst] = w_in[i];
                 idx_out[(size_t)q * n_ent + dst] = i;

@@ -76,9 +76,8 @@ def workload_desc(w):
     terms = {"shape_ace": "shape + 18 desolvation types (18 folded terms)", "shape": "shape (1 term)",
              "lj_comp": "the reference's ljComp soft-core LJ (2 terms, weighted ligand entries)",
              "lj_avg": "the reference's ljAvg soft-core LJ (1 term)"}[w["term_set"]]
-    return ("%s: receptor %d / ligand %d atoms, %d^3 at %.1f A, %s, %d rotations, %d per batch, %d peaks/rotation"
-            % (w["name"], w["n_rec"], w["n_lig"], w["grid_n"], w["grid_step"], terms, w["n_rot"], w["rot_batch"],
-               w["peaks"]))
+    return ("%s: receptor %d / ligand %d atoms, %d^3 at %.1f A, %s, %d rotations, %d peaks/rotation"
+            % (w["name"], w["n_rec"], w["n_lig"], w["grid_n"], w["grid_step"], terms, w["n_rot"], w["peaks"]))
 
 
 class ClockSampler:
@@ -374,11 +373,18 @@ def run_ours(args):
         achieved = flops_per_launch / (avg_launch_ms / 1000.0) / 1e12
         peak, peak_kind = load_peaks("bf16_tflops")
         traffic = committed_traffic("pencil_tc_%s" % w["name"])
+        # the same launches against the reference schedule's bytes (the FFT
+        # form's roofline), for comparison between the two forms
+        rot_per_launch = n_rot * args.steps / max(launches, 1)
+        alg_gbs = reference_schedule_bytes(n, k_terms, batch) * rot_per_launch / (avg_launch_ms / 1000.0) / 1e9
+        peak_gbs, _ = load_peaks("hbm_gbs")
         roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                     "frac": achieved / peak, "traffic": traffic, "kernel": "pencil_tc",
                     "peak_source": peak_kind,
                     "flops_basis": "executed FP16 MMA work: N^2(N/2+1) pencils x K x W/8 chunks x 6 MMAs "
                                    "of 128x128x16 per 128-rotation group (W = %d)" % info["window_w"],
+                    "hbm_reference_schedule": {"achieved": alg_gbs, "peak": peak_gbs, "unit": "GB/s",
+                                               "frac": alg_gbs / peak_gbs},
                     "kernel_share": share}
     else:
         rot_per_launch = n_rot * args.steps / max(launches, 1)
@@ -412,7 +418,7 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32",
         "data": "synthetic (seeded globules, uniform quaternion rotations)",
-        "config": {"workload": workload_desc(w),
+        "config": {"workload": workload_desc(w), "rot_batch": batch,
                    "mode": ("exhaustive, translational clustering of a %d-cell queue per rotation (radius %g A)"
                             % (queue, args.cluster_radius)) if args.cluster else "exhaustive",
                    "parallelism": "replicas" if world == 1 else "rotation sets per rank (replicas)",

@@ -70,11 +70,16 @@ enum {
 };
 
 /* how the per-pencil x stage (x transforms and the spectrum product summed
- * over terms) runs.  AUTO = FFT.  TENSOR (grid edges <= 128) restates the
- * stage as a circular correlation along x computed with split-FP16 tcgen05
- * GEMMs (hi*hi + hi*lo + lo*hi, FP32 accumulate); on GB300 at 128^3 with 18
- * terms it measured 3.4x slower than FFT and its FP32 candidate values carry
- * up to ~2e-4 relative error against 1.6e-5 for FFT, so it is opt-in only. */
+ * over terms) runs.  FFT: FP32 x-FFTs on the CUDA cores.  TENSOR (grid
+ * edges <= 128, unweighted term sets) restates the stage as a circular
+ * correlation along x computed with split-FP16 tcgen05 GEMMs (hi*hi + hi*lo
+ * + lo*hi, FP32 accumulate) over ligand bins summed on the CUDA cores; the
+ * scan then takes rotations in groups of 128 (rot_batch is rounded up).  Its
+ * FP32 candidate values carry up to a few 1e-4 relative error (FFT: ~2e-5);
+ * reported scores are FP64 direct-space energies either way.  AUTO = TENSOR
+ * where it applies (grid edge <= 128, FP32 spectra, not the LJ sets), else
+ * FFT; a ligand whose window exceeds the tensor stage's shared memory runs
+ * the FFT form.  The no-allocation scan always runs the FFT form. */
 enum {
     FFTDOCK_PENCIL_AUTO = 0,
     FFTDOCK_PENCIL_FFT = 1,     /* FP32 x-FFTs on the CUDA cores */

@@ -474,9 +474,12 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
         return fail(ctx, FFTDOCK_EINVAL, "unknown pencil_mode");
     if (c.pencil_mode == FFTDOCK_PENCIL_TENSOR && !ctx->ops->has_tc)
         return fail(ctx, FFTDOCK_EUNSUPPORTED, "the tensor-core pencil stage covers grid edges up to 128");
-    // AUTO runs the FP32 FFT form: the tensor form measured slower and less
-    // accurate on the candidate values (see fftdock.h, FFTDOCK_PENCIL_TENSOR)
-    ctx->use_tc = c.pencil_mode == FFTDOCK_PENCIL_TENSOR;
+    // AUTO runs the tensor form where it applies (faster at 128^3 with 18
+    // terms); the FFT form keeps the more accurate FP32 candidate values
+    const bool lj_set = c.term_set == FFTDOCK_TERMS_LJ_COMP || c.term_set == FFTDOCK_TERMS_LJ_AVG;
+    ctx->use_tc = c.pencil_mode == FFTDOCK_PENCIL_TENSOR ||
+                  (c.pencil_mode == FFTDOCK_PENCIL_AUTO && ctx->ops->has_tc && !lj_set &&
+                   c.precision == FFTDOCK_PREC_FP32);
     if (!(c.shape_core_radius >= 0.0) || !(c.shape_surface_width >= 0.0))
         return fail(ctx, FFTDOCK_EINVAL, "shape radii must be >= 0");
     if (c.cluster_trans != 0 && c.cluster_trans != 1) return fail(ctx, FFTDOCK_EINVAL, "cluster_trans must be 0 or 1");

@@ -65,10 +65,6 @@ extern "C" int fftdock_scan_device_noalloc(fftdock_ctx* ctx, int32_t n_rot, cons
     if (in.args.lig_w32)
         return fftdock::ctx_fail(ctx, FFTDOCK_EUNSUPPORTED,
                                  "weighted ligand entries (ljComp) are not covered by the no-allocation scan");
-    if (in.args.use_tc)
-        return fftdock::ctx_fail(ctx, FFTDOCK_EUNSUPPORTED,
-                                 "the tensor pencil stage needs transposed entries per 128 rotations; the "
-                                 "no-allocation scan runs the FFT form (FFTDOCK_PENCIL_FFT)");
     if (in.args.wide.corr)
         return fftdock::ctx_fail(ctx, FFTDOCK_EUNSUPPORTED,
                                  "translational clustering needs a full correlation grid per rotation; the "
@@ -116,6 +112,9 @@ extern "C" int fftdock_scan_device_noalloc(fftdock_ctx* ctx, int32_t n_rot, cons
     a.pool_v = nullptr;
     a.pool_i = nullptr;
     a.ev = nullptr;
+    // the FFT form of the pencil stage: its work memory fits the static array
+    a.use_tc = 0;
+    a.ent_t = nullptr;
     cudaStream_t s = stream ? (cudaStream_t)stream : in.stream;
     for (int b0 = 0; b0 < n_rot; b0 += b) {
         a.n_rot = n_rot - b0 < b ? n_rot - b0 : b;

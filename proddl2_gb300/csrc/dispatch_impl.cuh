@@ -136,7 +136,7 @@ template <int N> struct SizeOpsImpl {
                 if ((e = set_smem((const void*)pencil_tc_kernel<N>, smt)) != cudaSuccess) return e;
                 dim3 gridt(N * H, (nb + TC_ROT - 1) / TC_ROT);
                 pencil_tc_kernel<N><<<gridt, TC_THREADS, smt, s>>>(a.circ, a.cscale, a.ent_t, a.tinfo,
-                                                                  a.n_tc_terms, a.tw32, a.g2, a.n_pad, nb, a.x0,
+                                                                  a.n_tc_terms, a.tw32, a.g2t, a.n_pad, nb, a.x0,
                                                                   a.W, a.err);
                 if ((e = cudaGetLastError()) != cudaSuccess) return e;
             }
@@ -151,6 +151,13 @@ template <int N> struct SizeOpsImpl {
             if (e != cudaSuccess) return e;
         }
         if (a.ev && (e = cudaEventRecord(a.ev[1], s)) != cudaSuccess) return e;
+        if constexpr (kHasTc) {
+            // the tensor stage's output into the plane stage's layout (timed with the plane stage)
+            if (tc) {
+                pencil_transpose_kernel<N><<<dim3((N * H + 31) / 32, nb), 256, 0, s>>>(a.g2t, a.g2);
+                if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            }
+        }
         // K3 (the queue + clustering path also writes every correlation grid)
         const size_t sm3 = plane_smem();
         dim3 grid3(N, nb);

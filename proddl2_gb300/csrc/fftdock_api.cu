@@ -71,6 +71,7 @@ struct fftdock_ctx {
     uint32_t* ent = nullptr;
     int32_t* offs = nullptr;
     float2* g2 = nullptr;
+    float2* g2t = nullptr;   // tensor stage output before the transpose
     float* cand_v = nullptr;
     int32_t* cand_i = nullptr;
 
@@ -189,6 +190,7 @@ BatchArgs batch_args(fftdock_ctx* ctx) {
     a.ent = ctx->ent;
     a.offs = ctx->offs;
     a.g2 = ctx->g2;
+    a.g2t = ctx->g2t;
     a.cand_v = ctx->cand_v;
     a.cand_i = ctx->cand_i;
     a.peak_stride = ctx->cfg.peaks_per_rot;
@@ -426,6 +428,7 @@ void fftdock_destroy(fftdock_ctx* ctx) {
     dfree(ctx->ent);
     dfree(ctx->offs);
     dfree(ctx->g2);
+    dfree(ctx->g2t);
     dfree(ctx->cand_v);
     dfree(ctx->cand_i);
     dfree(ctx->rot_all);
@@ -570,6 +573,7 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
     CK(dalloc(&ctx->rgrid, (size_t)ctx->K * ctx->V));
     CK(dalloc(&ctx->offs, (size_t)ctx->G * (ctx->K * N + 1)));
     CK(dalloc(&ctx->g2, (size_t)ctx->B * N * ctx->PP));
+    if (ctx->use_tc) CK(dalloc(&ctx->g2t, (size_t)ctx->B * N * ctx->H * N));
     CK(dalloc(&ctx->cand_v, (size_t)ctx->G * N * fftdock::kKC));
     CK(dalloc(&ctx->cand_i, (size_t)ctx->G * N * fftdock::kKC));
     CK(dalloc(&ctx->err_dev, 1));

@@ -171,12 +171,11 @@ __device__ __forceinline__ void tc_walk(const uint4* eq, int nblk, unsigned ky, 
 template <int N>
 __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
     const float2* __restrict__ circ, const int8_t* __restrict__ cscale, const uint32_t* __restrict__ ent_t,
-    const int32_t* __restrict__ tinfo, int Ka, const float2* __restrict__ tw, float2* __restrict__ g2, int n_pad,
+    const int32_t* __restrict__ tinfo, int Ka, const float2* __restrict__ tw, float2* __restrict__ g2t, int n_pad,
     int n_rot, int x0, int W, int* __restrict__ err) {
     static_assert(N <= 128, "the tensor pencil stage covers x in one 128-row tile");
     constexpr int H = N / 2 + 1;
     constexpr int NH = N * H;
-    constexpr int PP = pencil_pitch(N);
     const int NC = W >> 3;
     const int RG = tc_ext_groups(NC);
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -378,7 +377,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
             tc::mbar_arrive(&full_bar);
             if (k + 1 < Ka) preload(k + 1);
         }
-        // ---------------- epilogue: TMEM -> g2[rot][x][PP] (the layout the plane stage reads) ----------------
+        // ---------------- epilogue: TMEM -> g2t[rot][p][x] (coalesced along x) ----------------
         if (!*(volatile int*)&abort_flag && !tc::mbar_wait(&done_bar, 0, TC_WAIT_NS)) {
             atomicOr(err, 4);
             abort_flag = 1;
@@ -399,7 +398,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
                 for (int j = 0; j < 32; ++j) {
                     const int rr = g * TC_ROT + c0 + j;
                     if (rr < n_rot)
-                        g2[((size_t)rr * N + xo) * PP + p] =
+                        g2t[((size_t)rr * NH + p) * N + xo] =
                             make_float2(__uint_as_float(dre[j]) * inv, __uint_as_float(dim[j]) * inv);
                 }
             }
@@ -410,6 +409,27 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, 256);
+}
+
+// g2t [rot][p][x] -> g2 [rot][x][PP] (the plane stage's layout): a CTA moves
+// 32 pencils x N cells of one rotation through shared memory, reading 32 N
+// contiguous values and writing, per x, 32 contiguous pencils
+template <int N>
+__global__ void __launch_bounds__(256) pencil_transpose_kernel(const float2* __restrict__ src,
+                                                               float2* __restrict__ dst) {
+    constexpr int H = N / 2 + 1, NH = N * H, PP = pencil_pitch(N);
+    __shared__ float2 tile[32][N + 1];
+    const int p0 = blockIdx.x * 32;
+    const size_t q = blockIdx.y;
+    const int np = NH - p0 < 32 ? NH - p0 : 32;
+    const float2* s = src + (q * NH + p0) * N;
+    for (int i = threadIdx.x; i < np * N; i += blockDim.x) tile[i / N][i % N] = s[i];
+    __syncthreads();
+    float2* d = dst + q * N * PP + p0;
+    for (int i = threadIdx.x; i < 32 * N; i += blockDim.x) {
+        const int x = i >> 5, pr = i & 31;
+        if (pr < np) d[(size_t)x * PP + pr] = tile[pr][x];
+    }
 }
 
 // per-pencil power-of-two exponent so that the largest circulant component

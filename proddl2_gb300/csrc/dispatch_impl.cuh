@@ -116,7 +116,8 @@ template <int N> struct SizeOpsImpl {
         if (e != cudaSuccess) return e;
         ligand_prep_kernel<N><<<nb, 256, sm1, s>>>(a.rot, a.lig_xyz, a.lig_term, a.n_ent, a.K, geo, a.ent, a.offs,
                                                     a.status, a.lig_w32, a.lig_w32 ? a.ent_w : nullptr, a.ent_idx,
-                                                    a.use_tc ? a.ent_t : nullptr, a.tpad, a.n_pad, a.x0);
+                                                    a.use_tc ? a.ent_t : nullptr, a.tpad, a.n_pad, a.x0,
+                                                    a.W);
         return cudaGetLastError();
     }
 

@@ -223,6 +223,11 @@ int check_pipeline(fftdock_ctx* ctx) {
     return FFTDOCK_OK;
 }
 
+__global__ void fill_u32_kernel(uint32_t* p, uint32_t v, size_t n) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
 // n events from the profiling pool; returns the index of the first
 int take_events(fftdock_ctx* ctx, size_t n, size_t* first) {
     while (ctx->ev_pool.size() < ctx->ev_used + n) {
@@ -791,8 +796,11 @@ int fftdock_set_ligand(fftdock_ctx* ctx, int32_t n, const double* xyz, const int
             // to 16 rows past a range
             const size_t n_t = (size_t)ctx->G * prun + 16 * fftdock::kTcRot;
             CK(dalloc(&ctx->ent_t, n_t));
-            // the padding rows are never written: 0xffffffff marks them
-            CK(cudaMemset(ctx->ent_t, 0xff, n_t * sizeof(uint32_t)));
+            // the padding rows are never written: x' = W (the tensor stage's
+            // dummy staging row), y = z = 0 marks them
+            fill_u32_kernel<<<(unsigned)((n_t + 255) / 256), 256, 0, ctx->stream>>>(ctx->ent_t, (uint32_t)W << 16, n_t);
+            CK(cudaGetLastError());
+            CK(cudaStreamSynchronize(ctx->stream));
             CK(dalloc(&ctx->tinfo, info.size()));
             CK(dalloc(&ctx->tpad, tpad.size()));
             CK(cudaMemcpy(ctx->tinfo, info.data(), info.size() * sizeof(int32_t), cudaMemcpyHostToDevice));

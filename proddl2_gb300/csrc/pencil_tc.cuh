@@ -21,8 +21,8 @@
 // c's descriptor starts (W/8 - 1 - c) 8-row groups into E.  F comes from the
 // ligand entries of the term, which ligand prep writes transposed per group
 // of 128 rotations ([entry / 4][rotation][entry % 4], sorted by (term, x) per
-// rotation, each term's range padded to a multiple of 16 with 0xffffffff, x
-// relative to x0).
+// rotation, each term's range padded to a multiple of 16, x relative to x0;
+// padding and cells outside the window carry x' = W, a dummy staging row).
 // A term's entries occupy the same index range in every rotation; two threads
 // per rotation walk the two halves of the range with coalesced loads.  Each
 // keeps the running sum of its current x bin and stores it after every entry
@@ -102,7 +102,7 @@ __host__ __device__ constexpr int tc_ext_groups(int n_chunks) { return 15 + n_ch
 // float2, staged samples [N], side slots [128] float2, term table; at least
 // 76 KB so that no more than two CTAs (2 x 256 TMEM columns) share an SM
 __host__ __device__ inline size_t tc_smem_bytes(int N, int n_chunks, int n_terms) {
-    size_t b = (size_t)n_chunks * TC_FCHUNK + (size_t)4 * tc_ext_groups(n_chunks) * 256 + (size_t)N * 32 * 8 +
+    size_t b = (size_t)n_chunks * TC_FCHUNK + 1024 + (size_t)4 * tc_ext_groups(n_chunks) * 256 + (size_t)N * 32 * 8 +
                (size_t)N * sizeof(TcPair) + (size_t)TC_ROT * 8 + (size_t)(2 * n_terms + 1) * 4;
     b = (b + 15) & ~(size_t)15;
     return b < 76 * 1024 ? 76 * 1024 : b;
@@ -114,7 +114,8 @@ __host__ __device__ inline size_t tc_smem_bytes(int N, int n_chunks, int n_terms
 template <bool SIDE, int N>
 __device__ __forceinline__ void tc_entry(uint32_t e, unsigned ky, unsigned kz, uint32_t twl, uint32_t stg,
                                          uint32_t sd, unsigned first, unsigned W, unsigned& cur, float2& acc) {
-    // x relative to the window start; padding 0xffffffff gives 0xffff, outside every window
+    // x relative to the window start; padding and cells outside the window
+    // carry x' = W, a dummy staging row
     const unsigned xr = e >> 16;
     const unsigned ph = (ky * ((e >> 8) & 255u) + kz * (e & 255u)) % (unsigned)N;
     const float2 z = ld_shared_f2_const(twl + ph * 256u);
@@ -124,7 +125,7 @@ __device__ __forceinline__ void tc_entry(uint32_t e, unsigned ky, unsigned kz, u
     cur = xr;
     uint32_t dst = stg + xr * 1024u;
     if (SIDE) dst = xr == first ? sd : dst;
-    if (xr < W) st_shared_f2(dst, acc.x, acc.y);
+    st_shared_f2(dst, acc.x, acc.y);
 }
 
 // Walk nblk blocks of 8 rows from eq (this rotation's quads of rows: one
@@ -180,7 +181,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
     const int RG = tc_ext_groups(NC);
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* fbuf = smem_raw;                                            // [NC][hi | lo]
-    unsigned char* abuf = fbuf + NC * TC_FCHUNK;                               // [4][RG][256]
+    unsigned char* abuf = fbuf + NC * TC_FCHUNK + 1024;                        // [4][RG][256] after the dummy row
     float2* twr = reinterpret_cast<float2*>(abuf + 4 * RG * 256);              // [N][32]
     TcPair* pr = reinterpret_cast<TcPair*>(twr + N * 32);                      // [N]
     float2* side = reinterpret_cast<float2*>(pr + N);                          // [128]

@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(256) ligand_prep_kernel(
     int n_ent, int K, Geo geo, uint32_t* __restrict__ ent_out, int32_t* __restrict__ offs_out,
     int32_t* __restrict__ status, const float* __restrict__ w_in, float* __restrict__ w_out,
     int32_t* __restrict__ idx_out, uint32_t* __restrict__ ent_t, const int32_t* __restrict__ tpad, int n_pad,
-    int x0) {
+    int x0, int W) {
     extern __shared__ unsigned char smem_raw[];
     int32_t* cnt = reinterpret_cast<int32_t*>(smem_raw);          // [K*N + 1]
     uint32_t* keys = reinterpret_cast<uint32_t*>(cnt + K * N + 1);  // [n_ent]
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(256) ligand_prep_kernel(
             if (act && ent_t) {
                 const size_t row = (size_t)(dst + __ldg(tpad + (key >> 24)));
                 ent_t[(((size_t)(q >> 7) * (n_pad >> 2) + (row >> 2)) * 128 + (q & 127)) * 4 + (row & 3)] =
-                    ((((key >> 16) - (uint32_t)x0) & 255u) << 16) | (key & 0xffffu);
+                    (min(((key >> 16) - (uint32_t)x0) & 255u, (uint32_t)W) << 16) | (key & 0xffffu);
             }
             if (act && w_out) {
                 w_out[(size_t)q * n_ent + dst] = w_in[i];

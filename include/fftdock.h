@@ -77,9 +77,11 @@ enum {
  * scan then takes rotations in groups of 128 (rot_batch is rounded up).  Its
  * FP32 candidate values carry up to a few 1e-4 relative error (FFT: ~2e-5);
  * reported scores are FP64 direct-space energies either way.  AUTO = TENSOR
- * where it applies (grid edge <= 128, FP32 spectra, not the LJ sets), else
- * FFT; a ligand whose window exceeds the tensor stage's shared memory runs
- * the FFT form.  The no-allocation scan always runs the FFT form. */
+ * where it applies (grid edge <= 128, FP32 spectra, an unweighted term set
+ * with at least 4 terms: at 64^3 with the single shape term the FFT form is
+ * faster), else FFT; a ligand whose window exceeds the tensor stage's shared
+ * memory runs the FFT form.  The no-allocation scan always runs the FFT form;
+ * fftdock_scan_pairs follows the same rule per grid edge. */
 enum {
     FFTDOCK_PENCIL_AUTO = 0,
     FFTDOCK_PENCIL_FFT = 1,     /* FP32 x-FFTs on the CUDA cores */

@@ -223,11 +223,6 @@ int check_pipeline(fftdock_ctx* ctx) {
     return FFTDOCK_OK;
 }
 
-__global__ void fill_u32_kernel(uint32_t* p, uint32_t v, size_t n) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) p[i] = v;
-}
-
 // n events from the profiling pool; returns the index of the first
 int take_events(fftdock_ctx* ctx, size_t n, size_t* first) {
     while (ctx->ev_pool.size() < ctx->ev_used + n) {
@@ -330,6 +325,61 @@ int check_ready(fftdock_ctx* ctx) {
 }  // namespace
 
 namespace fftdock {
+
+namespace {
+__global__ void fill_u32_kernel(uint32_t* p, uint32_t v, size_t n) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+}  // namespace
+
+cudaError_t fill_padding(uint32_t* ent_t, int W, size_t n, cudaStream_t s) {
+    fill_u32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(ent_t, (uint32_t)W << 16, n);
+    return cudaGetLastError();
+}
+
+TcTables tc_tables(const double* xyz, const int32_t* term, int n, int K, int N, double h, double zero_h) {
+    TcTables t;
+    // window of x cells that holds the ligand under every rotation about the
+    // origin: |R p| <= max |p|, with a cell of margin on each side
+    double rmax = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double r2 = xyz[3 * i] * xyz[3 * i] + xyz[3 * i + 1] * xyz[3 * i + 1] + xyz[3 * i + 2] * xyz[3 * i + 2];
+        rmax = std::max(rmax, std::sqrt(r2));
+    }
+    rmax = rmax * (1.0 + 1e-9) + 1e-9;
+    long lo = (long)std::floor((-rmax - zero_h) / h) - 2;
+    long hi = (long)std::floor((rmax - zero_h) / h) + 0;
+    lo = std::max(lo, 0L);
+    hi = std::min(hi, (long)N - 1);
+    int W = (int)((hi - lo + 1 + 7) / 8 * 8);
+    if (W > N) W = N;
+    long x0 = lo;
+    if (x0 + W > N) x0 = N - W;
+    t.x0 = (int)x0;
+    t.W = W;
+    // rows of the transposed entries: each non-empty term's range padded to 16
+    std::vector<int32_t> cnt(K, 0);
+    for (int i = 0; i < n; ++i) ++cnt[term[i]];
+    std::vector<int32_t> starts, ids;
+    t.tpad.assign(K, 0);
+    int run = 0, prun = 0;
+    for (int k = 0; k < K; ++k) {
+        if (cnt[k] == 0) continue;
+        starts.push_back(prun);
+        ids.push_back(k);
+        t.tpad[k] = prun - run;
+        run += cnt[k];
+        prun += (cnt[k] + 15) / 16 * 16;
+    }
+    starts.push_back(prun);
+    t.ka = (int)ids.size();
+    t.n_pad = prun;
+    t.info = starts;
+    t.info.insert(t.info.end(), ids.begin(), ids.end());
+    t.ok = W / 8 <= kTcMaxChunks && t.ka <= kTcMaxTerms && t.ka >= 1;
+    return t;
+}
 
 // Inputs of a scan held by a ready context, for entry points that bring
 // their own work memory.
@@ -485,9 +535,10 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
     // AUTO runs the tensor form where it applies (faster at 128^3 with 18
     // terms); the FFT form keeps the more accurate FP32 candidate values
     const bool lj_set = c.term_set == FFTDOCK_TERMS_LJ_COMP || c.term_set == FFTDOCK_TERMS_LJ_AVG;
+    const int k_terms = c.term_set == FFTDOCK_TERMS_SHAPE_ACE ? c.n_types : 1;
     ctx->use_tc = c.pencil_mode == FFTDOCK_PENCIL_TENSOR ||
                   (c.pencil_mode == FFTDOCK_PENCIL_AUTO && ctx->ops->has_tc && !lj_set &&
-                   c.precision == FFTDOCK_PREC_FP32);
+                   c.precision == FFTDOCK_PREC_FP32 && k_terms >= fftdock::kTcMinTerms);
     if (!(c.shape_core_radius >= 0.0) || !(c.shape_surface_width >= 0.0))
         return fail(ctx, FFTDOCK_EINVAL, "shape radii must be >= 0");
     if (c.cluster_trans != 0 && c.cluster_trans != 1) return fail(ctx, FFTDOCK_EINVAL, "cluster_trans must be 0 or 1");
@@ -747,25 +798,9 @@ int fftdock_set_ligand(fftdock_ctx* ctx, int32_t n, const double* xyz, const int
     CK(dalloc(&ctx->ent, (size_t)ctx->G * n));
     CK(cudaMemcpy(ctx->lig_xyz, xyz, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->lig_term, term.data(), (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice));
-    // window of x cells that holds the ligand under every rotation about the
-    // origin: |R p| <= max |p|, with a cell of margin on each side
-    double rmax = 0.0;
-    for (int i = 0; i < n; ++i) {
-        const double r2 = xyz[3 * i] * xyz[3 * i] + xyz[3 * i + 1] * xyz[3 * i + 1] + xyz[3 * i + 2] * xyz[3 * i + 2];
-        rmax = std::max(rmax, std::sqrt(r2));
-    }
-    rmax = rmax * (1.0 + 1e-9) + 1e-9;
-    const int N = ctx->N;
-    long lo = (long)std::floor((-rmax - ctx->zero_h) / ctx->h) - 2;
-    long hi = (long)std::floor((rmax - ctx->zero_h) / ctx->h) + 0;
-    lo = std::max(lo, 0L);
-    hi = std::min(hi, (long)N - 1);
-    int W = (int)((hi - lo + 1 + 7) / 8 * 8);
-    if (W > N) W = N;
-    long x0 = lo;
-    if (x0 + W > N) x0 = N - W;
-    ctx->x0 = (int)x0;
-    ctx->W = W;
+    const fftdock::TcTables tt = fftdock::tc_tables(xyz, term.data(), n, ctx->K, ctx->N, ctx->h, ctx->zero_h);
+    ctx->x0 = tt.x0;
+    ctx->W = tt.W;
     ctx->n_ent = n;
     // tensor stage: entry ranges of the non-empty terms (the same in every
     // rotation: entries are sorted by term first)
@@ -773,42 +808,20 @@ int fftdock_set_ligand(fftdock_ctx* ctx, int32_t n, const double* xyz, const int
     dfree(ctx->ent_t);
     dfree(ctx->tinfo);
     dfree(ctx->tpad);
-    if (ctx->use_tc) {
-        std::vector<int32_t> cnt(ctx->K, 0);
-        for (int i = 0; i < n; ++i) ++cnt[term[i]];
-        // rows of the transposed entries: each term's range padded to 16
-        std::vector<int32_t> starts, ids, tpad(ctx->K, 0);
-        int run = 0, prun = 0;
-        for (int t = 0; t < ctx->K; ++t) {
-            if (cnt[t] == 0) continue;
-            starts.push_back(prun);
-            ids.push_back(t);
-            tpad[t] = prun - run;
-            run += cnt[t];
-            prun += (cnt[t] + 15) / 16 * 16;
-        }
-        starts.push_back(prun);
-        const int ka = (int)ids.size();
-        if (W / 8 <= fftdock::kTcMaxChunks && ka <= fftdock::kTcMaxTerms) {
-            std::vector<int32_t> info(starts);
-            info.insert(info.end(), ids.begin(), ids.end());
-            // 16 spare rows of 128 at the end: the tensor stage's loads run up
-            // to 16 rows past a range
-            const size_t n_t = (size_t)ctx->G * prun + 16 * fftdock::kTcRot;
-            CK(dalloc(&ctx->ent_t, n_t));
-            // the padding rows are never written: x' = W (the tensor stage's
-            // dummy staging row), y = z = 0 marks them
-            fill_u32_kernel<<<(unsigned)((n_t + 255) / 256), 256, 0, ctx->stream>>>(ctx->ent_t, (uint32_t)W << 16, n_t);
-            CK(cudaGetLastError());
-            CK(cudaStreamSynchronize(ctx->stream));
-            CK(dalloc(&ctx->tinfo, info.size()));
-            CK(dalloc(&ctx->tpad, tpad.size()));
-            CK(cudaMemcpy(ctx->tinfo, info.data(), info.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
-            CK(cudaMemcpy(ctx->tpad, tpad.data(), tpad.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
-            ctx->n_tc_terms = ka;
-            ctx->n_pad = prun;
-            ctx->tc_ready = true;
-        }
+    if (ctx->use_tc && tt.ok) {
+        // 16 spare rows of 128 at the end: the tensor stage's loads run up
+        // to 16 rows past a range
+        const size_t n_t = (size_t)ctx->G * tt.n_pad + 16 * fftdock::kTcRot;
+        CK(dalloc(&ctx->ent_t, n_t));
+        CK(fftdock::fill_padding(ctx->ent_t, tt.W, n_t, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        CK(dalloc(&ctx->tinfo, tt.info.size()));
+        CK(dalloc(&ctx->tpad, tt.tpad.size()));
+        CK(cudaMemcpy(ctx->tinfo, tt.info.data(), tt.info.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(ctx->tpad, tt.tpad.data(), tt.tpad.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+        ctx->n_tc_terms = tt.ka;
+        ctx->n_pad = tt.n_pad;
+        ctx->tc_ready = true;
     }
     ctx->have_lig = true;
     return FFTDOCK_OK;

@@ -156,6 +156,27 @@ struct BatchArgs {
     WideArgs wide;              // queue + clustering path (wide.corr != nullptr)
 };
 
+// The tensor pencil stage's per-ligand tables: the x window [x0, x0 + W)
+// that holds the ligand's cells under every rotation about the origin, and
+// the rows of the transposed entries (each non-empty term's range padded to
+// 16).  ok = the window and the term count fit the stage.
+struct TcTables {
+    int x0 = 0, W = 0;
+    int n_pad = 0;                 // padded rows per rotation
+    int ka = 0;                    // non-empty terms
+    std::vector<int32_t> info;     // [ka + 1] padded starts, then [ka] term ids
+    std::vector<int32_t> tpad;     // [K] padded start - start of each term
+    bool ok = false;
+};
+TcTables tc_tables(const double* xyz, const int32_t* term, int n, int K, int N, double h, double zero_h);
+// the padding rows of the transposed entries: x' = W (the tensor stage's
+// dummy staging row), y = z = 0
+cudaError_t fill_padding(uint32_t* ent_t, int W, size_t n, cudaStream_t s);
+// AUTO selection of the tensor form: grid edge <= 128 (has_tc), FP32
+// spectra, an unweighted term set with at least kTcMinTerms terms (at 64^3
+// with the single shape term the FFT form measured faster)
+constexpr int kTcMinTerms = 4;
+
 // queue + clustering stage of one batch, after the correlation grids of the
 // batch are in a.wide.corr; writes a.peaks / a.n_peaks
 cudaError_t wide_select_batch(const BatchArgs& a, int N, cudaStream_t s);

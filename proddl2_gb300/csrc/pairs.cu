@@ -7,7 +7,9 @@
 // buffers per (queue, grid size), and captures the whole workload -- per pair:
 // receptor grids, receptor transforms, ligand binning and the scan batches --
 // into one CUDA graph over several streams ("queues", pairs spread by
-// longest-processing-time first), launched once.  The autotuner picks the
+// longest-processing-time first), launched once.  Grid edges up to 128 run
+// the tensor form of the pencil stage under the same rule as the single-pair
+// contexts (AUTO: term sets of at least kTcMinTerms terms).  The autotuner picks the
 // rotations per launch for each grid size (timed probe scans of the pair's own
 // kernels) and the number of queues (timed probe graphs over a subset of the
 // pairs).  The FFT radix plan of each grid size is fixed at compile time.
@@ -67,6 +69,8 @@ struct SizeData {
     int batch = 64;
     int max_lig = 1;
     int max_rec = 1;
+    bool tc = false;      // tensor form of the pencil stage
+    int max_pad = 16;     // largest padded entry rows per rotation among its pairs
 };
 
 // work buffers of one queue for one grid size
@@ -84,7 +88,16 @@ struct Work {
     int32_t* cand_i = nullptr;
     int* err = nullptr;
     int* box = nullptr;
+    // tensor form
+    float2* circ = nullptr;
+    int8_t* cscale = nullptr;
+    uint32_t* ent_t = nullptr;
+    float2* g2t = nullptr;
     void release() {
+        dfree(circ);
+        dfree(cscale);
+        dfree(ent_t);
+        dfree(g2t);
         dfree(box);
         dfree(rgrid);
         if (spec) cudaFree(spec);
@@ -117,7 +130,14 @@ struct Staged {
     int* box = nullptr;         // [sum n_rec][6]
     std::vector<size_t> rec_off, lig_off, rot_off, bin_off;
     std::vector<fftdock::HostAtomBins> bins;
+    // tensor form: per pair its window and entry tables (concatenated on the device)
+    std::vector<fftdock::TcTables> tct;
+    std::vector<size_t> info_off, tpad_off;
+    int32_t* tinfo = nullptr;
+    int32_t* tpad = nullptr;
     void release() {
+        dfree(tinfo);
+        dfree(tpad);
         dfree(bin_start);
         dfree(bin_atoms);
         dfree(box);
@@ -137,6 +157,7 @@ struct Run {
     fftdock_config cfg{};
     int K = 1;
     bool ace = false;
+    bool tc = false;      // the tensor form where the grid edge allows it
     std::map<int, SizeData> sizes;
     std::vector<std::vector<Work>> work;  // [queue][slot]
     Staged st;
@@ -189,6 +210,14 @@ int alloc_work(Run& r, Work& w, const SizeData& sd, int B) {
     PCK(dalloc(&w.cand_i, (size_t)B * N * kKC));
     PCK(dalloc(&w.err, 1));
     PCK(cudaMemset(w.err, 0, sizeof(int)));
+    if (sd.tc) {
+        const size_t nh = (size_t)N * sd.H;
+        PCK(dalloc(&w.circ, (size_t)K * nh * N));
+        PCK(dalloc(&w.cscale, nh));
+        PCK(dalloc(&w.g2t, (size_t)B * nh * N));
+        // 16 spare rows of 128: the tensor stage's loads run up to 16 rows past a range
+        PCK(dalloc(&w.ent_t, (size_t)B * sd.max_pad + 16 * fftdock::kTcRot));
+    }
     return FFTDOCK_OK;
 }
 
@@ -232,10 +261,19 @@ cudaError_t enqueue_pair(Run& r, const fftdock_pair& p, int i, Work& w, const Si
     if (e != cudaSuccess) return e;
     const bool bf = c.precision == FFTDOCK_PREC_BF16_SPECTRA;
     const size_t elem = bf ? 4 : 8;
+    const bool tc = sd.tc && r.st.tct[i].ok;
+    const size_t nh = (size_t)N * sd.H;
     for (int t = 0; t < r.K; ++t) {
         e = sd.ops->receptor_fft(w.rgrid + (size_t)t * sd.V, w.cbuf, w.hbuf, sd.tw64,
                                  static_cast<unsigned char*>(w.spec) + (size_t)t * N * sd.PP * elem, bf ? 1 : 0,
-                                 sd.PP, nullptr, s);
+                                 sd.PP, tc ? w.circ + (size_t)t * nh * N : nullptr, s);
+        if (e != cudaSuccess) return e;
+    }
+    if (tc) {
+        if ((e = sd.ops->circ_scales(w.circ, r.K, w.cscale, s)) != cudaSuccess) return e;
+        const fftdock::TcTables& tt = r.st.tct[i];
+        // this pair's padding rows (x' = its window width) over the rows its batches use
+        e = fftdock::fill_padding(w.ent_t, tt.W, (size_t)B * tt.n_pad + 16 * fftdock::kTcRot, s);
         if (e != cudaSuccess) return e;
     }
     BatchArgs a{};
@@ -260,6 +298,20 @@ cudaError_t enqueue_pair(Run& r, const fftdock_pair& p, int i, Work& w, const Si
     a.k_out = std::min(c.peaks_per_rot, c.max_trans_inp);
     a.max_val = c.max_val_corr;
     a.err = w.err;
+    if (tc) {
+        const fftdock::TcTables& tt = r.st.tct[i];
+        a.use_tc = 1;
+        a.circ = w.circ;
+        a.cscale = w.cscale;
+        a.x0 = tt.x0;
+        a.W = tt.W;
+        a.ent_t = w.ent_t;
+        a.tinfo = r.st.tinfo + r.st.info_off[i];
+        a.tpad = r.st.tpad + r.st.tpad_off[i];
+        a.n_tc_terms = tt.ka;
+        a.n_pad = tt.n_pad;
+        a.g2t = w.g2t;
+    }
     const size_t ro = r.st.rot_off[i] + rot_lo;
     for (int b0 = 0; b0 < rot_n; b0 += B) {
         const int nb = std::min(B, rot_n - b0);
@@ -434,6 +486,27 @@ int stage(Run& r, int n_pairs, const fftdock_pair* pairs) {
         PCK(dalloc(&st.emat, ne));
         PCK(cudaMemcpy(st.emat, r.cfg.ace_matrix, ne * sizeof(double), cudaMemcpyHostToDevice));
     }
+    // tensor form: each pair's window and entry tables, for the grid edges that run it
+    st.tct.assign(n_pairs, fftdock::TcTables{});
+    std::vector<int32_t> info_all, tpad_all;
+    for (int i = 0; i < n_pairs; ++i) {
+        SizeData& sd = r.sizes[pairs[i].grid_n];
+        st.info_off.push_back(info_all.size());
+        st.tpad_off.push_back(tpad_all.size());
+        if (!sd.tc) continue;
+        st.tct[i] = fftdock::tc_tables(pairs[i].lig_xyz, lt.data() + st.lig_off[i], pairs[i].n_lig, r.K, sd.N,
+                                      r.cfg.grid_step, sd.zero_h);
+        if (!st.tct[i].ok) continue;
+        info_all.insert(info_all.end(), st.tct[i].info.begin(), st.tct[i].info.end());
+        tpad_all.insert(tpad_all.end(), st.tct[i].tpad.begin(), st.tct[i].tpad.end());
+        sd.max_pad = std::max(sd.max_pad, st.tct[i].n_pad);
+    }
+    if (!info_all.empty()) {
+        PCK(dalloc(&st.tinfo, info_all.size()));
+        PCK(dalloc(&st.tpad, tpad_all.size()));
+        PCK(cudaMemcpy(st.tinfo, info_all.data(), info_all.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+        PCK(cudaMemcpy(st.tpad, tpad_all.data(), tpad_all.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    }
     return FFTDOCK_OK;
 }
 
@@ -456,6 +529,9 @@ int setup_sizes(Run& r, int n_pairs, const fftdock_pair* pairs) {
         sd.center0 = zero + h / 2.0;
         sd.ops = fftdock::size_ops(N);
         sd.batch = r.cfg.rot_batch;
+        sd.tc = r.tc && sd.ops->has_tc;
+        // the tensor form takes rotations in groups of 128
+        if (sd.tc) sd.batch = (sd.batch + fftdock::kTcRot - 1) / fftdock::kTcRot * fftdock::kTcRot;
         std::vector<float2> t32(N);
         std::vector<double2> t64(N);
         for (int k = 0; k < N; ++k) {
@@ -484,7 +560,8 @@ int tune_batch(Run& r, const fftdock_pair* pairs, int n_pairs, int N, cudaStream
     double best = 1e300;
     int best_b = sd.batch;
     for (int B : cand) {
-        if (B > 1024) continue;
+        // rotations per launch: multiples of 128 for the tensor form
+        if (B > 1024 || (sd.tc && B % fftdock::kTcRot)) continue;
         Work w;
         SizeData tmp = sd;
         int rc = alloc_work(r, w, tmp, B);
@@ -563,7 +640,8 @@ int fftdock_scan_pairs(const fftdock_config* cfg, int32_t n_pairs, const fftdock
     r.cfg = *cfg;
     const fftdock_config& c = r.cfg;
     if (c.cluster_trans) return fail(FFTDOCK_EUNSUPPORTED, "translational clustering is not part of the pair batch");
-    if (c.pencil_mode == FFTDOCK_PENCIL_TENSOR) return fail(FFTDOCK_EUNSUPPORTED, "the pair batch runs the FFT form");
+    if (c.pencil_mode < FFTDOCK_PENCIL_AUTO || c.pencil_mode > FFTDOCK_PENCIL_TENSOR)
+        return fail(FFTDOCK_EINVAL, "unknown pencil_mode");
     if (c.peaks_per_rot < 1 || c.peaks_per_rot > kKC) return fail(FFTDOCK_EINVAL, "peaks_per_rot must be in [1, 16]");
     if (c.max_trans_inp < 1) return fail(FFTDOCK_EINVAL, "max_trans_inp must be >= 1");
     if (c.rot_batch < 1 || c.rot_batch > 1024) return fail(FFTDOCK_EINVAL, "rot_batch must be in [1, 1024]");
@@ -583,6 +661,9 @@ int fftdock_scan_pairs(const fftdock_config* cfg, int32_t n_pairs, const fftdock
     } else {
         return fail(FFTDOCK_EINVAL, "unknown term_set");
     }
+    r.tc = c.precision == FFTDOCK_PREC_FP32 &&
+           (c.pencil_mode == FFTDOCK_PENCIL_TENSOR ||
+            (c.pencil_mode == FFTDOCK_PENCIL_AUTO && r.K >= fftdock::kTcMinTerms));
     for (int i = 0; i < n_pairs; ++i) {
         int rc = check_pair(c, pairs[i], i, r.K, r.ace);
         if (rc) return rc;
@@ -635,6 +716,8 @@ int fftdock_scan_pairs(const fftdock_config* cfg, int32_t n_pairs, const fftdock
             for (auto& kv : r.sizes) {
                 const int b = report->rot_batch[size_slot(kv.first)];
                 if (b >= 1 && b <= 1024) kv.second.batch = b;
+                if (kv.second.tc)
+                    kv.second.batch = (kv.second.batch + fftdock::kTcRot - 1) / fftdock::kTcRot * fftdock::kTcRot;
             }
         }
         if (tune) {

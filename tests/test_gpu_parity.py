@@ -185,11 +185,12 @@ def test_full_size_shape_ace_128(mode):
         assert_peaks_match(off, score, ref.offsets, ref.scores, exact)
 
 
-def test_batch_size_does_not_change_results():
+@pytest.mark.parametrize("mode", ["fft", "tensor"])
+def test_batch_size_does_not_change_results(mode):
     f = _fixture("scan_shape_ace_n32")
     out = []
-    for batch in (1, 4, 64):
-        with _scan(32, f["term_set"], f["ace"], batch=batch) as s:
+    for batch in (1, 4, 64, 300):
+        with _scan(32, f["term_set"], f["ace"], batch=batch, mode=mode) as s:
             s.set_receptor(f["rec_xyz"], f["rec_type"])
             s.set_ligand(f["lig_xyz"], f["lig_type"])
             out.append(s.scan(f["rotations"], first_rot_id=10))
@@ -198,7 +199,10 @@ def test_batch_size_does_not_change_results():
     assert np.all(out[0].peaks["rot_id"][:, 0] == 10 + np.arange(len(f["rotations"])))
 
 
-def test_out_of_grid_rotations_are_reported():
+@pytest.mark.parametrize("mode", ["auto", "tensor"])
+def test_out_of_grid_rotations_are_reported(mode):
+    """Out-of-grid atoms are clamped into the grid (and, in the tensor form,
+    aimed at its dummy staging row) and the rotation is reported."""
     from proddl2_gb300 import FFTDockError, _lib
     f = _fixture("scan_shape_n48")
     geom = O.Geometry.centred(1.2, 48)
@@ -211,7 +215,7 @@ def test_out_of_grid_rotations_are_reported():
     rots = np.stack([np.eye(3), turn, np.eye(3)])
     ok = [O.bin_ligand(geom, r, lig)[1] for r in rots]
     assert ok == [False, True, False]
-    with _scan(48, f["term_set"], f["ace"]) as s:
+    with _scan(48, f["term_set"], f["ace"], mode=mode) as s:
         s.set_receptor(f["rec_xyz"], f["rec_type"])
         s.set_ligand(lig, f["lig_type"])
         with pytest.raises(FFTDockError) as ei:
@@ -239,8 +243,9 @@ def test_value_limit_and_queue_bound():
         assert np.all(res.peaks[i, :expect]["score"] < limit)
 
 
-def test_empty_receptor_and_single_atom_ligand():
-    with _scan(32, O.TERMS_SHAPE, None) as s:
+@pytest.mark.parametrize("mode", ["auto", "tensor"])
+def test_empty_receptor_and_single_atom_ligand(mode):
+    with _scan(32, O.TERMS_SHAPE, None, mode=mode) as s:
         s.set_receptor(np.zeros((0, 3)))
         s.set_ligand(np.zeros((1, 3)))
         res = s.scan(np.eye(3)[None])

@@ -358,7 +358,7 @@ TcTables tc_tables(const double* xyz, const int32_t* term, int n, int K, int N, 
     if (x0 + W > N) x0 = N - W;
     t.x0 = (int)x0;
     t.W = W;
-    // rows of the transposed entries: each non-empty term's range padded to 16
+    // rows of the transposed entries: each non-empty term's range padded to 8
     std::vector<int32_t> cnt(K, 0);
     for (int i = 0; i < n; ++i) ++cnt[term[i]];
     std::vector<int32_t> starts, ids;
@@ -370,7 +370,7 @@ TcTables tc_tables(const double* xyz, const int32_t* term, int n, int K, int N, 
         ids.push_back(k);
         t.tpad[k] = prun - run;
         run += cnt[k];
-        prun += (cnt[k] + 15) / 16 * 16;
+        prun += (cnt[k] + 7) / 8 * 8;
     }
     starts.push_back(prun);
     t.ka = (int)ids.size();

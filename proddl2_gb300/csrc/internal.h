@@ -151,7 +151,7 @@ struct BatchArgs {
     const int32_t* tinfo;       // padded entry starts of the n_tc_terms non-empty terms, then their term ids
     const int32_t* tpad;        // [K] padded start - start of each term's entries
     int n_tc_terms;
-    int n_pad;                  // entries per rotation with every term padded to a multiple of 16
+    int n_pad;                  // entries per rotation with every term padded to a multiple of 8
     int* err;                   // device word: nonzero after a pipeline timeout
     WideArgs wide;              // queue + clustering path (wide.corr != nullptr)
 };
@@ -159,7 +159,7 @@ struct BatchArgs {
 // The tensor pencil stage's per-ligand tables: the x window [x0, x0 + W)
 // that holds the ligand's cells under every rotation about the origin, and
 // the rows of the transposed entries (each non-empty term's range padded to
-// 16).  ok = the window and the term count fit the stage.
+// 8).  ok = the window and the term count fit the stage.
 struct TcTables {
     int x0 = 0, W = 0;
     int n_pad = 0;                 // padded rows per rotation

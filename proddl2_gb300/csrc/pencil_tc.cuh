@@ -21,7 +21,7 @@
 // c's descriptor starts (W/8 - 1 - c) 8-row groups into E.  F comes from the
 // ligand entries of the term, which ligand prep writes transposed per group
 // of 128 rotations ([entry / 4][rotation][entry % 4], sorted by (term, x) per
-// rotation, each term's range padded to a multiple of 16, x relative to x0;
+// rotation, each term's range padded to a multiple of 8, x relative to x0;
 // padding and cells outside the window carry x' = W, a dummy staging row).
 // A term's entries occupy the same index range in every rotation; two threads
 // per rotation walk the two halves of the range with coalesced loads.  Each
@@ -167,7 +167,7 @@ __device__ __forceinline__ void tc_walk(const uint4* eq, int nblk, unsigned ky, 
     }
 }
 
-// tinfo: [0, Ka] padded entry starts (multiples of 16) of the Ka non-empty
+// tinfo: [0, Ka] padded entry starts (multiples of 8) of the Ka non-empty
 // terms, [Ka + 1, 2 Ka] their term ids; n_pad = entry rows per rotation group
 template <int N>
 __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(

@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(256) ligand_prep_kernel(
             if (act) ent[dst] = key;
             // transposed copy for the tensor pencil stage,
             // [q / 128][row / 4][q % 128][row % 4], with each term's rows
-            // padded to a multiple of 16; the term is implied by the row and
+            // padded to a multiple of 8; the term is implied by the row and
             // x is stored relative to the window start x0 (mod 256: cells
             // outside the window stay outside it)
             if (act && ent_t) {

@@ -108,24 +108,33 @@ __host__ __device__ inline size_t tc_smem_bytes(int N, int n_chunks, int n_terms
     return b < 76 * 1024 ? 76 * 1024 : b;
 }
 
-// One entry e of a rotation's sorted walk: add its phase to the running sum
-// of its x bin (restarted when x changes) and store the sum into the bin's
-// staging row, or, for SIDE and the walk's first bin, into the side slot.
+// A rotation's sorted walk, eight entries at a time: first the eight phase
+// lookups (so that none waits behind a staging store), then for each entry
+// the running sum of its x bin (restarted when x changes), stored into the
+// bin's staging row or, for SIDE and the walk's first bin, into the side slot.
 template <bool SIDE, int N>
-__device__ __forceinline__ void tc_entry(uint32_t e, unsigned ky, unsigned kz, uint32_t twl, uint32_t stg,
-                                         uint32_t sd, unsigned first, unsigned W, unsigned& cur, float2& acc) {
-    // x relative to the window start; padding and cells outside the window
-    // carry x' = W, a dummy staging row
-    const unsigned xr = e >> 16;
-    const unsigned ph = (ky * ((e >> 8) & 255u) + kz * (e & 255u)) % (unsigned)N;
-    const float2 z = ld_shared_f2_const(twl + ph * 256u);
-    const float keep = xr != cur ? 0.f : 1.f;
-    acc.x = fmaf(acc.x, keep, z.x);
-    acc.y = fmaf(acc.y, keep, z.y);
-    cur = xr;
-    uint32_t dst = stg + xr * 1024u;
-    if (SIDE) dst = xr == first ? sd : dst;
-    st_shared_f2(dst, acc.x, acc.y);
+__device__ __forceinline__ void tc_entries8(const uint32_t (&e)[8], unsigned ky, unsigned kz, uint32_t twl,
+                                            uint32_t stg, uint32_t sd, unsigned first, unsigned& cur, float2& acc) {
+    float2 z[8];
+    unsigned xr[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        // x relative to the window start; padding and cells outside the
+        // window carry x' = W, a dummy staging row
+        xr[q] = e[q] >> 16;
+        const unsigned ph = (ky * ((e[q] >> 8) & 255u) + kz * (e[q] & 255u)) % (unsigned)N;
+        z[q] = ld_shared_f2_const(twl + ph * 256u);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const float keep = xr[q] != cur ? 0.f : 1.f;
+        acc.x = fmaf(acc.x, keep, z[q].x);
+        acc.y = fmaf(acc.y, keep, z[q].y);
+        cur = xr[q];
+        uint32_t dst = stg + xr[q] * 1024u;
+        if (SIDE) dst = xr[q] == first ? sd : dst;
+        st_shared_f2(dst, acc.x, acc.y);
+    }
 }
 
 // Walk nblk blocks of 8 rows from eq (this rotation's quads of rows: one
@@ -137,6 +146,7 @@ template <bool SIDE, int N>
 __device__ __forceinline__ void tc_walk(const uint4* eq, int nblk, unsigned ky, unsigned kz, uint32_t twl,
                                         uint32_t stg, uint32_t sd, unsigned first, unsigned W, uint4 a0, uint4 a1,
                                         uint4 b0, uint4 b1) {
+    (void)W;
     unsigned cur = 0xffffffffu;
     float2 acc = make_float2(0.f, 0.f);
     if (nblk <= 0) return;
@@ -146,14 +156,8 @@ __device__ __forceinline__ void tc_walk(const uint4* eq, int nblk, unsigned ky, 
         x1 = __ldg(eq + (size_t)(2 * blk + 1) * TC_ROT);
     };
     auto sum = [&](const uint4& x0, const uint4& x1) {
-        tc_entry<SIDE, N>(x0.x, ky, kz, twl, stg, sd, first, W, cur, acc);
-        tc_entry<SIDE, N>(x0.y, ky, kz, twl, stg, sd, first, W, cur, acc);
-        tc_entry<SIDE, N>(x0.z, ky, kz, twl, stg, sd, first, W, cur, acc);
-        tc_entry<SIDE, N>(x0.w, ky, kz, twl, stg, sd, first, W, cur, acc);
-        tc_entry<SIDE, N>(x1.x, ky, kz, twl, stg, sd, first, W, cur, acc);
-        tc_entry<SIDE, N>(x1.y, ky, kz, twl, stg, sd, first, W, cur, acc);
-        tc_entry<SIDE, N>(x1.z, ky, kz, twl, stg, sd, first, W, cur, acc);
-        tc_entry<SIDE, N>(x1.w, ky, kz, twl, stg, sd, first, W, cur, acc);
+        const uint32_t e[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+        tc_entries8<SIDE, N>(e, ky, kz, twl, stg, sd, first, cur, acc);
     };
     for (int blk = 0; blk < nblk; blk += 3) {
         ld(blk + 2, c0, c1);

@@ -356,8 +356,7 @@ def run_ours(args):
     avg_launch_ms = pencil_ms / max(launches, 1)
     # one timed stage is one kernel, except the queue + clustering stage:
     # bound, gather, check, 6 x (digit pass + pick), gather, finish
-    # the tensor form's plane stage also runs the g2 transpose
-    per_stage = {"finalize": 17 if args.cluster else 1, "plane": 2 if info["pencil_path"] == "tensor" else 1}
+    per_stage = {"finalize": 17 if args.cluster else 1}
     gpu_launches = sum(v[0] * per_stage.get(k, 1) for k, v in kstats.items())
     total_kernel_ms = sum(v[1] for v in kstats.values())
     share = pencil_ms / total_kernel_ms if total_kernel_ms else None

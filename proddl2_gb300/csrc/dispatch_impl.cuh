@@ -98,12 +98,37 @@ template <int N> struct SizeOpsImpl {
         return cudaGetLastError();
     }
 
-    template <bool DBG>
-    static cudaError_t launch_plane(dim3 grid, size_t sm, const BatchArgs& a, float* corr, cudaStream_t s) {
-        cudaError_t e = set_smem((const void*)plane_kernel<N, DBG>, sm);
+    template <bool DBG, bool QUAD>
+    static cudaError_t launch_plane(dim3 grid, size_t sm, const float2* src, const BatchArgs& a, float* corr,
+                                    cudaStream_t s) {
+        cudaError_t e = set_smem((const void*)plane_kernel<N, DBG, QUAD>, sm);
         if (e != cudaSuccess) return e;
-        plane_kernel<N, DBG><<<grid, 32 * G, sm, s>>>(a.g2, a.tw32, a.cand_v, a.cand_i, corr);
-        return cudaGetLastError();
+        if constexpr (QUAD) {
+            // clusters of 4 CTAs along x (the planes of one x-quad)
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = grid;
+            cfg.blockDim = dim3(32 * G);
+            cfg.dynamicSmemBytes = sm;
+            cfg.stream = s;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = 4;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            return cudaLaunchKernelEx(&cfg, plane_kernel<N, DBG, QUAD>, src, (const float2*)a.tw32, a.cand_v,
+                                      a.cand_i, corr);
+        } else {
+            plane_kernel<N, DBG, QUAD><<<grid, 32 * G, sm, s>>>(src, a.tw32, a.cand_v, a.cand_i, corr);
+            return cudaGetLastError();
+        }
+    }
+    template <bool QUAD>
+    static cudaError_t plane(dim3 grid, size_t sm, const float2* src, const BatchArgs& a, float* corr,
+                             cudaStream_t s) {
+        return corr ? launch_plane<true, QUAD>(grid, sm, src, a, corr, s)
+                    : launch_plane<false, QUAD>(grid, sm, src, a, nullptr, s);
     }
 
     // K1 over a.n_rot rotations
@@ -152,19 +177,14 @@ template <int N> struct SizeOpsImpl {
             if (e != cudaSuccess) return e;
         }
         if (a.ev && (e = cudaEventRecord(a.ev[1], s)) != cudaSuccess) return e;
-        if constexpr (kHasTc) {
-            // the tensor stage's output into the plane stage's layout (timed with the plane stage)
-            if (tc) {
-                pencil_transpose_kernel<N><<<dim3((N * H + 31) / 32, nb), 256, 0, s>>>(a.g2t, a.g2);
-                if ((e = cudaGetLastError()) != cudaSuccess) return e;
-            }
-        }
         // K3 (the queue + clustering path also writes every correlation grid)
         const size_t sm3 = plane_smem();
         dim3 grid3(N, nb);
         float* corr = a.dbg_corr ? a.dbg_corr : a.wide.corr;
-        if (corr) e = launch_plane<true>(grid3, sm3, a, corr, s);
-        else e = launch_plane<false>(grid3, sm3, a, nullptr, s);
+        if constexpr (kHasTc) {
+            if (tc) e = plane<true>(grid3, sm3, a.g2t, a, corr, s);  // the tensor stage's x-quads
+        }
+        if (!tc) e = plane<false>(grid3, sm3, a.g2, a, corr, s);
         if (e != cudaSuccess) return e;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if (a.ev && (e = cudaEventRecord(a.ev[2], s)) != cudaSuccess) return e;

@@ -71,7 +71,7 @@ struct fftdock_ctx {
     uint32_t* ent = nullptr;
     int32_t* offs = nullptr;
     float2* g2 = nullptr;
-    float2* g2t = nullptr;   // tensor stage output before the transpose
+    float2* g2t = nullptr;   // tensor stage output (x-quads)
     float* cand_v = nullptr;
     int32_t* cand_i = nullptr;
 

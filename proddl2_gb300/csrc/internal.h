@@ -140,8 +140,9 @@ struct BatchArgs {
     float* pool_v;              // optional [B][KC]
     int32_t* pool_i;
     cudaEvent_t* ev;            // optional: events recorded by the middle stage (see SizeOps::middle)
-    // tensor-core pencil stage (use_tc): it writes g2t [B][N*H][N] (x fastest,
-    // coalesced), transposed into g2 before the plane stage
+    // tensor-core pencil stage (use_tc): it writes g2t as x-quads
+    // [B][N/4][N*H][4] (four consecutive x per pencil), which the plane stage
+    // reads in clusters of 4 CTAs
     float2* g2t;
     int use_tc;
     const float2* circ;         // [K][N*H][N] receptor circulant samples

@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
             tc::mbar_arrive(&full_bar);
             if (k + 1 < Ka) preload(k + 1);
         }
-        // ---------------- epilogue: TMEM -> g2t[rot][p][x] (coalesced along x) ----------------
+        // ---- epilogue: TMEM -> x-quads g2t[rot][x/4][p][x%4] (a warp store fills 8 sectors) ----
         if (!*(volatile int*)&abort_flag && !tc::mbar_wait(&done_bar, 0, TC_WAIT_NS)) {
             atomicOr(err, 4);
             abort_flag = 1;
@@ -402,9 +402,9 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
                     const int rr = g * TC_ROT + c0 + j;
+                    const size_t o = (size_t)rr * NH * N + (size_t)(xo >> 2) * NH * 4 + (size_t)p * 4 + (xo & 3);
                     if (rr < n_rot)
-                        g2t[((size_t)rr * NH + p) * N + xo] =
-                            make_float2(__uint_as_float(dre[j]) * inv, __uint_as_float(dim[j]) * inv);
+                        g2t[o] = make_float2(__uint_as_float(dre[j]) * inv, __uint_as_float(dim[j]) * inv);
                 }
             }
         }
@@ -414,27 +414,6 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, 256);
-}
-
-// g2t [rot][p][x] -> g2 [rot][x][PP] (the plane stage's layout): a CTA moves
-// 32 pencils x N cells of one rotation through shared memory, reading 32 N
-// contiguous values and writing, per x, 32 contiguous pencils
-template <int N>
-__global__ void __launch_bounds__(256) pencil_transpose_kernel(const float2* __restrict__ src,
-                                                               float2* __restrict__ dst) {
-    constexpr int H = N / 2 + 1, NH = N * H, PP = pencil_pitch(N);
-    __shared__ float2 tile[32][N + 1];
-    const int p0 = blockIdx.x * 32;
-    const size_t q = blockIdx.y;
-    const int np = NH - p0 < 32 ? NH - p0 : 32;
-    const float2* s = src + (q * NH + p0) * N;
-    for (int i = threadIdx.x; i < np * N; i += blockDim.x) tile[i / N][i % N] = s[i];
-    __syncthreads();
-    float2* d = dst + q * N * PP + p0;
-    for (int i = threadIdx.x; i < 32 * N; i += blockDim.x) {
-        const int x = i >> 5, pr = i & 31;
-        if (pr < np) d[(size_t)x * PP + pr] = tile[pr][x];
-    }
 }
 
 // per-pencil power-of-two exponent so that the largest circulant component

@@ -341,8 +341,14 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G, PencilTraits<N>::MINB) 
 // bound on the KC-th value and only cells at or below it reach a warp top-KC.
 // (FFTW c2r of FFTCorrelator::correlate + CorrelationProcessor::
 // selectIntoQueue, docking_fft.hpp:452-468.)
+// Input layouts: QUAD = false, the FFT pencil stage's [B][N][PP] (each plane
+// contiguous); QUAD = true, the tensor pencil stage's x-quads
+// [B][N/4][N*H][4] (four consecutive planes interleaved per pencil), read by
+// clusters of 4 CTAs (planes 4c..4c+3) that each load a quarter of the
+// pencils as whole 32-byte groups and store every plane's value into that
+// plane's CTA through distributed shared memory.
 // ---------------------------------------------------------------------------
-template <int N, bool DBG>
+template <int N, bool DBG, bool QUAD>
 __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     const float2* __restrict__ g2, const float2* __restrict__ tw, float* __restrict__ cand_v,
     int32_t* __restrict__ cand_i, float* __restrict__ dbg) {
@@ -373,9 +379,38 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     const int q = blockIdx.y;
     const int tid = threadIdx.x;
     const int w = tid >> 5, l = tid & 31;
+    if constexpr (QUAD) asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
     for (int i = tid; i < N; i += blockDim.x) tws[i] = tw[i];
-    // element (ky, kz) of plane x: [B][N][PP], x-planes contiguous
-    const float2* src = g2 + ((size_t)q * N + x) * PP;
+    // element (ky, kz) of plane x at src[ky * H + kz]: global memory (FFT
+    // form) or this CTA's staged copy (x-quads)
+    const float2* src = QUAD ? plane : g2 + ((size_t)q * N + x) * PP;
+    if constexpr (QUAD) {
+        constexpr int NH = N * H;
+        static_assert(N % 4 == 0 && NH % 4 == 0, "x-quads need N % 4 == 0");
+        uint32_t rank;
+        asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
+        const int xb = x - (int)rank;  // the cluster's first plane
+        // this CTA's quarter of the pencils: NH / 2 16-byte halves (planes
+        // xb, xb + 1 | xb + 2, xb + 3), one per thread and step, coalesced
+        const float4* gs = reinterpret_cast<const float4*>(g2 + (size_t)q * NH * N + (size_t)(xb >> 2) * NH * 4) +
+                           (size_t)rank * (NH / 2);
+        const uint32_t loc = static_cast<uint32_t>(__cvta_generic_to_shared(plane)) + rank * (NH / 4) * 8u;
+        uint32_t rb[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(rb[j]) : "r"(loc), "r"(j));
+        asm volatile("barrier.cluster.wait.aligned;" ::: "memory");  // every CTA of the cluster runs
+#pragma unroll 4
+        for (int e = tid; e < NH / 2; e += 32 * G) {
+            const float4 a = gs[e];
+            const int hf = e & 1;
+            const uint32_t off = (uint32_t)(e >> 1) * 8u;
+            const uint32_t d0 = hf ? rb[2] : rb[0], d1 = hf ? rb[3] : rb[1];
+            asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(d0 + off), "f"(a.x), "f"(a.y) : "memory");
+            asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(d1 + off), "f"(a.z), "f"(a.w) : "memory");
+        }
+        asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+    }
     __syncthreads();
 
     // columns: inverse DFT along ky
@@ -390,15 +425,16 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
             float2 a = make_float2(0.f, 0.f);
             if (valid) {
                 if (s == 0) {
-                    const float2 d = src[(size_t)(ky * H)], ny = src[(size_t)(ky * H + NS)];
+                    const float2 d = src[ky * H], ny = src[ky * H + NS];
                     a = make_float2(d.x - ny.y, d.y + ny.x);
                 } else {
-                    a = src[(size_t)(ky * H + s)];
+                    a = src[ky * H + s];
                 }
             }
             v[r] = a;
         }
         dft<R1, +1>(v);
+        if constexpr (QUAD) __syncthreads();  // the staged columns are read: their slots take the outputs
         if (valid) {
 #pragma unroll
             for (int r = 0; r < R1; ++r) plane[(w * R1 + r) * H + s] = v[r];

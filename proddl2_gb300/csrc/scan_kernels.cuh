@@ -101,6 +101,33 @@ struct WarpTopK {
     }
 };
 
+// Compare-exchange with lane ^ j under better(): this lane keeps the better
+// of the two pairs when keep_min, else the other one.
+__device__ __forceinline__ void warp_cmp_swap(float& v, int& i, int j, bool keep_min) {
+    const float pv = __shfl_xor_sync(0xffffffffu, v, j);
+    const int pi = __shfl_xor_sync(0xffffffffu, i, j);
+    if (better(pv, pi, v, i) == keep_min) {
+        v = pv;
+        i = pi;
+    }
+}
+
+// Bitonic sort of one (value, index) pair per lane, ascending by better()
+// across the warp (15 compare-exchange steps).
+__device__ __forceinline__ void warp_sort32(float& v, int& i, int lane) {
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1)
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) warp_cmp_swap(v, i, j, ((lane & k) == 0) == ((lane & j) == 0));
+}
+
+// Lanes 0..15 ascending and lanes 16..31 descending (a bitonic sequence) ->
+// all 32 ascending: lanes < 16 then hold the 16 best of both halves.
+__device__ __forceinline__ void warp_merge32(float& v, int& i, int lane) {
+#pragma unroll
+    for (int j = 16; j > 0; j >>= 1) warp_cmp_swap(v, i, j, (lane & j) == 0);
+}
+
 // Merge per-warp lists staged in shared memory (nw lists of KC) into warp 0's
 // list; the caller syncs before and reads lanes < KC of warp 0 after.
 __device__ __forceinline__ void merge_lists(const float* sv, const int* si, int n, WarpTopK& tk, int lane) {
@@ -368,8 +395,6 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     float* lv_s = reinterpret_cast<float*>(tws + N);      // [G*KC]
     int* li_s = reinterpret_cast<int*>(lv_s + G * KC);    // [G*KC]
     constexpr int PCAND = 256;                            // candidate list capacity
-    __shared__ float tmin_v[32 * G];                      // each thread's best cell
-    __shared__ int tmin_i[32 * G];
     __shared__ float cand_sv[PCAND];
     __shared__ int cand_si[PCAND];
     __shared__ float bound_v;
@@ -400,55 +425,89 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
         for (int j = 0; j < 4; ++j)
             asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(rb[j]) : "r"(loc), "r"(j));
         asm volatile("barrier.cluster.wait.aligned;" ::: "memory");  // every CTA of the cluster runs
-#pragma unroll 4
-        for (int e = tid; e < NH / 2; e += 32 * G) {
-            const float4 a = gs[e];
-            const int hf = e & 1;
-            const uint32_t off = (uint32_t)(e >> 1) * 8u;
-            const uint32_t d0 = hf ? rb[2] : rb[0], d1 = hf ? rb[3] : rb[1];
-            asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(d0 + off), "f"(a.x), "f"(a.y) : "memory");
-            asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(d1 + off), "f"(a.z), "f"(a.w) : "memory");
+        // loads in batches ahead of their stores (a store's memory clobber
+        // would otherwise hold each load until the previous store)
+        constexpr int PER = (NH / 2 + 32 * G - 1) / (32 * G), BATCH = 9;
+#pragma unroll
+        for (int b0 = 0; b0 < PER; b0 += BATCH) {
+            float4 a[BATCH];
+#pragma unroll
+            for (int k = 0; k < BATCH; ++k) {
+                const int e = tid + (b0 + k) * 32 * G;
+                if (b0 + k < PER && e < NH / 2) a[k] = gs[e];
+            }
+#pragma unroll
+            for (int k = 0; k < BATCH; ++k) {
+                const int e = tid + (b0 + k) * 32 * G;
+                if (b0 + k < PER && e < NH / 2) {
+                    const uint32_t off = (uint32_t)(e >> 1) * 8u;
+                    const uint32_t d0 = (e & 1) ? rb[2] : rb[0], d1 = (e & 1) ? rb[3] : rb[1];
+                    asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(d0 + off), "f"(a[k].x), "f"(a[k].y)
+                                 : "memory");
+                    asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(d1 + off), "f"(a[k].z), "f"(a[k].w)
+                                 : "memory");
+                }
+            }
         }
         asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
     }
     __syncthreads();
 
+    // Warp-local passes at N = 128 (8 lanes share a column or a row, so
+    // their exchanges need __syncwarp only).  A group's pass-1 outputs are
+    // stored swizzled within the line: position 16a + b (columns) or 8a + b
+    // (rows) at slot 16a + ((a + b) & 15) or 8a + ((a + b) & 7); with the
+    // half-warp's two lines 8 apart (column kz or row y), every 8-byte access
+    // of a half-warp hits distinct bank pairs.  Columns need the plane staged
+    // in shared memory (x-quads); the FFT form's columns stay lane-per-column
+    // for coalesced global loads.
+    constexpr bool WLR = N == 128 && G == 8 && GR == 8 && R1R == 8;
+    constexpr bool WLC = WLR && QUAD && R1 == 16;
+    const int lg = l >> 3, lm = l & 7;  // group (line) within the warp, thread within the group
+
     // columns: inverse DFT along ky
+    if constexpr (WLC) {
 #pragma unroll 1
-    for (int c = 0; c < CC; ++c) {
-        const int s = 32 * c + l;
-        const bool valid = s < NS;
-        float2 v[R1];
+        for (int c = 0; c < CC; ++c) {
+            const int s = 32 * c + w + 8 * lg;  // < NS
+            float2 v[16];
 #pragma unroll
-        for (int r = 0; r < R1; ++r) {
-            const int ky = w + G * r;
-            float2 a = make_float2(0.f, 0.f);
-            if (valid) {
+            for (int r = 0; r < 16; ++r) {
+                const int ky = lm + 8 * r;
                 if (s == 0) {
-                    const float2 d = src[ky * H], ny = src[ky * H + NS];
-                    a = make_float2(d.x - ny.y, d.y + ny.x);
+                    const float2 d = plane[ky * H], ny = plane[ky * H + NS];
+                    v[r] = make_float2(d.x - ny.y, d.y + ny.x);
                 } else {
-                    a = src[ky * H + s];
+                    v[r] = plane[ky * H + s];
                 }
             }
-            v[r] = a;
-        }
-        dft<R1, +1>(v);
-        if constexpr (QUAD) __syncthreads();  // the staged columns are read: their slots take the outputs
-        if (valid) {
+            dft<16, +1>(v);
+            __syncwarp();  // the group's column is read: its slots take the outputs
 #pragma unroll
-            for (int r = 0; r < R1; ++r) plane[(w * R1 + r) * H + s] = v[r];
-        }
-        __syncthreads();
-        if (valid) {
-            float2 out[R1];
-            line_pass2<PC, +1, 1, H>(plane, w, s, tws, out);
+            for (int r = 0; r < 16; ++r) plane[(16 * lm + ((r + lm) & 15)) * H + s] = v[r];
+            __syncwarp();
+            float2 out[16];
 #pragma unroll
-            for (int i = 0; i < PC::NB; ++i)
+            for (int i = 0; i < 2; ++i) {
+                const int j = lm + 8 * i;
+                float2 u[8];
 #pragma unroll
-                for (int r = 0; r < G; ++r) {
-                    const int y = w + G * i + R1 * r;
-                    const float2 o = out[i * G + r];
+                for (int r = 0; r < 8; ++r) {
+                    float2 a = plane[(16 * r + ((j + r) & 15)) * H + s];  // position j + 16 r
+                    if (r != 0) a = ctwiddle<+1>(a, tws[j * r]);
+                    u[r] = a;
+                }
+                dft<8, +1>(u);
+#pragma unroll
+                for (int r = 0; r < 8; ++r) out[i * 8 + r] = u[r];
+            }
+            __syncwarp();
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    const int y = lm + 8 * i + 16 * r;
+                    const float2 o = out[i * 8 + r];
                     if (s == 0) {
                         plane[y * H] = make_float2(o.x, 0.f);
                         plane[y * H + NS] = make_float2(o.y, 0.f);
@@ -457,18 +516,65 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
                     }
                 }
         }
+    } else {
+#pragma unroll 1
+        for (int c = 0; c < CC; ++c) {
+            const int s = 32 * c + l;
+            const bool valid = s < NS;
+            float2 v[R1];
+#pragma unroll
+            for (int r = 0; r < R1; ++r) {
+                const int ky = w + G * r;
+                float2 a = make_float2(0.f, 0.f);
+                if (valid) {
+                    if (s == 0) {
+                        const float2 d = src[ky * H], ny = src[ky * H + NS];
+                        a = make_float2(d.x - ny.y, d.y + ny.x);
+                    } else {
+                        a = src[ky * H + s];
+                    }
+                }
+                v[r] = a;
+            }
+            dft<R1, +1>(v);
+            if constexpr (QUAD) __syncthreads();  // the staged columns are read: their slots take the outputs
+            if (valid) {
+#pragma unroll
+                for (int r = 0; r < R1; ++r) plane[(w * R1 + r) * H + s] = v[r];
+            }
+            __syncthreads();
+            if (valid) {
+                float2 out[R1];
+                line_pass2<PC, +1, 1, H>(plane, w, s, tws, out);
+#pragma unroll
+                for (int i = 0; i < PC::NB; ++i)
+#pragma unroll
+                    for (int r = 0; r < G; ++r) {
+                        const int y = w + G * i + R1 * r;
+                        const float2 o = out[i * G + r];
+                        if (s == 0) {
+                            plane[y * H] = make_float2(o.x, 0.f);
+                            plane[y * H + NS] = make_float2(o.y, 0.f);
+                        } else {
+                            plane[y * H + s] = o;
+                        }
+                    }
+            }
+        }
     }
     __syncthreads();
 
     // rows: C2R along kz via an N/2-point complex inverse DFT.  Each row's N
     // real outputs replace its spectrum in shared memory, and every thread
     // keeps the smallest (value, offset) it produced.
-    const int gi = w / GR, m = w % GR;
+    const int gi = w / GR, m = WLR ? lm : w % GR;
+    // the row a thread works on in round ro
+    auto row_of = [&](int ro) { return WLR ? 32 * ro + w + 8 * lg : ro * ROWS + gi * 32 + l; };
     float bmin_v = INFINITY;
     int bmin_i = 0x7fffffff;
 #pragma unroll 1
     for (int ro = 0; ro < ROUNDS; ++ro) {
-        const int y = ro * ROWS + gi * 32 + l;
+        const int y = row_of(ro);
         const bool valid = y < N;
         float2* row = plane + (valid ? y : 0) * H;
         float2 v[R1R];
@@ -486,16 +592,32 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
             }
             v[r] = yk;
         }
-        __syncthreads();
-        dft<R1R, +1>(v);
-        if (valid) {
-#pragma unroll
-            for (int r = 0; r < R1R; ++r) row[m * R1R + r] = v[r];
-        }
-        __syncthreads();
         float2 out[R1R];
-        if (valid) line_pass2<PR, +1, 2, 1>(row, m, 0, tws, out);
-        __syncthreads();  // the row's spectrum is consumed: its slots take the real outputs
+        if constexpr (WLR) {
+            __syncwarp();
+            dft<8, +1>(v);
+#pragma unroll
+            for (int r = 0; r < 8; ++r) row[8 * m + ((r + m) & 7)] = v[r];
+            __syncwarp();
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                float2 a = row[8 * r + ((m + r) & 7)];  // position m + 8 r
+                if (r != 0) a = ctwiddle<+1>(a, tws[2 * m * r]);
+                out[r] = a;
+            }
+            dft<8, +1>(out);
+            __syncwarp();  // the row's spectrum is consumed: its slots take the real outputs
+        } else {
+            __syncthreads();
+            dft<R1R, +1>(v);
+            if (valid) {
+#pragma unroll
+                for (int r = 0; r < R1R; ++r) row[m * R1R + r] = v[r];
+            }
+            __syncthreads();
+            if (valid) line_pass2<PR, +1, 2, 1>(row, m, 0, tws, out);
+            __syncthreads();  // the row's spectrum is consumed: its slots take the real outputs
+        }
         const int rowbase = (x * N + y) * N;
 #pragma unroll
         for (int i = 0; i < PR::NB; ++i)
@@ -515,17 +637,33 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     // Selection.  The KC-th best of the threads' minima bounds the plane's
     // KC-th best from above (at least KC cells lie at or below it), so only
     // cells at or below it can enter the plane's top KC.
-    tmin_v[tid] = bmin_v;
-    tmin_i[tid] = bmin_i;
+    // Every warp sorts its threads' minima; warp 0 merges the warps' 16 best
+    // (the KC best of all minima are among them).
+    static_assert(KC == 16, "the bitonic selection keeps 16 of 32 lanes");
+    {
+        float sv = bmin_v;
+        int si = bmin_i;
+        warp_sort32(sv, si, l);
+        if (l < KC) {
+            lv_s[w * KC + l] = sv;
+            li_s[w * KC + l] = si;
+        }
+    }
     if (tid == 0) n_cand = 0;
     __syncthreads();
-    WarpTopK tk;
     if (w == 0) {
-        tk.init();
-        for (int base = 0; base < 32 * G; base += 32) tk.offer(tmin_v[base + l], tmin_i[base + l], l);
-        if (l == 0) {
-            bound_v = tk.tv;
-            bound_i = tk.ti;
+        float sv = l < KC ? lv_s[l] : INFINITY;
+        int si = l < KC ? li_s[l] : 0x7fffffff;
+        for (int g = 1; g < G; ++g) {
+            if (l >= KC) {  // warp g's list, reversed
+                sv = lv_s[g * KC + 31 - l];
+                si = li_s[g * KC + 31 - l];
+            }
+            warp_merge32(sv, si, l);
+        }
+        if (l == KC - 1) {
+            bound_v = sv;
+            bound_i = si;
         }
     }
     __syncthreads();
@@ -534,7 +672,7 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     // every thread re-reads its own cells (the positions the row pass gave it)
 #pragma unroll 1
     for (int ro = 0; ro < ROUNDS; ++ro) {
-        const int y = ro * ROWS + gi * 32 + l;
+        const int y = row_of(ro);
         if (y >= N) continue;
         const float2* row = plane + y * H;
         const int rowbase = (x * N + y) * N;
@@ -558,24 +696,42 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     const int nc = n_cand;
     if (nc <= PCAND) {
         if (w == 0) {
-            tk.init();
+            // running best KC in lanes < KC; each chunk of 32 is sorted and its
+            // best KC merged in
+            float sv = INFINITY;
+            int si = 0x7fffffff;
             for (int base = 0; base < nc; base += 32) {
                 const int e = base + l;
-                tk.offer(e < nc ? cand_sv[e] : INFINITY, e < nc ? cand_si[e] : 0x7fffffff, l);
+                float cv = e < nc ? cand_sv[e] : INFINITY;
+                int ci = e < nc ? cand_si[e] : 0x7fffffff;
+                warp_sort32(cv, ci, l);
+                const float rv = __shfl_sync(0xffffffffu, cv, 31 - l);
+                const int ri = __shfl_sync(0xffffffffu, ci, 31 - l);
+                if (base == 0) {
+                    sv = cv;
+                    si = ci;
+                } else {
+                    if (l >= KC) {
+                        sv = rv;
+                        si = ri;
+                    }
+                    warp_merge32(sv, si, l);
+                }
             }
             if (l < KC) {
-                cand_v[((size_t)q * N + x) * KC + l] = tk.lv;
-                cand_i[((size_t)q * N + x) * KC + l] = tk.li;
+                cand_v[((size_t)q * N + x) * KC + l] = sv;
+                cand_i[((size_t)q * N + x) * KC + l] = si;
             }
         }
         return;
     }
     // many cells tie at the bound (a flat plane): every warp offers its own
     // cells, then warp 0 merges the warps' lists
+    WarpTopK tk;
     tk.init();
 #pragma unroll 1
     for (int ro = 0; ro < ROUNDS; ++ro) {
-        const int y = ro * ROWS + gi * 32 + l;
+        const int y = row_of(ro);
         const bool valid = y < N;
         const float2* row = plane + (valid ? y : 0) * H;
         const int rowbase = (x * N + y) * N;

@@ -49,6 +49,9 @@ def parse_args():
     p.add_argument("--workload", default="shape_ace128")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--n-rot", type=int, default=0, help="scan only this many rotations per step (profiling runs)")
+    p.add_argument("--rot-batch", type=int, default=0,
+                   help="rotations per pencil/plane launch (default: the workload's, rounded up to 128 by the "
+                        "tensor pencil stage)")
     p.add_argument("--pencil", default="auto", choices=["auto", "fft", "tensor"])
     p.add_argument("--precision", default="fp32", choices=["fp32", "bf16"],
                    help="receptor spectra storage (bf16: the precision-study mode)")
@@ -266,6 +269,8 @@ def run_ours(args):
     w = workload(args.workload)
     if args.n_rot > 0:
         w["n_rot"] = args.n_rot
+    if args.rot_batch > 0:
+        w["rot_batch"] = args.rot_batch
     pair = synth.make_pair(w["n_rec"], w["n_lig"], w["n_rot"], seed=1)
     n_rot = w["n_rot"]
     queue = (args.cluster_queue or 100 * w["peaks"]) if args.cluster else 10000

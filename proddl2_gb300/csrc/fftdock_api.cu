@@ -334,7 +334,7 @@ __global__ void fill_u32_kernel(uint32_t* p, uint32_t v, size_t n) {
 }  // namespace
 
 cudaError_t fill_padding(uint32_t* ent_t, int W, size_t n, cudaStream_t s) {
-    fill_u32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(ent_t, (uint32_t)W << 16, n);
+    fill_u32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(ent_t, (uint32_t)W << 24, n);
     return cudaGetLastError();
 }
 

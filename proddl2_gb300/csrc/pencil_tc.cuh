@@ -112,18 +112,27 @@ __host__ __device__ inline size_t tc_smem_bytes(int N, int n_chunks, int n_terms
 // lookups (so that none waits behind a staging store), then for each entry
 // the running sum of its x bin (restarted when x changes), stored into the
 // bin's staging row or, for SIDE and the walk's first bin, into the side slot.
+// Entry e = x' << 24 | y << 16 | z and kyz = kz << 16 | ky: bits 16 and up
+// of e * kyz (mod 2^32) hold ky y + kz z (< 2^15; the z ky term stays below
+// bit 16 and x' ky starts at bit 24), so a power-of-two N needs one multiply
+// and one field extract for the phase.
+template <int N>
+__device__ __forceinline__ unsigned tc_phase(uint32_t e, uint32_t kyz) {
+    if constexpr ((N & (N - 1)) == 0) return ((e * kyz) >> 16) & (unsigned)(N - 1);
+    else return (((e & 0xffffffu) * kyz) >> 16) % (unsigned)N;
+}
+
 template <bool SIDE, int N>
-__device__ __forceinline__ void tc_entries8(const uint32_t (&e)[8], unsigned ky, unsigned kz, uint32_t twl,
-                                            uint32_t stg, uint32_t sd, unsigned first, unsigned& cur, float2& acc) {
+__device__ __forceinline__ void tc_entries8(const uint32_t (&e)[8], uint32_t kyz, uint32_t twl, uint32_t stg,
+                                            uint32_t sd, unsigned first, unsigned& cur, float2& acc) {
     float2 z[8];
     unsigned xr[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         // x relative to the window start; padding and cells outside the
         // window carry x' = W, a dummy staging row
-        xr[q] = e[q] >> 16;
-        const unsigned ph = (ky * ((e[q] >> 8) & 255u) + kz * (e[q] & 255u)) % (unsigned)N;
-        z[q] = ld_shared_f2_const(twl + ph * 256u);
+        xr[q] = e[q] >> 24;
+        z[q] = ld_shared_f2_const(twl + tc_phase<N>(e[q], kyz) * 256u);
     }
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -143,7 +152,7 @@ __device__ __forceinline__ void tc_entries8(const uint32_t (&e)[8], unsigned ky,
 // one is summed; the loads may run up to 16 rows past the range, which the
 // entry buffer provides.
 template <bool SIDE, int N>
-__device__ __forceinline__ void tc_walk(const uint4* eq, int nblk, unsigned ky, unsigned kz, uint32_t twl,
+__device__ __forceinline__ void tc_walk(const uint4* eq, int nblk, uint32_t kyz, uint32_t twl,
                                         uint32_t stg, uint32_t sd, unsigned first, unsigned W, uint4 a0, uint4 a1,
                                         uint4 b0, uint4 b1) {
     (void)W;
@@ -157,7 +166,7 @@ __device__ __forceinline__ void tc_walk(const uint4* eq, int nblk, unsigned ky, 
     };
     auto sum = [&](const uint4& x0, const uint4& x1) {
         const uint32_t e[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
-        tc_entries8<SIDE, N>(e, ky, kz, twl, stg, sd, first, cur, acc);
+        tc_entries8<SIDE, N>(e, kyz, twl, stg, sd, first, cur, acc);
     };
     for (int blk = 0; blk < nblk; blk += 3) {
         ld(blk + 2, c0, c1);
@@ -201,6 +210,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
     const unsigned ky = (unsigned)(p / H), kz = (unsigned)(p - (p / H) * H);
+    const uint32_t kyz = (kz << 16) | ky;  // the phase multiplier of tc_phase
     const float c_scale = ldexpf(1.0f, (int)cscale[p]);
 
     if (tid == 0) abort_flag = *(volatile int*)err;
@@ -340,11 +350,11 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
             const int b0 = half ? na : 0, nb8 = half ? n8 - na : na;
             const uint4* eq = ent_g + (size_t)((jt0 >> 2) + 2 * b0) * TC_ROT;
             // the second half's first bin goes to the side slot
-            const unsigned first = half && nb8 > 0 ? (pa0.x >> 16) : 0xfffffffeu;
+            const unsigned first = half && nb8 > 0 ? (pa0.x >> 24) : 0xfffffffeu;
             if (half)
-                tc_walk<true, N>(eq, nb8, ky, kz, twl, stg, sd, first, (unsigned)W, pa0, pa1, pb0, pb1);
+                tc_walk<true, N>(eq, nb8, kyz, twl, stg, sd, first, (unsigned)W, pa0, pa1, pb0, pb1);
             else
-                tc_walk<false, N>(eq, nb8, ky, kz, twl, stg, sd, first, (unsigned)W, pa0, pa1, pb0, pb1);
+                tc_walk<false, N>(eq, nb8, kyz, twl, stg, sd, first, (unsigned)W, pa0, pa1, pb0, pb1);
             asm volatile("bar.sync 1, 256;" ::: "memory");
             // the second half's first bin: add its partial sum
             if (half && first < (unsigned)W) {

@@ -231,11 +231,13 @@ __global__ void __launch_bounds__(256) ligand_prep_kernel(
             // [q / 128][row / 4][q % 128][row % 4], with each term's rows
             // padded to a multiple of 8; the term is implied by the row and
             // x is stored relative to the window start x0 (mod 256: cells
-            // outside the window stay outside it)
+            // outside the window stay outside it); entry = x' << 24 | y << 16
+            // | z, so that one multiply by kz << 16 | ky gives the phase
             if (act && ent_t) {
                 const size_t row = (size_t)(dst + __ldg(tpad + (key >> 24)));
                 ent_t[(((size_t)(q >> 7) * (n_pad >> 2) + (row >> 2)) * 128 + (q & 127)) * 4 + (row & 3)] =
-                    (min(((key >> 16) - (uint32_t)x0) & 255u, (uint32_t)W) << 16) | (key & 0xffffu);
+                    (min(((key >> 16) - (uint32_t)x0) & 255u, (uint32_t)W) << 24) | (((key >> 8) & 255u) << 16) |
+                    (key & 255u);
             }
             if (act && w_out) {
                 w_out[(size_t)q * n_ent + dst] = w_in[i];

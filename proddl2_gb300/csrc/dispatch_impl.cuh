@@ -16,7 +16,7 @@ template <int N> struct SizeOpsImpl {
         return pencil_smem(K, n_ent) + (weighted ? (size_t)n_ent * sizeof(float) : 0);
     }
     static size_t pencil_smem(int K, int n_ent) {
-        return (size_t)PencilTraits<N>::BUFS * N * 32 * sizeof(float2) + N * sizeof(float2) +
+        return (size_t)PencilTraits<N>::BUFS * N * 32 * sizeof(float2) + (size_t)N * 17 * sizeof(float2) +
                ((size_t)K * N + 1) * sizeof(int32_t) +
                (size_t)n_ent * sizeof(uint32_t);
     }

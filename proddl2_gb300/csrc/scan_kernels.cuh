@@ -274,7 +274,11 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G, PencilTraits<N>::MINB) 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* xbuf = reinterpret_cast<float2*>(smem_raw);  // [BUFS][N][32]
     float2* tws = xbuf + BUFS * N * 32;                  // [N]
-    int32_t* offs_s = reinterpret_cast<int32_t*>(tws + N);  // [K*N+1]
+    // the phase table once per half-warp lane ([phase][16]): a warp's lanes
+    // are consecutive pencils, whose phases for one entry step by its z, so
+    // a single table would put lanes on the same banks whenever z is even
+    float2* twr = tws + N;                                  // [N][16]
+    int32_t* offs_s = reinterpret_cast<int32_t*>(twr + N * 16);  // [K*N+1]
     uint32_t* ent_s = reinterpret_cast<uint32_t*>(offs_s + K * N + 1);  // [n_ent]
     float* w_s = reinterpret_cast<float*>(ent_s + n_ent);                 // [n_ent] (weighted)
 
@@ -284,12 +288,20 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G, PencilTraits<N>::MINB) 
     const int w = tid >> 5, l = tid & 31;
     const int p = tile * 32 + l;
     const unsigned ky = (unsigned)(p / H), kz = (unsigned)(p - (p / H) * H);
+    // entries staged as y << 16 | z (x and the term are the bin's): bits 16 and
+    // up of u * (kz << 16 | ky) (mod 2^32) hold ky y + kz z (< 2^16 for N <=
+    // 144; the z ky term stays below bit 16), one multiply per phase
+    const uint32_t kyz = (kz << 16) | ky;
 
     for (int i = tid; i < N; i += blockDim.x) tws[i] = tw[i];
+    for (int i = tid; i < N * 16; i += blockDim.x) twr[i] = tw[i >> 4];
     const int32_t* offs_g = offs + (size_t)q * (K * N + 1);
     for (int i = tid; i <= K * N; i += blockDim.x) offs_s[i] = offs_g[i];
     const uint32_t* ent_g = ent + (size_t)q * n_ent;
-    for (int i = tid; i < n_ent; i += blockDim.x) ent_s[i] = ent_g[i];
+    for (int i = tid; i < n_ent; i += blockDim.x) {
+        const uint32_t u = ent_g[i];
+        ent_s[i] = (((u >> 8) & 255u) << 16) | (u & 255u);
+    }
     if constexpr (WEIGHTED) {
         const float* w_g = ent_w + (size_t)q * n_ent;
         for (int i = tid; i < n_ent; i += blockDim.x) w_s[i] = w_g[i];
@@ -308,9 +320,9 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G, PencilTraits<N>::MINB) 
             const int b = offs_s[t * N + x], e = offs_s[t * N + x + 1];
             float2 acc = make_float2(0.f, 0.f);
             for (int j = b; j < e; ++j) {
-                const uint32_t u = ent_s[j];
-                const unsigned ph = (ky * ((u >> 8) & 255u) + kz * (u & 255u)) % (unsigned)N;
-                const float2 z = tws[ph];
+                const uint32_t yz = (ent_s[j] * kyz) >> 16;
+                const unsigned ph = (N & (N - 1)) == 0 ? (yz & (unsigned)(N - 1)) : yz % (unsigned)N;
+                const float2 z = twr[ph * 16 + (l & 15)];
                 if constexpr (WEIGHTED) {
                     const float wj = w_s[j];
                     acc.x = fmaf(wj, z.x, acc.x);

@@ -379,7 +379,8 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G, PencilTraits<N>::MINB) 
 // then the half-spectrum rows along kz are turned into N reals through one
 // N/2-point complex transform each; the plane's KC smallest (value, offset)
 // cells are then selected exactly: the threads' own minima give an upper
-// bound on the KC-th value and only cells at or below it reach a warp top-KC.
+// bound on the KC-th value (bitonic warp sorts and a merge) and only cells at
+// or below it are sorted and merged into the plane's top KC.
 // (FFTW c2r of FFTCorrelator::correlate + CorrelationProcessor::
 // selectIntoQueue, docking_fft.hpp:452-468.)
 // Input layouts: QUAD = false, the FFT pencil stage's [B][N][PP] (each plane

@@ -278,9 +278,10 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G, PencilTraits<N>::MINB) 
     // are consecutive pencils, whose phases for one entry step by its z, so
     // a single table would put lanes on the same banks whenever z is even
     float2* twr = tws + N;                                  // [N][16]
-    int32_t* offs_s = reinterpret_cast<int32_t*>(twr + N * 16);  // [K*N+1]
-    uint32_t* ent_s = reinterpret_cast<uint32_t*>(offs_s + K * N + 1);  // [n_ent]
-    float* w_s = reinterpret_cast<float*>(ent_s + n_ent);                 // [n_ent] (weighted)
+    // entries ([n_ent]; weighted: [n_ent] pairs of entry and weight bits, one
+    // 8-byte broadcast load per entry)
+    uint32_t* ent_s = reinterpret_cast<uint32_t*>(twr + N * 16);
+    int32_t* offs_s = reinterpret_cast<int32_t*>(ent_s + (WEIGHTED ? 2 : 1) * n_ent);  // [K*N+1]
 
     const int q = blockIdx.x;
     const int tile = blockIdx.y;
@@ -298,13 +299,16 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G, PencilTraits<N>::MINB) 
     const int32_t* offs_g = offs + (size_t)q * (K * N + 1);
     for (int i = tid; i <= K * N; i += blockDim.x) offs_s[i] = offs_g[i];
     const uint32_t* ent_g = ent + (size_t)q * n_ent;
+    const float* w_g = WEIGHTED ? ent_w + (size_t)q * n_ent : nullptr;
     for (int i = tid; i < n_ent; i += blockDim.x) {
         const uint32_t u = ent_g[i];
-        ent_s[i] = (((u >> 8) & 255u) << 16) | (u & 255u);
-    }
-    if constexpr (WEIGHTED) {
-        const float* w_g = ent_w + (size_t)q * n_ent;
-        for (int i = tid; i < n_ent; i += blockDim.x) w_s[i] = w_g[i];
+        const uint32_t yz = (((u >> 8) & 255u) << 16) | (u & 255u);
+        if constexpr (WEIGHTED) {
+            ent_s[2 * i] = yz;
+            ent_s[2 * i + 1] = __float_as_uint(w_g[i]);
+        } else {
+            ent_s[i] = yz;
+        }
     }
     __syncthreads();
 
@@ -320,11 +324,19 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G, PencilTraits<N>::MINB) 
             const int b = offs_s[t * N + x], e = offs_s[t * N + x + 1];
             float2 acc = make_float2(0.f, 0.f);
             for (int j = b; j < e; ++j) {
-                const uint32_t yz = (ent_s[j] * kyz) >> 16;
+                uint32_t ej;
+                float wj = 1.f;
+                if constexpr (WEIGHTED) {
+                    const uint2 ew = reinterpret_cast<const uint2*>(ent_s)[j];
+                    ej = ew.x;
+                    wj = __uint_as_float(ew.y);
+                } else {
+                    ej = ent_s[j];
+                }
+                const uint32_t yz = (ej * kyz) >> 16;
                 const unsigned ph = (N & (N - 1)) == 0 ? (yz & (unsigned)(N - 1)) : yz % (unsigned)N;
                 const float2 z = twr[ph * 16 + (l & 15)];
                 if constexpr (WEIGHTED) {
-                    const float wj = w_s[j];
                     acc.x = fmaf(wj, z.x, acc.x);
                     acc.y = fmaf(wj, z.y, acc.y);
                 } else {

@@ -35,7 +35,12 @@ namespace {
 
 typedef unsigned long long u64;
 
-constexpr int kChunk = 16384;  // cells per CTA in the digit and gather passes
+constexpr int kChunk = 16384;  // cells per CTA in the first gather pass
+// cells per CTA in the radix passes and the final gather when a bound exists
+// (only rotations whose gathered set overflowed take that path): a grid of a
+// few CTAs per rotation keeps their mostly idle launches short.  Without a
+// bound every rotation takes the radix path and they use kChunk.
+constexpr int kRadixChunk = 16 * kChunk;
 constexpr int kPassThreads = 256;
 constexpr int kDigitBits = 12;
 constexpr int kMaxPasses = 6;  // 5 x 12 + 4 = 64 key bits
@@ -135,7 +140,8 @@ __global__ void wide_check_kernel(WideState* __restrict__ st, int32_t* __restric
 // histogram of the next digit of the keys inside each active rotation's bin
 __global__ void __launch_bounds__(kPassThreads) wide_digit_kernel(const float* __restrict__ corr, long V,
                                                                   const WideState* __restrict__ st,
-                                                                  uint32_t* __restrict__ hist, float mv) {
+                                                                  uint32_t* __restrict__ hist, float mv,
+                                                                  long chunk) {
     __shared__ uint32_t sh[kWideBins];
     const int q = blockIdx.y;
     const WideState s = st[q];
@@ -147,8 +153,8 @@ __global__ void __launch_bounds__(kPassThreads) wide_digit_kernel(const float* _
     const int shift = rem - bits;
     const u64 want = s.nres ? (s.pfx >> rem) : 0ull;
     const uint32_t dmask = (1u << bits) - 1u;
-    const long c0 = (long)blockIdx.x * kChunk;
-    const long c1 = c0 + kChunk < V ? c0 + kChunk : V;
+    const long c0 = (long)blockIdx.x * chunk;
+    const long c1 = c0 + chunk < V ? c0 + chunk : V;
     const float4* src = reinterpret_cast<const float4*>(corr + (size_t)q * V);
     const int lane = threadIdx.x & 31;
     for (long e4 = c0 / 4 + threadIdx.x; e4 < c1 / 4; e4 += blockDim.x) {
@@ -243,7 +249,7 @@ __global__ void __launch_bounds__(256) wide_pick_kernel(WideState* __restrict__ 
 __global__ void __launch_bounds__(kPassThreads) wide_gather_kernel(const float* __restrict__ corr, long V,
                                                                    const WideState* __restrict__ st,
                                                                    u64* __restrict__ cand, int32_t* __restrict__ cnt,
-                                                                   float mv, int phase) {
+                                                                   float mv, int phase, long chunk) {
     const int q = blockIdx.y;
     const WideState s = st[q];
     const bool radix = (s.flags & kWideRadix) != 0;
@@ -251,8 +257,8 @@ __global__ void __launch_bounds__(kPassThreads) wide_gather_kernel(const float* 
     const bool all = phase == 0 || (s.flags & kWideAll) != 0 || s.nres == 0;
     const int rem = 64 - s.nres;
     const u64 bound = all ? 0ull : (s.pfx >> rem);
-    const long c0 = (long)blockIdx.x * kChunk;
-    const long c1 = c0 + kChunk < V ? c0 + kChunk : V;
+    const long c0 = (long)blockIdx.x * chunk;
+    const long c1 = c0 + chunk < V ? c0 + chunk : V;
     const float4* src = reinterpret_cast<const float4*>(corr + (size_t)q * V);
     u64* out = cand + (size_t)q * kWideMax;
     const int lane = threadIdx.x & 31;
@@ -425,17 +431,19 @@ cudaError_t wide_select_batch(const BatchArgs& a, int N, cudaStream_t s) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const dim3 grid((unsigned)((V + kChunk - 1) / kChunk), (unsigned)nb);
-    wide_gather_kernel<<<grid, kPassThreads, 0, s>>>(w.corr, V, w.st, w.cand, w.cnt, mv, 0);
+    const long rchunk = w.m > N * kPoolPerPlane ? (long)kChunk : (long)kRadixChunk;
+    const dim3 grid_r((unsigned)((V + rchunk - 1) / rchunk), (unsigned)nb);
+    wide_gather_kernel<<<grid, kPassThreads, 0, s>>>(w.corr, V, w.st, w.cand, w.cnt, mv, 0, (long)kChunk);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     wide_check_kernel<<<(nb + 127) / 128, 128, 0, s>>>(w.st, w.cnt, nb);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     for (int p = 0; p < kMaxPasses; ++p) {
-        wide_digit_kernel<<<grid, kPassThreads, 0, s>>>(w.corr, V, w.st, w.hist, mv);
+        wide_digit_kernel<<<grid_r, kPassThreads, 0, s>>>(w.corr, V, w.st, w.hist, mv, rchunk);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         wide_pick_kernel<<<nb, 256, 0, s>>>(w.st, w.hist);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    wide_gather_kernel<<<grid, kPassThreads, 0, s>>>(w.corr, V, w.st, w.cand, w.cnt, mv, 1);
+    wide_gather_kernel<<<grid_r, kPassThreads, 0, s>>>(w.corr, V, w.st, w.cand, w.cnt, mv, 1, rchunk);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const size_t sm = (size_t)kWideMax * sizeof(u64);
     e = cudaFuncSetAttribute((const void*)wide_finish_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);

@@ -390,6 +390,9 @@ def run_ours(args):
                                    "of 128x128x16 per 128-rotation group (W = %d)" % info["window_w"],
                     "hbm_reference_schedule": {"achieved": alg_gbs, "peak": peak_gbs, "unit": "GB/s",
                                                "frac": alg_gbs / peak_gbs},
+                    "limiter": "shared-memory bandwidth: the MMAs' operand reads (8 KB per 128x128x16 MMA) "
+                               "and the producers' loads and stores share the SM's 128 B per clock "
+                               "(profiles/pencil_tc_shape_ace128.md)",
                     "kernel_share": share}
     else:
         rot_per_launch = n_rot * args.steps / max(launches, 1)

@@ -34,11 +34,13 @@
 // table (scaled by the F scale) is replicated per lane ([phase][lane]) so
 // that the 32 lanes' lookups never share a bank.
 //
-// CTA (288 threads): eight producer warps (two threads per rotation) and an
-// MMA-issuing warp; the producers fill the next term's tiles only after the
-// tensor core has read the current ones, so two CTAs share an SM (shared
-// memory and 2 x 256 TMEM columns permitting) and overlap each other's MMAs
-// and production.  All waits are bounded; a timeout is reported through *err.
+// CTA (256 threads): eight producer warps (two threads per rotation); thread
+// 0 also issues each term's MMAs once every producer has arrived.  The
+// producers fill the next term's tiles only after the tensor core has read
+// the current ones, so two CTAs share an SM (shared memory and 2 x 256 TMEM
+// columns permitting) and overlap each other's MMAs and production; 16 warps
+// per SM leave 128 registers per thread.  All waits are bounded; a timeout is
+// reported through *err.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -50,7 +52,7 @@
 namespace fftdock {
 
 constexpr int TC_ROT = kTcRot;              // rotations per CTA (MMA N)
-constexpr int TC_THREADS = 288;             // 8 producer warps + the MMA warp
+constexpr int TC_THREADS = 256;             // 8 producer warps; thread 0 also issues the MMAs
 constexpr uint32_t TC_LBO = 128, TC_SBO = 256;
 constexpr uint32_t TC_FTILE = 128 * 16 * 2;       // one 128 x 16 FP16 tile (hi or lo)
 constexpr uint32_t TC_FCHUNK = 2 * TC_FTILE;      // hi + lo of one window chunk
@@ -240,42 +242,32 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
     const uint32_t fb = tc::smem_u32(fbuf);
     const uint32_t ab = tc::smem_u32(abuf);
 
-    if (warp == 8) {
-        // ---------------- MMA issuer ----------------
-        if (lane == 0) {
-            const uint32_t idesc = tc::idesc_f16_f32(128, TC_ROT);
-            const uint32_t d_re = tmem, d_im = tmem + TC_ROT;
-            for (int k = 0; k < Ka; ++k) {
-                if (*(volatile int*)&abort_flag) break;
-                if (!tc::mbar_wait(&full_bar, (uint32_t)(k & 1), TC_WAIT_NS)) {
-                    atomicOr(err, 1);
-                    abort_flag = 1;
-                    break;
-                }
-                tc::fence_after_sync();
-                for (int c = 0; c < NC; ++c) {
-                    const uint32_t ao = (uint32_t)(NC - 1 - c) * TC_SBO;
-                    const uint64_t cre_h = tc::smem_desc(ab + 0 * RG * 256 + ao, TC_LBO, TC_SBO);
-                    const uint64_t cre_l = tc::smem_desc(ab + 1 * RG * 256 + ao, TC_LBO, TC_SBO);
-                    const uint64_t cim_h = tc::smem_desc(ab + 2 * RG * 256 + ao, TC_LBO, TC_SBO);
-                    const uint64_t cim_l = tc::smem_desc(ab + 3 * RG * 256 + ao, TC_LBO, TC_SBO);
-                    const uint64_t f_h = tc::smem_desc(fb + c * TC_FCHUNK, TC_LBO, TC_SBO);
-                    const uint64_t f_l = tc::smem_desc(fb + c * TC_FCHUNK + TC_FTILE, TC_LBO, TC_SBO);
-                    const uint32_t acc = (k == 0 && c == 0) ? 0u : 1u;
-                    tc::mma_f16(d_re, cre_h, f_h, idesc, acc);
-                    tc::mma_f16(d_re, cre_h, f_l, idesc, 1u);
-                    tc::mma_f16(d_re, cre_l, f_h, idesc, 1u);
-                    tc::mma_f16(d_im, cim_h, f_h, idesc, acc);
-                    tc::mma_f16(d_im, cim_h, f_l, idesc, 1u);
-                    tc::mma_f16(d_im, cim_l, f_h, idesc, 1u);
-                }
-                tc::mma_commit(&empty_bar);
-            }
-            // arrives when every MMA issued above has completed
-            tc::mma_commit(&done_bar);
+    // MMA issue for term k (thread 0, after the producers' arrivals): 6 MMAs
+    // per window chunk into the real and imaginary accumulators, then a
+    // commit that arrives on empty_bar once they have read the tiles
+    const uint32_t idesc = tc::idesc_f16_f32(128, TC_ROT);
+    auto issue_term = [&](int k) {
+        const uint32_t d_re = tmem, d_im = tmem + TC_ROT;
+        for (int c = 0; c < NC; ++c) {
+            const uint32_t ao = (uint32_t)(NC - 1 - c) * TC_SBO;
+            const uint64_t cre_h = tc::smem_desc(ab + 0 * RG * 256 + ao, TC_LBO, TC_SBO);
+            const uint64_t cre_l = tc::smem_desc(ab + 1 * RG * 256 + ao, TC_LBO, TC_SBO);
+            const uint64_t cim_h = tc::smem_desc(ab + 2 * RG * 256 + ao, TC_LBO, TC_SBO);
+            const uint64_t cim_l = tc::smem_desc(ab + 3 * RG * 256 + ao, TC_LBO, TC_SBO);
+            const uint64_t f_h = tc::smem_desc(fb + c * TC_FCHUNK, TC_LBO, TC_SBO);
+            const uint64_t f_l = tc::smem_desc(fb + c * TC_FCHUNK + TC_FTILE, TC_LBO, TC_SBO);
+            const uint32_t acc = (k == 0 && c == 0) ? 0u : 1u;
+            tc::mma_f16(d_re, cre_h, f_h, idesc, acc);
+            tc::mma_f16(d_re, cre_h, f_l, idesc, 1u);
+            tc::mma_f16(d_re, cre_l, f_h, idesc, 1u);
+            tc::mma_f16(d_im, cim_h, f_h, idesc, acc);
+            tc::mma_f16(d_im, cim_h, f_l, idesc, 1u);
+            tc::mma_f16(d_im, cim_l, f_h, idesc, 1u);
         }
-        __syncwarp();
-    } else {
+        tc::mma_commit(&empty_bar);
+    };
+
+    {
         // ---------------- producers: thread (r, half) ----------------
         const int r = tid & 127;
         const int half = tid >> 7;
@@ -390,8 +382,19 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
             }
             tc::fence_proxy_async_smem();
             tc::mbar_arrive(&full_bar);
+            if (tid == 0 && !*(volatile int*)&abort_flag) {
+                if (!tc::mbar_wait(&full_bar, (uint32_t)(k & 1), TC_WAIT_NS)) {
+                    atomicOr(err, 1);
+                    abort_flag = 1;
+                } else {
+                    tc::fence_after_sync();
+                    issue_term(k);
+                }
+            }
             if (k + 1 < Ka) preload(k + 1);
         }
+        // arrives when every MMA issued above has completed
+        if (tid == 0) tc::mma_commit(&done_bar);
         // ---- epilogue: TMEM -> x-quads g2t[rot][x/4][p][x%4] (a warp store fills 8 sectors) ----
         if (!*(volatile int*)&abort_flag && !tc::mbar_wait(&done_bar, 0, TC_WAIT_NS)) {
             atomicOr(err, 4);
@@ -420,7 +423,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
         }
     }
     // the MMA issuer's done barrier covers every MMA before TMEM is released
-    if (warp == 8 && lane == 0 && !tc::mbar_wait(&done_bar, 0, TC_WAIT_NS)) atomicOr(err, 16);
+    if (tid == 0 && !tc::mbar_wait(&done_bar, 0, TC_WAIT_NS)) atomicOr(err, 16);
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, 256);

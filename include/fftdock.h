@@ -74,8 +74,12 @@ enum {
  * edges <= 128, unweighted term sets) restates the stage as a circular
  * correlation along x computed with split-FP16 tcgen05 GEMMs (hi*hi + hi*lo
  * + lo*hi, FP32 accumulate) over ligand bins summed on the CUDA cores; the
- * scan then takes rotations in groups of 128 (rot_batch is rounded up).  Its
- * FP32 candidate values carry up to a few 1e-4 relative error (FFT: ~2e-5);
+ * scan then takes rotations in groups of 128 (rot_batch is rounded up).  The
+ * tensor core's FP32 accumulation error grows with the chain of MMAs into one
+ * accumulator, so the accumulator restarts every tc_terms_per_sum terms and
+ * the groups are summed in FP32 with round-to-nearest: with the default 6 the
+ * FP32 candidate values stay within 1e-4 relative of FP64 (measured 8.4e-5
+ * at 128^3 with 18 terms; one group of all 18 terms: 2.3e-4; FFT: 3.8e-5);
  * reported scores are FP64 direct-space energies either way.  AUTO = TENSOR
  * where it applies (grid edge <= 128, FP32 spectra, an unweighted term set
  * with at least 4 terms: at 64^3 with the single shape term the FFT form is
@@ -130,7 +134,12 @@ typedef struct fftdock_config {
     int32_t lj_mix;              /* LJ term sets: sigma combination rule (PotentialsT::LJ_MIX_0 = 0:
                                     arithmetic, LJ_MIX_1 = 1: geometric; ljComp requires 1) */
     double lj_cut;               /* LJ term sets: field cutoff ("cutOffFft"), grid length units */
+    int32_t tc_terms_per_sum;    /* tensor pencil stage: terms accumulated in tensor memory before each
+                                    group's sum is added into the FP32 result (round to nearest); the
+                                    tensor core's own accumulation error grows with this chain length.
+                                    0 = the library default (FFTDOCK_TC_TERMS_PER_SUM_DEFAULT) */
 } fftdock_config;
+#define FFTDOCK_TC_TERMS_PER_SUM_DEFAULT 6
 
 /* one selected translation; the reference's TranValue
  * (include/PRODDL/types.hpp:68-84) plus the rotation id and the raw
@@ -202,13 +211,17 @@ int fftdock_scan_device(fftdock_ctx* ctx, int32_t n_rot, const double* d_rot, in
  * cannot allocate at scan time: a host whose memory pool already owns the
  * GPU, or a pipeline that forbids allocation once running.  Same arguments
  * and results as fftdock_scan_device, but the per-batch work memory lives in
- * one 16 MiB array compiled into the library (one per GPU, kept until the
- * process exits) instead of the context's buffers; the context must already
- * hold a receptor and a ligand.  Batches shrink to fit the array; a context
+ * one 16 MiB array compiled into the library instead of the context's
+ * buffers; the context must already hold a receptor and a ligand.  The array
+ * exists once per CUDA context that loads the library (for this library's
+ * contexts: the primary context of their device) and stays until that
+ * context ends.  fftdock_create commits it on the device and looks up its
+ * address, so the scan call itself allocates nothing and looks nothing up;
+ * create contexts at start-up, before the host's pool takes the GPU and
+ * before any stream capture.  Batches shrink to fit the array; a context
  * whose single rotation needs more than 16 MiB is rejected with
- * FFTDOCK_EINVAL.  The first call on a device looks up the array's device
- * address, so make it before any stream capture.  All calls share the array:
- * calls whose GPU work overlaps race and must be serialised by the caller. */
+ * FFTDOCK_EINVAL.  All calls in one CUDA context share the array: calls whose
+ * GPU work overlaps race and must be serialised by the caller. */
 int fftdock_scan_device_noalloc(fftdock_ctx* ctx, int32_t n_rot, const double* d_rot, int32_t first_rot_id,
                                 fftdock_peak* d_peaks, int32_t* d_n_peaks, void* stream);
 

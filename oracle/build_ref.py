@@ -7,20 +7,34 @@ oracle/_ref (test infrastructure; never part of the product).
   points.  The rest of the reference needs FFTW3, Blitz++, Boost and HDF5 and
   is not built.
 
-Runs only where the reference tree exists; elsewhere it does nothing.
+The reference tree is taken from the FFTDOCK_REFERENCE_DIR environment
+variable or the ``reference`` argument of build(), else from the checkout
+beside this repository (../reference).  Runs only where that tree exists;
+elsewhere it does nothing.
 """
 from __future__ import annotations
 
+import os
 import shutil
 import subprocess
+import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-REFERENCE = Path("/root/reference")
 
 
-def build(verbose=False):
+def reference_dir(reference=None):
+    if reference:
+        return Path(reference)
+    env = os.environ.get("FFTDOCK_REFERENCE_DIR")
+    if env:
+        return Path(env)
+    return HERE.parent.parent / "reference"
+
+
+def build(verbose=False, reference=None):
+    REFERENCE = reference_dir(reference)
     srcs = [REFERENCE / "src/PRODDL/External/Gdiam/gdiam.cpp", REFERENCE / "src/PRODDL/Geom/gdiam_simple.cpp"]
     if not all(p.exists() for p in srcs):
         return None
@@ -43,4 +57,4 @@ def build(verbose=False):
 
 
 if __name__ == "__main__":
-    print(build(verbose=True))
+    print(build(verbose=True, reference=sys.argv[1] if len(sys.argv) > 1 else None))

@@ -66,6 +66,7 @@ class Config(C.Structure):
         ("cluster_radius", C.c_double),
         ("lj_mix", C.c_int32),
         ("lj_cut", C.c_double),
+        ("tc_terms_per_sum", C.c_int32),
     ]
 
 

@@ -161,9 +161,10 @@ template <int N> struct SizeOpsImpl {
                 const size_t smt = tc_smem_bytes(N, a.W / 8, a.n_tc_terms);
                 if ((e = set_smem((const void*)pencil_tc_kernel<N>, smt)) != cudaSuccess) return e;
                 dim3 gridt(N * H, (nb + TC_ROT - 1) / TC_ROT);
+                const int tg = a.tc_group > 0 ? a.tc_group : FFTDOCK_TC_TERMS_PER_SUM_DEFAULT;
                 pencil_tc_kernel<N><<<gridt, TC_THREADS, smt, s>>>(a.circ, a.cscale, a.ent_t, a.tinfo,
                                                                   a.n_tc_terms, a.tw32, a.g2t, a.n_pad, nb, a.x0,
-                                                                  a.W, a.err);
+                                                                  a.W, tg, a.err);
                 if ((e = cudaGetLastError()) != cudaSuccess) return e;
             }
         }
@@ -217,9 +218,21 @@ template <int N> struct SizeOpsImpl {
         return finish(a, s);
     }
 
+    // cudaFuncGetAttributes loads a kernel's code under lazy module loading
+    static cudaError_t load_fft_form(int spec_bf16) {
+        cudaFuncAttributes fa;
+        cudaError_t e = cudaFuncGetAttributes(&fa, (const void*)ligand_prep_kernel<N>);
+        if (e == cudaSuccess)
+            e = spec_bf16 ? cudaFuncGetAttributes(&fa, (const void*)pencil_kernel<N, __nv_bfloat162, false>)
+                          : cudaFuncGetAttributes(&fa, (const void*)pencil_kernel<N, float2, false>);
+        if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)plane_kernel<N, false, false>);
+        if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)finalize_kernel<N>);
+        return e;
+    }
+
     static const SizeOps* ops() {
         static const SizeOps o{N, &receptor_fft, &circ_scales, kHasTc, &scan_batch, &pencil_smem, &prep, &middle,
-                               &finish};
+                               &finish, &load_fft_form};
         return &o;
     }
 };

@@ -96,6 +96,9 @@ struct fftdock_ctx {
     int32_t* tpad = nullptr;     // [K] padded start - start per term
     int n_tc_terms = 0, n_pad = 0;
 
+    // the no-allocation scan's work array, resolved at creation
+    void* noalloc_scratch = nullptr;
+
     // queue + clustering path (cfg.cluster_trans)
     fftdock::WideArgs wide{};
 
@@ -205,6 +208,7 @@ BatchArgs batch_args(fftdock_ctx* ctx) {
     a.tinfo = ctx->tinfo;
     a.tpad = ctx->tpad;
     a.n_tc_terms = ctx->n_tc_terms;
+    a.tc_group = ctx->cfg.tc_terms_per_sum;
     a.n_pad = ctx->n_pad;
     a.err = ctx->err_dev;
     a.wide = ctx->wide;
@@ -395,6 +399,7 @@ int ctx_scan_inputs(fftdock_ctx* ctx, ScanInputs* in) {
     in->PP = ctx->PP;
     in->B = ctx->B;
     in->n_ent = ctx->n_ent;
+    in->noalloc_scratch = ctx->noalloc_scratch;
     return FFTDOCK_OK;
 }
 
@@ -530,6 +535,8 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
     if (std::isnan(c.max_val_corr)) return fail(ctx, FFTDOCK_EINVAL, "max_val_corr is NaN");
     if (c.pencil_mode < FFTDOCK_PENCIL_AUTO || c.pencil_mode > FFTDOCK_PENCIL_TENSOR)
         return fail(ctx, FFTDOCK_EINVAL, "unknown pencil_mode");
+    if (c.tc_terms_per_sum < 0 || c.tc_terms_per_sum > fftdock::kTcMaxTerms)
+        return fail(ctx, FFTDOCK_EINVAL, "tc_terms_per_sum must be in [0, 64]");
     if (c.pencil_mode == FFTDOCK_PENCIL_TENSOR && !ctx->ops->has_tc)
         return fail(ctx, FFTDOCK_EUNSUPPORTED, "the tensor-core pencil stage covers grid edges up to 128");
     // AUTO runs the tensor form where it applies (faster at 128^3 with 18
@@ -597,13 +604,18 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0) return fail(ctx, FFTDOCK_ECUDA, "no CUDA device available");
     if (c.device < 0 || c.device >= ndev) return fail(ctx, FFTDOCK_EINVAL, "device ordinal out of range");
-    CK(cudaSetDevice(c.device));
+    fftdock::DeviceScope dev_scope(c.device);
+    CK(dev_scope.status());
     cudaDeviceProp prop;
     CK(cudaGetDeviceProperties(&prop, c.device));
     if (prop.major != 10 || prop.minor != 3)
         return fail(ctx, FFTDOCK_EUNSUPPORTED, std::string("libfftdock is built for sm_103a only; device is ") +
                                                    prop.name);
     CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    // commit the no-allocation scan's array and load the kernels it runs now,
+    // so that its calls allocate nothing
+    CK(fftdock::noalloc_scratch_address(&ctx->noalloc_scratch));
+    CK(ctx->ops->load_fft_form(c.precision == FFTDOCK_PREC_BF16_SPECTRA ? 1 : 0));
 
     std::vector<float2> tw32(N);
     std::vector<double2> tw64(N);
@@ -668,7 +680,8 @@ int fftdock_set_receptor(fftdock_ctx* ctx, int32_t n, const double* xyz, const i
         for (int i = 0; i < n; ++i)
             if (type[i] < 0 || type[i] >= c.n_types) return fail(ctx, FFTDOCK_EINVAL, "receptor type out of range");
     }
-    CK(cudaSetDevice(c.device));
+    fftdock::DeviceScope dev_scope(c.device);
+    CK(dev_scope.status());
     ctx->have_rec = false;
     const int N = ctx->N;
     const size_t V = ctx->V;
@@ -787,7 +800,8 @@ int fftdock_set_ligand(fftdock_ctx* ctx, int32_t n, const double* xyz, const int
     }
     if (ctx->ops->pencil_smem(ctx->K, n) > fftdock::kMaxSmem)
         return fail(ctx, FFTDOCK_EINVAL, "ligand too large for the pencil kernel's shared memory");
-    CK(cudaSetDevice(c.device));
+    fftdock::DeviceScope dev_scope(c.device);
+    CK(dev_scope.status());
     ctx->have_lig = false;
     CK(cudaStreamSynchronize(ctx->stream));
     dfree(ctx->lig_xyz);
@@ -907,7 +921,8 @@ int fftdock_set_pair_lj(fftdock_ctx* ctx, int32_t n_rec, const double* rec_xyz, 
             p[4] = gshift;
         }
     }
-    CK(cudaSetDevice(c.device));
+    fftdock::DeviceScope dev_scope(c.device);
+    CK(dev_scope.status());
     ctx->have_rec = ctx->have_lig = false;
     CK(cudaStreamSynchronize(ctx->stream));
     const int N = ctx->N;
@@ -1037,7 +1052,8 @@ int fftdock_scan(fftdock_ctx* ctx, int32_t n_rot, const double* rot, int32_t fir
     if (rc) return rc;
     if (n_rot < 0 || (n_rot > 0 && (!rot || !peaks || !n_peaks))) return fail(ctx, FFTDOCK_EINVAL, "bad arguments");
     if (n_rot == 0) return FFTDOCK_OK;
-    CK(cudaSetDevice(ctx->cfg.device));
+    fftdock::DeviceScope dev_scope(ctx->cfg.device);
+    CK(dev_scope.status());
     if ((rc = grow_call_buffers(ctx, n_rot))) return rc;
     cudaStream_t s = ctx->stream;
     const int P = ctx->cfg.peaks_per_rot;
@@ -1065,7 +1081,8 @@ int fftdock_scan_device(fftdock_ctx* ctx, int32_t n_rot, const double* d_rot, in
     if (rc) return rc;
     if (n_rot < 0 || (n_rot > 0 && (!d_rot || !d_peaks || !d_n_peaks))) return fail(ctx, FFTDOCK_EINVAL, "bad arguments");
     if (n_rot == 0) return FFTDOCK_OK;
-    CK(cudaSetDevice(ctx->cfg.device));
+    fftdock::DeviceScope dev_scope(ctx->cfg.device);
+    CK(dev_scope.status());
     if ((rc = grow_status(ctx, n_rot))) return rc;
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
     return run_batches(ctx, n_rot, d_rot, first_rot_id, d_peaks, d_n_peaks, ctx->status_dev, s, nullptr, nullptr,
@@ -1076,7 +1093,8 @@ int fftdock_get_receptor_grid(fftdock_ctx* ctx, int32_t term, double* out) {
     if (!ctx || !out) return FFTDOCK_EINVAL;
     if (!ctx->have_rec) return fail(ctx, FFTDOCK_ESTATE, "fftdock_set_receptor has not been called");
     if (term < 0 || term >= ctx->K) return fail(ctx, FFTDOCK_EINVAL, "term out of range");
-    CK(cudaSetDevice(ctx->cfg.device));
+    fftdock::DeviceScope dev_scope(ctx->cfg.device);
+    CK(dev_scope.status());
     CK(cudaStreamSynchronize(ctx->stream));
     CK(cudaMemcpy(out, ctx->rgrid + (size_t)term * ctx->V, ctx->V * sizeof(double), cudaMemcpyDeviceToHost));
     return FFTDOCK_OK;
@@ -1086,7 +1104,8 @@ int fftdock_correlation_grid(fftdock_ctx* ctx, const double* rot, float* out) {
     int rc = check_ready(ctx);
     if (rc) return rc;
     if (!rot || !out) return fail(ctx, FFTDOCK_EINVAL, "bad arguments");
-    CK(cudaSetDevice(ctx->cfg.device));
+    fftdock::DeviceScope dev_scope(ctx->cfg.device);
+    CK(dev_scope.status());
     if ((rc = grow_call_buffers(ctx, 1))) return rc;
     cudaStream_t s = ctx->stream;
     float* dbg = nullptr;
@@ -1109,7 +1128,8 @@ int fftdock_scan_candidates(fftdock_ctx* ctx, int32_t n_rot, const double* rot, 
     if (n_rot < 1 || !rot || !values || !offsets) return fail(ctx, FFTDOCK_EINVAL, "bad arguments");
     if (ctx->wide.corr)
         return fail(ctx, FFTDOCK_EUNSUPPORTED, "a clustering context keeps no per-plane candidate pools");
-    CK(cudaSetDevice(ctx->cfg.device));
+    fftdock::DeviceScope dev_scope(ctx->cfg.device);
+    CK(dev_scope.status());
     if ((rc = grow_call_buffers(ctx, n_rot))) return rc;
     cudaStream_t s = ctx->stream;
     float* pv = nullptr;
@@ -1151,7 +1171,8 @@ int fftdock_get_kernel_stats(fftdock_ctx* ctx, fftdock_kernel_stats* out) {
     if (!ctx || !out) return FFTDOCK_EINVAL;
     std::memset(out, 0, sizeof(*out));
     if (ctx->ev_used == 0) return FFTDOCK_OK;
-    CK(cudaSetDevice(ctx->cfg.device));
+    fftdock::DeviceScope dev_scope(ctx->cfg.device);
+    CK(dev_scope.status());
     CK(cudaEventSynchronize(ctx->ev_pool[ctx->ev_used - 1]));
     for (const auto& r : ctx->ev_recs) {
         float ms = 0.f;

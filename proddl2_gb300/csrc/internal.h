@@ -11,6 +11,29 @@
 
 namespace fftdock {
 
+// Makes a context's device current for one entry point and puts the caller's
+// current device back when the entry point returns, so that no call leaves
+// the library's device selected on the calling thread (nothing is restored
+// when the two are the same device).
+class DeviceScope {
+  public:
+    explicit DeviceScope(int device) : dev_(device) {
+        if (cudaGetDevice(&prev_) != cudaSuccess) prev_ = -1;
+        err_ = prev_ == device ? cudaSuccess : cudaSetDevice(device);
+    }
+    ~DeviceScope() {
+        if (prev_ >= 0 && prev_ != dev_) cudaSetDevice(prev_);
+    }
+    DeviceScope(const DeviceScope&) = delete;
+    DeviceScope& operator=(const DeviceScope&) = delete;
+    cudaError_t status() const { return err_; }
+
+  private:
+    int dev_;
+    int prev_ = -1;
+    cudaError_t err_ = cudaSuccess;
+};
+
 // pencils per x-plane, N (N/2 + 1), rounded up to whole 32-lane tiles
 __host__ __device__ constexpr int pencil_pitch(int n) { return (n * (n / 2 + 1) + 31) / 32 * 32; }
 
@@ -152,6 +175,7 @@ struct BatchArgs {
     const int32_t* tinfo;       // padded entry starts of the n_tc_terms non-empty terms, then their term ids
     const int32_t* tpad;        // [K] padded start - start of each term's entries
     int n_tc_terms;
+    int tc_group;               // terms per tensor-memory sum (<= 0: FFTDOCK_TC_TERMS_PER_SUM_DEFAULT)
     int n_pad;                  // entries per rotation with every term padded to a multiple of 8
     int* err;                   // device word: nonzero after a pipeline timeout
     WideArgs wide;              // queue + clustering path (wide.corr != nullptr)
@@ -198,6 +222,10 @@ struct SizeOps {
     cudaError_t (*prep)(const BatchArgs& a, cudaStream_t s);
     cudaError_t (*middle)(const BatchArgs& a, cudaStream_t s);
     cudaError_t (*finish)(const BatchArgs& a, cudaStream_t s);
+    // load the code of the FFT-form kernels (the ones the no-allocation scan
+    // runs) into the current CUDA context, so that their first launch loads
+    // nothing
+    cudaError_t (*load_fft_form)(int spec_bf16);
 };
 
 const SizeOps* size_ops(int n);
@@ -210,8 +238,13 @@ struct ScanInputs {
     int device;
     cudaStream_t stream;
     int N, K, PP, B, n_ent;
+    void* noalloc_scratch;  // the no-allocation scan's array in the context's CUDA context
 };
 int ctx_scan_inputs(fftdock_ctx* ctx, ScanInputs* in);
+// Device address, in the current CUDA context, of the no-allocation scan's
+// work array (noalloc.cu); resolving it loads the library's module for that
+// file, which commits the array on the device.  Called by fftdock_create.
+cudaError_t noalloc_scratch_address(void** addr);
 int ctx_fail(fftdock_ctx* ctx, int code, const char* msg);
 
 }  // namespace fftdock

@@ -9,17 +9,20 @@
 // same kernels with that work memory in one fixed-size array compiled into
 // this library instead.
 //
-// The array (kScratchBytes, 16 MiB) exists once per GPU that loads the
-// library and lives until the process exits.  Its device address is looked up
-// with cudaGetSymbolAddress the first time the entry point runs on a device,
-// with that device current; do that first call before any stream capture.
-// Every call uses the same array and nothing in it needs to start at zero
-// (each batch writes every word it later reads), so calls whose GPU work
-// overlaps -- on two streams, or from two contexts on one device -- race and
-// must be serialised by the caller.
+// The array (kScratchBytes, 16 MiB) exists once per CUDA context that loads
+// this file's module (for the library's contexts: the primary context of
+// their device) and lives until that context ends.  Its address in the
+// current context is resolved by noalloc_scratch_address(), which
+// fftdock_create calls with the context's device current: resolving it loads
+// the module, which is when the driver commits the array on the device.  So
+// the scan call itself neither allocates nor looks anything up; callers
+// create their contexts at start-up, before their own pool takes the GPU and
+// before any stream capture.  Every call uses the same array and nothing in it
+// needs to start at zero (each batch writes every word it later reads), so
+// calls whose GPU work overlaps -- on two streams, or from two library
+// contexts in one CUDA context -- race and must be serialised by the caller.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "fftdock.h"
@@ -29,12 +32,8 @@ namespace {
 
 constexpr size_t kScratchBytes = size_t(16) << 20;
 constexpr int kKC = 16;
-constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_scan_scratch[kScratchBytes];
-
-std::mutex g_scratch_mu;
-void* g_scratch_addr[kMaxDevices] = {};
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -51,6 +50,22 @@ size_t scratch_bytes(const fftdock::ScanInputs& in, int b) {
 }
 
 }  // namespace
+
+namespace fftdock {
+
+// The host-side name g_scan_scratch stands for the array but is not its
+// device address; kernels get the address resolved here.
+cudaError_t noalloc_scratch_address(void** addr) {
+    *addr = nullptr;
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_scan_scratch);
+    if (e != cudaSuccess) return e;
+    if (!p) return cudaErrorInvalidSymbol;
+    *addr = p;
+    return cudaSuccess;
+}
+
+}  // namespace fftdock
 
 extern "C" int fftdock_scan_device_noalloc(fftdock_ctx* ctx, int32_t n_rot, const double* d_rot,
                                            int32_t first_rot_id, fftdock_peak* d_peaks, int32_t* d_n_peaks,
@@ -69,29 +84,18 @@ extern "C" int fftdock_scan_device_noalloc(fftdock_ctx* ctx, int32_t n_rot, cons
         return fftdock::ctx_fail(ctx, FFTDOCK_EUNSUPPORTED,
                                  "translational clustering needs a full correlation grid per rotation; the "
                                  "no-allocation scan does not cover it");
-    if (in.device < 0 || in.device >= kMaxDevices)
-        return fftdock::ctx_fail(ctx, FFTDOCK_EINVAL, "device ordinal beyond the no-allocation scan's table");
     if (scratch_bytes(in, 1) > kScratchBytes) {
         const std::string msg = "one rotation of this context needs " + std::to_string(scratch_bytes(in, 1)) +
                                 " bytes of work memory; the no-allocation scan has " +
                                 std::to_string(kScratchBytes);
         return fftdock::ctx_fail(ctx, FFTDOCK_EINVAL, msg.c_str());
     }
-    cudaError_t e = cudaSetDevice(in.device);
+    if (!in.noalloc_scratch)
+        return fftdock::ctx_fail(ctx, FFTDOCK_ECUDA, "the no-allocation scan's array was not resolved");
+    fftdock::DeviceScope dev_scope(in.device);
+    cudaError_t e = dev_scope.status();
     if (e != cudaSuccess) return fftdock::ctx_fail(ctx, FFTDOCK_ECUDA, cudaGetErrorString(e));
-    unsigned char* base = nullptr;
-    {
-        std::lock_guard<std::mutex> lock(g_scratch_mu);
-        if (!g_scratch_addr[in.device]) {
-            void* p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_scan_scratch);
-            if (e != cudaSuccess || !p)
-                return fftdock::ctx_fail(ctx, FFTDOCK_ECUDA,
-                                         (std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e)).c_str());
-            g_scratch_addr[in.device] = p;
-        }
-        base = static_cast<unsigned char*>(g_scratch_addr[in.device]);
-    }
+    unsigned char* base = static_cast<unsigned char*>(in.noalloc_scratch);
     int b = in.B;
     while (b > 1 && scratch_bytes(in, b) > kScratchBytes) --b;
 

@@ -677,7 +677,8 @@ int fftdock_scan_pairs(const fftdock_config* cfg, int32_t n_pairs, const fftdock
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(FFTDOCK_ECUDA, "no CUDA device available");
     if (c.device < 0 || c.device >= ndev) return fail(FFTDOCK_EINVAL, "device ordinal out of range");
-    PCK(cudaSetDevice(c.device));
+    fftdock::DeviceScope dev_scope(c.device);
+    PCK(dev_scope.status());
     cudaDeviceProp prop;
     PCK(cudaGetDeviceProperties(&prop, c.device));
     if (prop.major != 10 || prop.minor != 3)

@@ -12,7 +12,12 @@
 // run on the tensor cores as real M = 128 (x) x N = 128 (r) x K = 16 MMAs,
 // D_re and D_im in tensor memory.  FP32 accuracy comes from splitting each
 // operand into FP16 hi + lo parts and accumulating hi*hi + hi*lo + lo*hi;
-// per-pencil power-of-two scales keep both parts in the normal range.
+// per-pencil power-of-two scales keep both parts in the normal range.  The
+// tensor core's FP32 accumulation does not round to nearest, and its error
+// grows with the length of the chain of MMAs into one accumulator (270 at
+// 18 terms and a 40-cell window), so the accumulator is restarted every `tg`
+// terms and each group's sum is added in FP32 (round to nearest) into the
+// output, which holds the running sum between groups.
 //
 // Operands.  C is Toeplitz: the tile of window chunk n0 = 8c is
 //   C_c[x][i] = c_t((x0 + 8c + i - x) mod N) = E[x + W - 8 - 8c][i],
@@ -188,7 +193,7 @@ template <int N>
 __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
     const float2* __restrict__ circ, const int8_t* __restrict__ cscale, const uint32_t* __restrict__ ent_t,
     const int32_t* __restrict__ tinfo, int Ka, const float2* __restrict__ tw, float2* __restrict__ g2t, int n_pad,
-    int n_rot, int x0, int W, int* __restrict__ err) {
+    int n_rot, int x0, int W, int tg, int* __restrict__ err) {
     static_assert(N <= 128, "the tensor pencil stage covers x in one 128-row tile");
     constexpr int H = N / 2 + 1;
     constexpr int NH = N * H;
@@ -256,7 +261,8 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
             const uint64_t cim_l = tc::smem_desc(ab + 3 * RG * 256 + ao, TC_LBO, TC_SBO);
             const uint64_t f_h = tc::smem_desc(fb + c * TC_FCHUNK, TC_LBO, TC_SBO);
             const uint64_t f_l = tc::smem_desc(fb + c * TC_FCHUNK + TC_FTILE, TC_LBO, TC_SBO);
-            const uint32_t acc = (k == 0 && c == 0) ? 0u : 1u;
+            // each group of tg terms starts a fresh accumulator
+            const uint32_t acc = (k % tg == 0 && c == 0) ? 0u : 1u;
             tc::mma_f16(d_re, cre_h, f_h, idesc, acc);
             tc::mma_f16(d_re, cre_h, f_l, idesc, 1u);
             tc::mma_f16(d_re, cre_l, f_h, idesc, 1u);
@@ -265,6 +271,42 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
             tc::mma_f16(d_im, cim_l, f_h, idesc, 1u);
         }
         tc::mma_commit(&empty_bar);
+    };
+
+    // TMEM -> x-quads g2t[rot][x/4][p][x%4] (a warp access covers 8 whole
+    // sectors): thread (warp, lane) holds output row x = 32 (warp % 4) +
+    // lane of the rotations [64 half, 64 half + 64).  The first group is
+    // stored; every later group is added with fire-and-forget FP32 atomic
+    // adds (round to nearest, performed in L2), so no thread waits for the
+    // running sum.  All accesses to one element come from one thread in
+    // program order, which fixes the order of the additions: the result is
+    // the same in every run.
+    const float inv = 1.0f / (c_scale * TC_F_SCALE);
+    auto drain = [&](bool first) {
+        const int xo = 32 * (warp & 3) + lane;  // TMEM lane = output row x
+        const uint32_t trow = (uint32_t)(32 * (warp & 3)) << 16;
+        const int half = tid >> 7;
+#pragma unroll 1
+        for (int cb = 0; cb < 4; ++cb) {
+            const int c0 = half * 64 + cb * 16;
+            uint32_t dre[16], dim[16];
+            tc::tmem_ld_32x32b_x16(tmem + trow + c0, dre);
+            tc::tmem_ld_32x32b_x16(tmem + trow + TC_ROT + c0, dim);
+            tc::tmem_wait_ld();
+            if (xo < N) {
+                float2* ob = g2t + (size_t)(g * TC_ROT + c0) * NH * N + (size_t)(xo >> 2) * NH * 4 + (size_t)p * 4 +
+                             (xo & 3);
+                const int nj = min(16, n_rot - (g * TC_ROT + c0));
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const float2 v = make_float2(__uint_as_float(dre[j]) * inv, __uint_as_float(dim[j]) * inv);
+                    if (j < nj) {
+                        if (first) ob[(size_t)j * NH * N] = v;
+                        else atomicAdd(ob + (size_t)j * NH * N, v);
+                    }
+                }
+            }
+        }
     };
 
     {
@@ -300,6 +342,14 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
                 !tc::mbar_wait(&empty_bar, (uint32_t)((k - 1) & 1), TC_WAIT_NS)) {
                 atomicOr(err, 2);
                 abort_flag = 1;
+            }
+            // a group of tg terms is complete in TMEM: add it into the output
+            // before term k restarts the accumulator (the loads have finished
+            // when this thread arrives on full_bar below)
+            if (k >= 1 && k % tg == 0 && !*(volatile int*)&abort_flag) {
+                tc::fence_after_sync();
+                drain(k == tg);
+                tc::fence_before_sync();
             }
             // receptor circulant samples of the term, scaled and split
             if (tid < N) {
@@ -401,26 +451,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
             abort_flag = 1;
         }
         tc::fence_after_sync();
-        const float inv = 1.0f / (c_scale * TC_F_SCALE);
-        const int xo = 32 * (warp & 3) + lane;  // TMEM lane = output row x
-        const uint32_t trow = (uint32_t)(32 * (warp & 3)) << 16;
-#pragma unroll 1
-        for (int cb = 0; cb < 2; ++cb) {
-            const int c0 = half * 64 + cb * 32;  // this warp's rotations [c0, c0 + 32)
-            uint32_t dre[32], dim[32];
-            tc::tmem_ld_32x32b_x32(tmem + trow + c0, dre);
-            tc::tmem_ld_32x32b_x32(tmem + trow + TC_ROT + c0, dim);
-            tc::tmem_wait_ld();
-            if (xo < N) {
-#pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const int rr = g * TC_ROT + c0 + j;
-                    const size_t o = (size_t)rr * NH * N + (size_t)(xo >> 2) * NH * 4 + (size_t)p * 4 + (xo & 3);
-                    if (rr < n_rot)
-                        g2t[o] = make_float2(__uint_as_float(dre[j]) * inv, __uint_as_float(dim[j]) * inv);
-                }
-            }
-        }
+        drain(Ka <= tg);
     }
     // the MMA issuer's done barrier covers every MMA before TMEM is released
     if (tid == 0 && !tc::mbar_wait(&done_bar, 0, TC_WAIT_NS)) atomicOr(err, 16);

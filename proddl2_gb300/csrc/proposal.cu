@@ -40,6 +40,7 @@
 #include <vector>
 
 #include "fftdock.h"
+#include "internal.h"
 
 namespace {
 
@@ -622,7 +623,8 @@ int fftdock_proposal_create(int32_t device, uint64_t seed, fftdock_proposal** ou
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return pfail(p, FFTDOCK_ECUDA, "no CUDA device");
     if (device < 0 || device >= ndev) return pfail(p, FFTDOCK_EINVAL, "device ordinal out of range");
     p->device = device;
-    PK(cudaSetDevice(device));
+    fftdock::DeviceScope dev_scope(device);
+    PK(dev_scope.status());
     cudaDeviceProp prop;
     PK(cudaGetDeviceProperties(&prop, device));
     if (prop.major != 10 || prop.minor != 3)
@@ -683,7 +685,8 @@ void fftdock_proposal_destroy(fftdock_proposal* p) {
 
 int fftdock_proposal_get_params(fftdock_proposal* p, float* out) {
     if (!p || !out) return FFTDOCK_EINVAL;
-    PK(cudaSetDevice(p->device));
+    fftdock::DeviceScope dev_scope(p->device);
+    PK(dev_scope.status());
     PK(cudaStreamSynchronize(p->stream));
     PK(cudaMemcpy(out, p->w, NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
     return FFTDOCK_OK;
@@ -693,7 +696,8 @@ int fftdock_proposal_set_params(fftdock_proposal* p, const float* in) {
     if (!p || !in) return FFTDOCK_EINVAL;
     for (int i = 0; i < NPARAM; ++i)
         if (!std::isfinite(in[i])) return pfail(p, FFTDOCK_EINVAL, "non-finite parameter");
-    PK(cudaSetDevice(p->device));
+    fftdock::DeviceScope dev_scope(p->device);
+    PK(dev_scope.status());
     PK(cudaStreamSynchronize(p->stream));
     PK(cudaMemcpy(p->w, in, NPARAM * sizeof(float), cudaMemcpyHostToDevice));
     PK(cudaMemset(p->m, 0, NPARAM * sizeof(float)));
@@ -753,7 +757,8 @@ int fftdock_proposal_train(fftdock_proposal* p, int32_t steps, int32_t batch, fl
                            float* mean_loss) {
     if (!p || steps < 0 || batch < 1 || batch > MAX_BATCH || !(lr > 0.f))
         return pfail(p, FFTDOCK_EINVAL, "bad arguments");
-    PK(cudaSetDevice(p->device));
+    fftdock::DeviceScope dev_scope(p->device);
+    PK(dev_scope.status());
     int rc;
     if ((rc = sync_ligands(p)) || (rc = sync_samples(p)) || (rc = grow_store(p, batch))) return rc;
     if (p->n_dev_samples < 1) return pfail(p, FFTDOCK_ESTATE, "no training samples");
@@ -804,7 +809,8 @@ int fftdock_proposal_gradients(fftdock_proposal* p, int32_t n, const int32_t* li
         return pfail(p, FFTDOCK_EINVAL, "bad arguments");
     for (int i = 0; i < n; ++i)
         if (lig[i] < 0 || lig[i] >= (int32_t)p->h_start.size()) return pfail(p, FFTDOCK_EINVAL, "unknown ligand id");
-    PK(cudaSetDevice(p->device));
+    fftdock::DeviceScope dev_scope(p->device);
+    PK(dev_scope.status());
     int rc;
     if ((rc = sync_ligands(p)) || (rc = grow_store(p, n))) return rc;
     cudaStream_t s = p->stream;
@@ -837,7 +843,8 @@ int fftdock_proposal_predict_device(fftdock_proposal* p, int32_t lig, int32_t n,
     if (!p || n < 0 || (n > 0 && (!d_rot || !d_out))) return pfail(p, FFTDOCK_EINVAL, "bad arguments");
     if (lig < 0 || lig >= (int32_t)p->h_start.size()) return pfail(p, FFTDOCK_EINVAL, "unknown ligand id");
     if (n == 0) return FFTDOCK_OK;
-    PK(cudaSetDevice(p->device));
+    fftdock::DeviceScope dev_scope(p->device);
+    PK(dev_scope.status());
     int rc;
     if ((rc = sync_ligands(p))) return rc;
     cudaStream_t s = stream ? (cudaStream_t)stream : p->stream;
@@ -853,7 +860,8 @@ int fftdock_proposal_predict_device(fftdock_proposal* p, int32_t lig, int32_t n,
 int fftdock_proposal_predict(fftdock_proposal* p, int32_t lig, int32_t n, const double* rot, float* out) {
     if (!p || n < 0 || (n > 0 && (!rot || !out))) return pfail(p, FFTDOCK_EINVAL, "bad arguments");
     if (n == 0) return FFTDOCK_OK;
-    PK(cudaSetDevice(p->device));
+    fftdock::DeviceScope dev_scope(p->device);
+    PK(dev_scope.status());
     double* d_rot = nullptr;
     float* d_out = nullptr;
     PK(dalloc(&d_rot, 9 * (size_t)n));

@@ -50,6 +50,7 @@ class ScanConfig:
     cluster_order: str = "reference"  # leader walk: "reference" (worst value first) or "best_first"
     lj_mix: int = 1                 # LJ sets: sigma rule (0 arithmetic, 1 geometric; ljComp needs 1)
     lj_cut: float = 9.0             # LJ sets: cutOffFft
+    tc_terms_per_sum: int = 0       # tensor form: terms per tensor-memory sum (0: library default)
 
     @classmethod
     def from_options(cls, opts: dict, **kw):
@@ -112,6 +113,7 @@ def native_config(config: ScanConfig):
     cfg.cluster_order = {"reference": 0, "best_first": 1}[config.cluster_order]
     cfg.lj_mix = int(config.lj_mix)
     cfg.lj_cut = float(config.lj_cut)
+    cfg.tc_terms_per_sum = int(config.tc_terms_per_sum)
     return cfg, ace
 
 

@@ -5,7 +5,8 @@ memory pool already holds the whole GPU, or a pipeline that forbids
 allocation once it runs.  fftdock_scan_device_noalloc keeps its work memory
 in a fixed array inside the library; here it must give the same peaks as
 fftdock_scan_device on the same context, on two calls in a row (the second
-call reuses the array the first one left behind).  Named to run last.
+call reuses the array the first one left behind), and the device's free
+memory must not change across either call.  Named to run last.
 """
 from pathlib import Path
 
@@ -18,6 +19,9 @@ GOLDEN = Path(__file__).resolve().parent / "golden"
 
 
 def _run(scan, rot, k, noalloc):
+    """One scan into fresh device buffers; with noalloc, also the device's
+    free memory just before and just after the call (buffers and stream are
+    made first, the call is synchronised before the second reading)."""
     import torch
     from proddl2_gb300 import _lib
     n = rot.shape[0]
@@ -25,12 +29,16 @@ def _run(scan, rot, k, noalloc):
     d_peaks = torch.zeros(n * k * _lib.peak_dtype().itemsize, dtype=torch.uint8, device="cuda")
     d_np = torch.full((n,), -1, dtype=torch.int32, device="cuda")
     stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
     with torch.cuda.stream(stream):
         fn = scan.scan_device_noalloc if noalloc else scan.scan_device
         fn(d_rot.data_ptr(), n, d_peaks.data_ptr(), d_np.data_ptr(), first_rot_id=5,
            stream_ptr=stream.cuda_stream)
     stream.synchronize()
-    return d_peaks.cpu().numpy().view(_lib.peak_dtype()).reshape(n, k), d_np.cpu().numpy()
+    free_after = torch.cuda.mem_get_info()[0]
+    out = d_peaks.cpu().numpy().view(_lib.peak_dtype()).reshape(n, k), d_np.cpu().numpy()
+    return out, (free_before, free_after)
 
 
 def _same(a, b):
@@ -45,12 +53,16 @@ def _same(a, b):
 
 
 def _check(scan, rot, k):
-    ref = _run(scan, rot, k, noalloc=False)
+    ref, _ = _run(scan, rot, k, noalloc=False)
     assert np.all(ref[1] == k)
-    first = _run(scan, rot, k, noalloc=True)
-    second = _run(scan, rot, k, noalloc=True)
+    first, mem1 = _run(scan, rot, k, noalloc=True)
+    second, mem2 = _run(scan, rot, k, noalloc=True)
     _same(first, ref)
     _same(second, ref)
+    # the array was committed when the context was created: neither call
+    # takes device memory
+    assert mem1[0] == mem1[1], mem1
+    assert mem2[0] == mem2[1], mem2
 
 
 def test_noalloc_scan_matches_device_scan_64():

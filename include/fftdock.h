@@ -109,13 +109,18 @@ enum {
     FFTDOCK_CLUSTER_ORDER_BEST_FIRST = 1
 };
 #define FFTDOCK_MAX_QUEUE_CLUSTERED 16384
+#define FFTDOCK_MAX_PEAKS 256
 
 typedef struct fftdock_config {
     int32_t struct_size;         /* sizeof(fftdock_config) */
     int32_t grid_n;              /* FFT grid edge N (cubic); see fftdock_supported_grid() */
     double grid_step;            /* h in Angstrom ("gridStep") */
     int32_t term_set;            /* FFTDOCK_TERMS_* ("potentialName") */
-    int32_t peaks_per_rot;       /* translations kept per rotation ("maxNTrans"), 1..16 */
+    int32_t peaks_per_rot;       /* translations kept per rotation ("maxNTrans"), 1..FFTDOCK_MAX_PEAKS;
+                                    above 16 (the per-plane candidate pools) the scan keeps each
+                                    rotation's exact queue like cluster_trans does, without the
+                                    clustering: its first peaks_per_rot + 16 cells are rescored in
+                                    FP64 and the best peaks_per_rot kept */
     int32_t max_trans_inp;       /* bound of the per-rotation queue ("maxNTransInp") */
     double max_val_corr;         /* only scores strictly below this are kept ("maxValCorr") */
     int32_t rot_batch;           /* rotations per device batch, 1..1024 */
@@ -138,6 +143,13 @@ typedef struct fftdock_config {
                                     group's sum is added into the FP32 result (round to nearest); the
                                     tensor core's own accumulation error grows with this chain length.
                                     0 = the library default (FFTDOCK_TC_TERMS_PER_SUM_DEFAULT) */
+    int32_t grid_nx, grid_ny, grid_nz; /* FFT sizes per axis (the reference's fftSize, each axis from
+                                    findBestSize over the padded receptor box, docking_fft.hpp:541-553);
+                                    all 0 = grid_n on every axis.  A cubic size with compiled plans
+                                    (fftdock_supported_grid) runs the cubic kernels; any other sizes,
+                                    each in [8, 256] with no prime factor above 13, run the box-grid
+                                    kernels (FFT pencil stage, up to 16 peaks per rotation, FP32 spectra,
+                                    no clustering, no pair graph, no no-allocation scan) */
 } fftdock_config;
 #define FFTDOCK_TC_TERMS_PER_SUM_DEFAULT 6
 
@@ -157,8 +169,15 @@ typedef struct fftdock_ctx fftdock_ctx;
  * must still be supplied), 4 peaks, queue 10000, maxValCorr +inf, batch 64. */
 void fftdock_config_init(fftdock_config* cfg);
 
-/* Grid sizes compiled into this library (1 if supported). */
+/* Cubic grid edges with compiled plans in this library (1 if supported). */
 int fftdock_supported_grid(int32_t n);
+
+/* 1 if this library scans a grid of these per-axis FFT sizes: a compiled
+ * cubic edge, or box-grid sizes (each in [8, 256], no prime factor above 13;
+ * every findBestSize result in that range qualifies).  Replaces the sizing of
+ * FFTCorrelator::init (include/PRODDL/docking_fft.hpp:541-553), which takes
+ * fftSize per axis. */
+int fftdock_supported_dims(int32_t nx, int32_t ny, int32_t nz);
 
 /* FFTW_Size::findBestSize (include/PRODDL/Math/fft.hpp:141-151): smallest
  * size >= start_n over primes {2,3,5,7,11,13} with e11 + e13 <= 1. */
@@ -225,8 +244,10 @@ int fftdock_scan_device(fftdock_ctx* ctx, int32_t n_rot, const double* d_rot, in
 int fftdock_scan_device_noalloc(fftdock_ctx* ctx, int32_t n_rot, const double* d_rot, int32_t first_rot_id,
                                 fftdock_peak* d_peaks, int32_t* d_n_peaks, void* stream);
 
-/* Introspection. */
+/* Introspection.  fftdock_grid_n: the x size (the edge of a cubic grid);
+ * fftdock_grid_dims: the three sizes. */
 int fftdock_grid_n(const fftdock_ctx* ctx);
+int fftdock_grid_dims(const fftdock_ctx* ctx, int32_t* dims3);
 int fftdock_n_terms(const fftdock_ctx* ctx);
 
 typedef struct fftdock_scan_info {

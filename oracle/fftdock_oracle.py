@@ -169,31 +169,58 @@ class BoundPriorityQueue:
 # ----------------------------------------------------------------------------
 @dataclass(frozen=True)
 class Geometry:
+    """Centred grid of cubic cells; the logical size may differ per axis
+    (``fftSize`` is a 3-vector, ``docking_fft.hpp:541-553``).  For a cubic
+    grid the scalar fields describe every axis; ``dims``/``zeros`` always
+    hold the per-axis sizes and low corners."""
     h: float
-    n: int
-    zero: float       # spatial coordinate of the grid's low corner
-    zero_h: float     # zero - h, used by toLogical
-    center0: float    # centre of cell 0
+    n: int            # the edge of a cubic grid (the x size of a box grid)
+    zero: float       # spatial coordinate of the grid's low corner (x axis)
+    zero_h: float     # zero - h, used by toLogical (x axis)
+    center0: float    # centre of cell 0 (x axis)
+    dims: tuple = ()  # (nx, ny, nz)
+    zeros: tuple = ()  # per-axis low corner
 
     @staticmethod
     def centred(h, n):
-        """``UniformCubicGeometry(step, logicalSize)`` (gridcoord.hpp:127-142)."""
+        """``UniformCubicGeometry(step, logicalSize)`` (gridcoord.hpp:127-142),
+        per axis: zero = -(toSpatialRight(n - 1) - toSpatialLeft(0)) / 2;
+        ``n`` is one edge or (nx, ny, nz)."""
         h = float(h)
-        s_upper = h + h * float(n - 1)   # toSpatialRight(n-1) with zero 0
-        s_size = s_upper - 0.0
-        zero = (-1.0 * s_size) / 2.0
-        return Geometry(h=h, n=int(n), zero=zero, zero_h=zero - h, center0=zero + h / 2.0)
+        dims = (int(n),) * 3 if np.ndim(n) == 0 else tuple(int(v) for v in n)
+        zeros = []
+        for nd in dims:
+            s_upper = h + h * float(nd - 1)   # toSpatialRight(n-1) with zero 0
+            s_size = s_upper - 0.0
+            zeros.append((-1.0 * s_size) / 2.0)
+        z = zeros[0]
+        return Geometry(h=h, n=dims[0], zero=z, zero_h=z - h, center0=z + h / 2.0, dims=dims, zeros=tuple(zeros))
+
+    @property
+    def cubic(self):
+        return self.dims[0] == self.dims[1] == self.dims[2]
+
+    @property
+    def volume(self):
+        return self.dims[0] * self.dims[1] * self.dims[2]
 
     def to_logical(self, x):
-        """``toLogical``: int((x - (zero - h)) / h) - 1, C truncation toward 0."""
-        v = (np.asarray(x, dtype=np.float64) - self.zero_h) / self.h
+        """``toLogical``: int((x - (zero - h)) / h) - 1, C truncation toward 0;
+        on a box grid ``x`` is (..., 3) points."""
+        x = np.asarray(x, dtype=np.float64)
+        zh = self.zero_h if self.cubic else np.array(self.zeros) - self.h
+        v = (x - zh) / self.h
         return np.trunc(v).astype(np.int64) - 1
 
-    def to_spatial(self, i):
-        return self.center0 + self.h * np.asarray(i, dtype=np.float64)
+    def to_spatial(self, i, axis=0):
+        c0 = self.center0 if self.cubic else self.zeros[axis] + self.h / 2.0
+        return c0 + self.h * np.asarray(i, dtype=np.float64)
 
     def spatial_domain(self):
-        return self.zero, self.zero + self.h * self.n
+        if self.cubic:
+            return self.zero, self.zero + self.h * self.n
+        z = np.array(self.zeros)
+        return z, z + self.h * np.array(self.dims)
 
 
 # ----------------------------------------------------------------------------
@@ -254,7 +281,7 @@ def _projection_boxes(geom, center, cut):
     lo = geom.to_logical(center - cut)
     hi = geom.to_logical(center + cut)
     lo = np.maximum(lo, 0)
-    hi = np.minimum(hi, geom.n - 1)
+    hi = np.minimum(hi, np.array(geom.dims) - 1)
     return lo, hi
 
 
@@ -267,9 +294,9 @@ def _cells_in_box(geom, center, cut):
     ix = np.arange(lo[0], hi[0] + 1)
     iy = np.arange(lo[1], hi[1] + 1)
     iz = np.arange(lo[2], hi[2] + 1)
-    dx = geom.to_spatial(ix) - center[0]
-    dy = geom.to_spatial(iy) - center[1]
-    dz = geom.to_spatial(iz) - center[2]
+    dx = geom.to_spatial(ix, 0) - center[0]
+    dy = geom.to_spatial(iy, 1) - center[1]
+    dz = geom.to_spatial(iz, 2) - center[2]
     r2 = (dx[:, None, None] * dx[:, None, None] + dy[None, :, None] * dy[None, :, None]) \
         + dz[None, None, :] * dz[None, None, :]
     return (slice(lo[0], hi[0] + 1), slice(lo[1], hi[1] + 1), slice(lo[2], hi[2] + 1)), r2
@@ -278,8 +305,7 @@ def _cells_in_box(geom, center, cut):
 def shape_grid(geom, rec_xyz, r_core, width):
     """Plug-in shape term: +1 on surface cells (centre within r_core+width of
     an atom, not core), -15 on core cells (within r_core)."""
-    n = geom.n
-    flag = np.zeros((n, n, n), dtype=np.int8)
+    flag = np.zeros(geom.dims, dtype=np.int8)
     cut = float(r_core) + float(width)
     rc2 = float(r_core) * float(r_core)
     rs2 = cut * cut
@@ -290,7 +316,7 @@ def shape_grid(geom, rec_xyz, r_core, width):
         sl, r2 = got
         f = np.where(r2 <= rc2, 2, np.where(r2 <= rs2, 1, 0)).astype(np.int8)
         np.maximum(flag[sl], f, out=flag[sl])
-    s = np.zeros((n, n, n), dtype=np.float64)
+    s = np.zeros(geom.dims, dtype=np.float64)
     s[flag == 1] = SHAPE_SURFACE
     s[flag == 2] = SHAPE_CORE
     return s
@@ -306,8 +332,7 @@ def ace_type_density(geom, rec_xyz, rec_type, n_types, b, k, a, cut):
     """G_tau(x) = sum over type-tau atoms of the sigmoid at the cell centre,
     r^2 <= cut^2, r^2 clamped to (h/4)^2 (project.hpp:143-159,
     docking_molforce.hpp:307-310)."""
-    n = geom.n
-    g = np.zeros((n_types, n, n, n), dtype=np.float64)
+    g = np.zeros((n_types,) + tuple(geom.dims), dtype=np.float64)
     cut2 = float(cut) * float(cut)
     min_d = geom.h / 4.0
     min_d2 = min_d * min_d
@@ -458,10 +483,9 @@ def lj_receptor_terms(geom, rec_xyz, lj: LjParams, term_set):
     """K receptor grids of the reference's LJ potentials, projected like
     ProjectorRadialField::projectFields (atoms in order, r^2 clamped to
     (h/4)^2 inside the cropped box, r^2 <= cut^2)."""
-    n = geom.n
     consts = lj_atom_constants(lj, term_set)
     k = 2 if term_set == TERMS_LJ_COMP else 1
-    grids = np.zeros((k, n, n, n))
+    grids = np.zeros((k,) + tuple(geom.dims))
     md = geom.h / 4.0
     md2 = md * md
     cut = float(lj.cut)
@@ -501,15 +525,15 @@ def bin_ligand(geom, rot, lig_xyz):
     """Rotated ligand cells (n, 3) int64 and an all-in-grid flag."""
     p = rotate_points(rot, lig_xyz)
     cells = geom.to_logical(p)
-    ok = bool(np.all((cells >= 0) & (cells < geom.n)))
+    ok = bool(np.all((cells >= 0) & (cells < np.array(geom.dims))))
     return cells, ok
 
 
 def ligand_grids(geom, cells, weights):
-    n = geom.n
+    nx, ny, nz = geom.dims
     k = weights.shape[1]
-    grids = np.zeros((k, n, n, n), dtype=np.float64)
-    flat = (cells[:, 0] * n + cells[:, 1]) * n + cells[:, 2]
+    grids = np.zeros((k, nx, ny, nz), dtype=np.float64)
+    flat = (cells[:, 0] * ny + cells[:, 1]) * nz + cells[:, 2]
     for t in range(k):
         np.add.at(grids[t].reshape(-1), flat, weights[:, t])
     return grids
@@ -527,11 +551,11 @@ def correlate(rec_spectra, lig_grids, workers=1):
     """sum_t IFFT(conj(R^_t) * FFT(L_t)) (normalised by V), one forward and one
     inverse transform per term as the reference does."""
     import scipy.fft as sfft
-    n = lig_grids.shape[1]
+    shape = lig_grids.shape[1:]
     total = None
     for rs, lg in zip(rec_spectra, lig_grids):
         lf = sfft.rfftn(lg, workers=workers)
-        c = sfft.irfftn(np.conj(rs) * lf, s=(n, n, n), workers=workers)
+        c = sfft.irfftn(np.conj(rs) * lf, s=shape, workers=workers)
         total = c if total is None else total + c
     return total
 
@@ -553,20 +577,25 @@ def select_minima(corr, k, max_val=np.inf):
 
 
 def unwrap(cell, n):
-    """``WrappedIndex::unwrap`` (Math/fft.hpp:199-206): y = -x, +n if y < -(n/2)."""
+    """``WrappedIndex::unwrap`` (Math/fft.hpp:199-206): y = -x, +n if y < -(n/2),
+    per axis (``n`` one edge or the three sizes)."""
+    n = np.asarray(n, dtype=np.int64)
     y = -np.asarray(cell, dtype=np.int64)
     y = np.where(y < -(n // 2), y + n, y)
     return y
 
 
 def offsets_to_cells(offsets, n):
+    """Flat C-order offsets (z fastest) -> (x, y, z); ``n`` one edge or the
+    three sizes."""
     offsets = np.asarray(offsets, dtype=np.int64)
-    return np.stack([offsets // (n * n), (offsets // n) % n, offsets % n], axis=-1)
+    ny, nz = (n, n) if np.ndim(n) == 0 else (int(n[1]), int(n[2]))
+    return np.stack([offsets // (ny * nz), (offsets // nz) % ny, offsets % nz], axis=-1)
 
 
 def translation(cell, geom):
     """``toSpatialDiff(unwrap(cell))`` (gridcoord.hpp:150)."""
-    return geom.h * unwrap(cell, geom.n).astype(np.float64)
+    return geom.h * unwrap(cell, geom.dims).astype(np.float64)
 
 
 # ----------------------------------------------------------------------------
@@ -577,9 +606,9 @@ def direct_score(rec_grids, cells, weights, shift_cell):
 
     ``shift_cell`` is the correlation offset s (the FFT output index); the
     ligand translation it stands for is h * unwrap(s)."""
-    n = rec_grids.shape[1]
+    dims = np.array(rec_grids.shape[1:], dtype=np.int64)
     s = np.asarray(shift_cell, dtype=np.int64)
-    c = (np.asarray(cells, dtype=np.int64) - s[None, :]) % n
+    c = (np.asarray(cells, dtype=np.int64) - s[None, :]) % dims[None, :]
     terms = []
     for t in range(rec_grids.shape[0]):
         w = weights[:, t]
@@ -614,7 +643,7 @@ def scan_rotation(geom, rec_grids, rec_spectra, lig_xyz, lig_weights, rot, k, ma
     lg = ligand_grids(geom, cells, lig_weights)
     corr = correlate(rec_spectra, lg, workers=workers)
     offs, vals = select_minima(corr, k, max_val)
-    pc = offsets_to_cells(offs, geom.n)
+    pc = offsets_to_cells(offs, geom.dims)
     return ScanResult(rot_id, offs, pc, vals, translation(pc, geom), True, corr if keep_corr else None)
 
 

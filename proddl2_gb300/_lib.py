@@ -67,6 +67,9 @@ class Config(C.Structure):
         ("lj_mix", C.c_int32),
         ("lj_cut", C.c_double),
         ("tc_terms_per_sum", C.c_int32),
+        ("grid_nx", C.c_int32),
+        ("grid_ny", C.c_int32),
+        ("grid_nz", C.c_int32),
     ]
 
 
@@ -167,6 +170,8 @@ _P = C.c_void_p
 SIGNATURES = {
     "fftdock_config_init": (None, [C.POINTER(Config)]),
     "fftdock_supported_grid": (C.c_int, [C.c_int32]),
+    "fftdock_supported_dims": (C.c_int, [C.c_int32, C.c_int32, C.c_int32]),
+    "fftdock_grid_dims": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "fftdock_find_best_size": (C.c_int, [C.c_int32, C.POINTER(C.c_int32)]),
     "fftdock_create": (C.c_int, [C.POINTER(Config), C.POINTER(_P)]),
     "fftdock_destroy": (None, [_P]),

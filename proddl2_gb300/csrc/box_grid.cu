@@ -1,0 +1,676 @@
+// The scan on box grids: FFT sizes chosen per axis (Nx, Ny, Nz), as the
+// reference sizes its grid (findBestSize<N_dim> per axis over the padded
+// receptor box, include/PRODDL/docking_fft.hpp:541-553 and
+// include/PRODDL/Math/fft.hpp:141-168), and cubic edges without a compiled
+// plan.  Same pipeline and conventions as the cubic kernels -- ligand prep
+// (rotate, toLogical per axis, stable sort by (term, x)), pencil stage
+// (y/z stages as direct sums over the ligand's entries, x transform,
+// spectrum product summed over terms, inverse x transform), plane stage
+// (inverse y transform, real inverse z transform, exact per-plane top 16),
+// finalize (merge, FP64 direct-space rescoring, sort, maxValCorr, unwrap per
+// axis) -- with every transform length a runtime value: one warp per line
+// runs a mixed-radix Stockham FFT (radices 4, 2, 3, 5, 7, 11, 13) out of
+// shared memory with a twiddle table per axis.  The receptor's transforms
+// run the same line FFT in FP64.
+//
+// Layout (Hz = Nz/2 + 1, pencil p = ky Hz + kz, PP = Ny Hz rounded up to 32):
+//   spec  [K][Nx][PP]  float2  R^_t(kx, p) / V
+//   rgrid [K][V]       double  real-space receptor terms (FP64 rescoring)
+//   ent   [B][n_ent]   uint32  t << 24 | x << 16 | y << 8 | z, sorted by (t, x)
+//   offs  [B][K Nx+1]  int32   start of bin (t, x)
+//   g2    [B][Nx][PP]  float2  per-x complex (ky, kz) planes
+//   cand  [B][Nx][16]          per-plane FP32 candidate pools
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "fft_core.cuh"
+#include "internal.h"
+#include "scan_kernels.cuh"
+
+namespace fftdock {
+
+namespace {
+
+constexpr int kBoxWarps = 8;  // lines (pencils, columns, rows) per CTA
+
+// radices in Stockham stage order; false if n has another prime factor
+bool factor_plan(int n, BoxPlan& pl) {
+    static const int radices[] = {4, 2, 3, 5, 7, 11, 13};
+    pl.n = n;
+    pl.nf = 0;
+    int m = n;
+    for (int r : radices)
+        while (m % r == 0 && pl.nf < kBoxMaxFactors) {
+            pl.f[pl.nf++] = r;
+            m /= r;
+        }
+    return m == 1 && n >= 2;
+}
+
+template <typename T2> __device__ __forceinline__ T2 c_mul(T2 a, T2 b) {
+    T2 r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+// table entry W_n^m = e^{-2 pi i m / n}, conjugated for the inverse transform
+template <typename T2, int SIGN> __device__ __forceinline__ T2 tw_at(const T2* tw, int m) {
+    T2 w = tw[m];
+    if (SIGN > 0) w.y = -w.y;
+    return w;
+}
+
+// one Stockham stage of radix R over a line of n points held in src:
+// butterfly j reads src[j + r n/R], applies the twiddles W^(j mod Ns) r n/(Ns R),
+// and writes its R-point DFT to dst[(j / Ns) Ns R + j mod Ns + k Ns]
+template <typename T2, int SIGN, int R>
+__device__ __forceinline__ void stockham_stage(const T2* src, T2* dst, const T2* tw, int n, int ns, int lane) {
+    const int nb = n / R, nr = n / R;
+    for (int j = lane; j < nb; j += 32) {
+        T2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = src[j + r * nb];
+        const int jm = j % ns;
+        const int step = jm * (n / (ns * R));
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[r] = c_mul(v[r], tw_at<T2, SIGN>(tw, (step * r) % n));
+        const int base = (j / ns) * ns * R + jm;
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            T2 acc = v[0];
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                const T2 p = c_mul(v[r], tw_at<T2, SIGN>(tw, ((r * k) % R) * nr));
+                acc.x += p.x;
+                acc.y += p.y;
+            }
+            dst[base + k * ns] = acc;
+        }
+    }
+}
+
+// Unnormalised DFT of the warp's line in a (n points), b a second buffer of
+// n points; returns the buffer that holds the result.  SIGN -1: forward
+// e^{-2 pi i jk/n}; +1: inverse.  Ends with __syncwarp.
+template <typename T2, int SIGN>
+__device__ T2* warp_fft(T2* a, T2* b, const T2* tw, const BoxPlan& pl, int lane) {
+    T2* src = a;
+    T2* dst = b;
+    int ns = 1;
+    __syncwarp();
+    for (int s = 0; s < pl.nf; ++s) {
+        const int R = pl.f[s];
+        switch (R) {
+            case 4: stockham_stage<T2, SIGN, 4>(src, dst, tw, pl.n, ns, lane); break;
+            case 2: stockham_stage<T2, SIGN, 2>(src, dst, tw, pl.n, ns, lane); break;
+            case 3: stockham_stage<T2, SIGN, 3>(src, dst, tw, pl.n, ns, lane); break;
+            case 5: stockham_stage<T2, SIGN, 5>(src, dst, tw, pl.n, ns, lane); break;
+            case 7: stockham_stage<T2, SIGN, 7>(src, dst, tw, pl.n, ns, lane); break;
+            case 11: stockham_stage<T2, SIGN, 11>(src, dst, tw, pl.n, ns, lane); break;
+            default: stockham_stage<T2, SIGN, 13>(src, dst, tw, pl.n, ns, lane); break;
+        }
+        __syncwarp();
+        T2* t = src;
+        src = dst;
+        dst = t;
+        ns *= R;
+    }
+    return src;
+}
+
+// ---------------------------------------------------------------------------
+// receptor transforms (FP64), one warp per line: line L starts at
+// (L / inner_count) outer_stride + (L % inner_count) inner_stride, element e
+// at + e elem_stride; in place
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(32 * kBoxWarps) box_line_fft64_kernel(double2* __restrict__ data,
+                                                                       const double2* __restrict__ tw, BoxPlan pl,
+                                                                       long n_lines, long elem_stride,
+                                                                       long inner_count, long inner_stride,
+                                                                       long outer_stride) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = pl.n;
+    double2* tws = reinterpret_cast<double2*>(smem_raw);  // [n]
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double2* a = tws + n + (size_t)w * 2 * n;
+    double2* b = a + n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) tws[i] = tw[i];
+    __syncthreads();
+    const long L = (long)blockIdx.x * kBoxWarps + w;
+    if (L >= n_lines) return;
+    double2* line = data + (L / inner_count) * outer_stride + (L % inner_count) * inner_stride;
+    for (int e = lane; e < n; e += 32) a[e] = line[(long)e * elem_stride];
+    const double2* r = warp_fft<double2, -1>(a, b, tws, pl, lane);
+    for (int e = lane; e < n; e += 32) line[(long)e * elem_stride] = r[e];
+}
+
+// [Nx][Ny][Nz] complex -> [Nx][Ny][Hz]
+__global__ void box_half_extract_kernel(const double2* __restrict__ full, double2* __restrict__ half, int nx, int ny,
+                                        int nz, int hz) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t tot = (size_t)nx * ny * hz;
+    if (i >= tot) return;
+    const size_t row = i / hz;
+    const int kz = (int)(i - row * hz);
+    half[i] = full[row * nz + kz];
+}
+
+// ---------------------------------------------------------------------------
+// ligand prep: rotate (the reference's operation order, no FMA), toLogical
+// per axis, bins (t, x), stable sort (one CTA per rotation)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) box_prep_kernel(const double* __restrict__ rot,
+                                                       const double* __restrict__ lig_xyz,
+                                                       const int32_t* __restrict__ lig_term, int n_ent, int K, Geo geo,
+                                                       uint32_t* __restrict__ ent_out, int32_t* __restrict__ offs_out,
+                                                       int32_t* __restrict__ status, const float* __restrict__ w_in,
+                                                       float* __restrict__ w_out, int32_t* __restrict__ idx_out) {
+    extern __shared__ unsigned char smem_raw[];
+    const int nx = geo.n[0], ny = geo.n[1], nz = geo.n[2];
+    const int nbins = K * nx;
+    int32_t* cnt = reinterpret_cast<int32_t*>(smem_raw);           // [K*Nx + 1]
+    uint32_t* keys = reinterpret_cast<uint32_t*>(cnt + nbins + 1);  // [n_ent]
+    __shared__ int bad;
+    __shared__ int wsum[8];
+    const int q = blockIdx.x;
+    const int tid = threadIdx.x;
+    for (int i = tid; i <= nbins; i += blockDim.x) cnt[i] = 0;
+    if (tid == 0) bad = 0;
+    __syncthreads();
+    const double* m = rot + 9 * (size_t)q;
+    for (int i = tid; i < n_ent; i += blockDim.x) {
+        const double x0 = lig_xyz[3 * i], x1 = lig_xyz[3 * i + 1], x2 = lig_xyz[3 * i + 2];
+        const double p0 = __dadd_rn(__dadd_rn(__dmul_rn(m[0], x0), __dmul_rn(m[1], x1)), __dmul_rn(m[2], x2));
+        const double p1 = __dadd_rn(__dadd_rn(__dmul_rn(m[3], x0), __dmul_rn(m[4], x1)), __dmul_rn(m[5], x2));
+        const double p2 = __dadd_rn(__dadd_rn(__dmul_rn(m[6], x0), __dmul_rn(m[7], x1)), __dmul_rn(m[8], x2));
+        int c0 = logical_q(p0, geo, 0), c1 = logical_q(p1, geo, 1), c2 = logical_q(p2, geo, 2);
+        const bool ok = c0 >= 1 && c0 <= nx && c1 >= 1 && c1 <= ny && c2 >= 1 && c2 <= nz;
+        if (!ok) atomicOr(&bad, 1);
+        // out-of-grid atoms are clamped for memory safety; the rotation is
+        // reported and gives no peaks
+        c0 = min(max(c0 - 1, 0), nx - 1);
+        c1 = min(max(c1 - 1, 0), ny - 1);
+        c2 = min(max(c2 - 1, 0), nz - 1);
+        const int t = lig_term[i];
+        keys[i] = ((uint32_t)t << 24) | ((uint32_t)c0 << 16) | ((uint32_t)c1 << 8) | (uint32_t)c2;
+        atomicAdd(&cnt[t * nx + c0], 1);
+    }
+    __syncthreads();
+    {
+        const int per = (nbins + blockDim.x - 1) / blockDim.x;
+        const int b0 = min(tid * per, nbins), b1 = min(b0 + per, nbins);
+        int local = 0;
+        for (int i = b0; i < b1; ++i) local += cnt[i];
+        const int lane = tid & 31, wid = tid >> 5;
+        int incl = local;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) wsum[wid] = incl;
+        __syncthreads();
+        int wbase = 0;
+        for (int k = 0; k < wid; ++k) wbase += wsum[k];
+        int run = wbase + incl - local;
+        for (int i = b0; i < b1; ++i) {
+            const int c = cnt[i];
+            cnt[i] = run;
+            run += c;
+        }
+        __syncthreads();
+        if (tid == 0) cnt[nbins] = n_ent;
+        __syncthreads();
+    }
+    int32_t* offs = offs_out + (size_t)q * (nbins + 1);
+    for (int i = tid; i <= nbins; i += blockDim.x) offs[i] = cnt[i];
+    __syncthreads();
+    if (tid < 32) {
+        uint32_t* ent = ent_out + (size_t)q * n_ent;
+        for (int base = 0; base < n_ent; base += 32) {
+            const int i = base + tid;
+            const bool act = i < n_ent;
+            const uint32_t key = act ? keys[i] : 0xffffffffu;
+            const int bin = act ? (int)((key >> 24) * nx + ((key >> 16) & 255u)) : -1;
+            const unsigned peers = __match_any_sync(0xffffffffu, bin);
+            const int rank = __popc(peers & ((1u << tid) - 1u));
+            const int leader = __ffs(peers) - 1;
+            int dst = 0;
+            if (act) dst = cnt[bin] + rank;
+            __syncwarp();
+            if (act) ent[dst] = key;
+            if (act && w_out) {
+                w_out[(size_t)q * n_ent + dst] = w_in[i];
+                idx_out[(size_t)q * n_ent + dst] = i;
+            }
+            if (act && tid == leader) cnt[bin] += __popc(peers);
+            __syncwarp();
+        }
+    }
+    if (tid == 0) status[q] = bad;
+}
+
+// ---------------------------------------------------------------------------
+// pencil stage: CTA = one rotation x 8 pencils, one warp per pencil (ky, kz):
+//   F(x) = sum over entries of bin (t, x) of w e^{-2 pi i (ky y / Ny + kz z / Nz)}
+//   S(kx) += conj(R^_t(kx)) FFT_x(F)(kx)   over the terms
+//   g2[x][p] = IFFT_x(S)(x)
+// ---------------------------------------------------------------------------
+template <bool WEIGHTED>
+__global__ void __launch_bounds__(32 * kBoxWarps) box_pencil_kernel(
+    const float2* __restrict__ spec, const uint32_t* __restrict__ ent, const int32_t* __restrict__ offs,
+    const float* __restrict__ ent_w, const float2* __restrict__ twx_g, const float2* __restrict__ twy_g,
+    const float2* __restrict__ twz_g, BoxPlan plx, float2* __restrict__ g2, int K, int n_ent, int ny, int nz, int pp) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nx = plx.n, hz = nz / 2 + 1, np = ny * hz;
+    float2* twx = reinterpret_cast<float2*>(smem_raw);  // [nx]
+    float2* twy = twx + nx;                             // [ny]
+    float2* twz = twy + ny;                             // [nz]
+    float2* wbuf = twz + nz;                            // [8][3][nx]
+    uint32_t* ent_s = reinterpret_cast<uint32_t*>(wbuf + kBoxWarps * 3 * nx);  // [n_ent]: y << 16 | z
+    float* w_s = reinterpret_cast<float*>(ent_s + n_ent);                      // WEIGHTED: [n_ent]
+    int32_t* offs_s = reinterpret_cast<int32_t*>(w_s + (WEIGHTED ? n_ent : 0));  // [K*Nx + 1]
+
+    const int q = blockIdx.x;
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    for (int i = tid; i < nx; i += blockDim.x) twx[i] = twx_g[i];
+    for (int i = tid; i < ny; i += blockDim.x) twy[i] = twy_g[i];
+    for (int i = tid; i < nz; i += blockDim.x) twz[i] = twz_g[i];
+    const uint32_t* eq = ent + (size_t)q * n_ent;
+    for (int i = tid; i < n_ent; i += blockDim.x) {
+        const uint32_t u = eq[i];
+        ent_s[i] = (((u >> 8) & 255u) << 16) | (u & 255u);
+        if (WEIGHTED) w_s[i] = ent_w[(size_t)q * n_ent + i];
+    }
+    const int32_t* oq = offs + (size_t)q * (K * nx + 1);
+    for (int i = tid; i <= K * nx; i += blockDim.x) offs_s[i] = oq[i];
+    __syncthreads();
+
+    const int p = blockIdx.y * kBoxWarps + w;
+    if (p >= np) return;
+    const int ky = p / hz, kz = p - (p / hz) * hz;
+    float2* a = wbuf + (size_t)w * 3 * nx;
+    float2* b = a + nx;
+    float2* acc = b + nx;
+    for (int x = lane; x < nx; x += 32) acc[x] = make_float2(0.f, 0.f);
+    for (int t = 0; t < K; ++t) {
+        __syncwarp();
+        for (int x = lane; x < nx; x += 32) {
+            const int j0 = offs_s[t * nx + x], j1 = offs_s[t * nx + x + 1];
+            float2 f = make_float2(0.f, 0.f);
+            for (int j = j0; j < j1; ++j) {
+                const uint32_t e = ent_s[j];
+                const int y = (int)(e >> 16), z = (int)(e & 0xffffu);
+                const float2 ph = c_mul(twy[(ky * y) % ny], twz[(kz * z) % nz]);
+                const float wj = WEIGHTED ? w_s[j] : 1.f;
+                f.x = fmaf(wj, ph.x, f.x);
+                f.y = fmaf(wj, ph.y, f.y);
+            }
+            a[x] = f;
+        }
+        const float2* fx = warp_fft<float2, -1>(a, b, twx, plx, lane);
+        const float2* sp = spec + (size_t)t * nx * pp + p;
+        for (int kx = lane; kx < nx; kx += 32) {
+            const float2 f = fx[kx];
+            const float2 rv = __ldg(sp + (size_t)kx * pp);
+            float2 s = acc[kx];
+            s.x += f.x * rv.x + f.y * rv.y;
+            s.y += f.y * rv.x - f.x * rv.y;
+            acc[kx] = s;
+        }
+    }
+    __syncwarp();
+    for (int x = lane; x < nx; x += 32) a[x] = acc[x];
+    const float2* out = warp_fft<float2, +1>(a, b, twx, plx, lane);
+    float2* dst = g2 + (size_t)q * nx * pp + p;
+    for (int x = lane; x < nx; x += 32) dst[(size_t)x * pp] = out[x];
+}
+
+// ---------------------------------------------------------------------------
+// plane stage: CTA = one (rotation, x) plane.  Inverse y transform of every
+// kz column, then each row's real inverse z transform (the half spectrum
+// extended by Hermitian symmetry, a complex inverse transform, the real
+// part); every warp keeps the KC smallest (value, offset) of its rows, and
+// warp 0 merges them into the plane's pool.
+// ---------------------------------------------------------------------------
+template <bool DBG>
+__global__ void __launch_bounds__(32 * kBoxWarps) box_plane_kernel(const float2* __restrict__ g2,
+                                                                  const float2* __restrict__ twy_g,
+                                                                  const float2* __restrict__ twz_g, BoxPlan ply,
+                                                                  BoxPlan plz, int nx, int pp,
+                                                                  float* __restrict__ cand_v,
+                                                                  int32_t* __restrict__ cand_i,
+                                                                  float* __restrict__ dbg) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ny = ply.n, nz = plz.n, hz = nz / 2 + 1;
+    const int lmax = ny > nz ? ny : nz;
+    float2* plane = reinterpret_cast<float2*>(smem_raw);  // [Ny][Hz]
+    float2* twy = plane + (size_t)ny * hz;                // [ny]
+    float2* twz = twy + ny;                               // [nz]
+    float2* wbuf = twz + nz;                              // [8][2][lmax]
+    __shared__ float lv_s[kBoxWarps * KC];
+    __shared__ int li_s[kBoxWarps * KC];
+
+    const int x = blockIdx.x, q = blockIdx.y;
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    for (int i = tid; i < ny; i += blockDim.x) twy[i] = twy_g[i];
+    for (int i = tid; i < nz; i += blockDim.x) twz[i] = twz_g[i];
+    const float2* src = g2 + ((size_t)q * nx + x) * pp;
+    for (int i = tid; i < ny * hz; i += blockDim.x) plane[i] = src[i];
+    __syncthreads();
+    float2* a = wbuf + (size_t)w * 2 * lmax;
+    float2* b = a + lmax;
+    // columns kz: inverse transform along ky
+    for (int kz = w; kz < hz; kz += kBoxWarps) {
+        __syncwarp();
+        for (int k = lane; k < ny; k += 32) a[k] = plane[k * hz + kz];
+        const float2* o = warp_fft<float2, +1>(a, b, twy, ply, lane);
+        for (int y = lane; y < ny; y += 32) plane[y * hz + kz] = o[y];
+    }
+    __syncthreads();
+    // rows y: real inverse transform along kz, and the warp's top KC
+    WarpTopK tk;
+    tk.init();
+    const size_t row0 = (size_t)x * ny;
+    for (int y = w; y < ny; y += kBoxWarps) {
+        __syncwarp();
+        const float2* row = plane + (size_t)y * hz;
+        for (int k = lane; k < nz; k += 32) {
+            if (k < hz) {
+                a[k] = row[k];
+            } else {
+                const float2 c = row[nz - k];
+                a[k] = make_float2(c.x, -c.y);
+            }
+        }
+        const float2* o = warp_fft<float2, +1>(a, b, twz, plz, lane);
+        for (int z0 = 0; z0 < nz; z0 += 32) {
+            const int z = z0 + lane;
+            const bool ok = z < nz;
+            const float v = ok ? o[z].x : INFINITY;
+            const int idx = ok ? (int)((row0 + y) * nz + z) : 0x7fffffff;
+            if (DBG && ok) dbg[(size_t)q * nx * ny * nz + (size_t)idx] = v;
+            tk.offer(v, idx, lane);
+        }
+    }
+    if (lane < KC) {
+        lv_s[w * KC + lane] = tk.lv;
+        li_s[w * KC + lane] = tk.li;
+    }
+    __syncthreads();
+    if (w == 0) {
+        merge_lists(lv_s, li_s, kBoxWarps * KC, tk, lane);
+        if (lane < KC) {
+            cand_v[((size_t)q * nx + x) * KC + lane] = tk.lv;
+            cand_i[((size_t)q * nx + x) * KC + lane] = tk.li;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// finalize: merge the Nx x KC pools, FP64 direct-space rescoring of the KC
+// best cells (mod each axis' size), sort by (energy, offset), maxValCorr,
+// translation = h unwrap(cell) per axis.  One CTA per rotation.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) box_finalize_kernel(
+    const float* __restrict__ cand_v, const int32_t* __restrict__ cand_i, const uint32_t* __restrict__ ent,
+    const int32_t* __restrict__ status, const double* __restrict__ rgrid, int n_ent, int nx, int ny, int nz,
+    int peak_stride, int k_out, double max_val, double h, int first_rot_id, fftdock_peak* __restrict__ peaks,
+    int32_t* __restrict__ n_peaks, float* __restrict__ pool_v, int32_t* __restrict__ pool_i,
+    const double* __restrict__ w64, const int32_t* __restrict__ ent_idx) {
+    __shared__ float lv_s[8 * KC];
+    __shared__ int li_s[8 * KC];
+    __shared__ double score_s[KC];
+    const int q = blockIdx.x;
+    const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
+    const long V = (long)nx * ny * nz;
+    const int ncand = nx * KC;
+    WarpTopK tk;
+    tk.init();
+    const float* cv = cand_v + (size_t)q * ncand;
+    const int32_t* ci = cand_i + (size_t)q * ncand;
+    for (int base = w * 32; base < ncand; base += 256) {
+        const int e = base + l;
+        tk.offer(e < ncand ? cv[e] : INFINITY, e < ncand ? ci[e] : 0x7fffffff, l);
+    }
+    if (l < KC) {
+        lv_s[w * KC + l] = tk.lv;
+        li_s[w * KC + l] = tk.li;
+    }
+    __syncthreads();
+    if (w == 0) {
+        merge_lists(lv_s, li_s, 8 * KC, tk, l);
+        __syncwarp();
+        if (l < KC) {
+            lv_s[l] = tk.lv;
+            li_s[l] = tk.li;
+        }
+    }
+    __syncthreads();
+    if (pool_v != nullptr && tid < KC) {
+        pool_v[(size_t)q * KC + tid] = lv_s[tid];
+        pool_i[(size_t)q * KC + tid] = li_s[tid];
+    }
+    const uint32_t* e_q = ent + (size_t)q * n_ent;
+    for (int c = w; c < KC; c += 8) {
+        const int off = li_s[c];
+        double sum = 0.0;
+        const bool ok = off >= 0 && off < V;
+        if (ok) {
+            const int sx = off / (ny * nz), sy = (off / nz) % ny, sz = off % nz;
+            for (int j = l; j < n_ent; j += 32) {
+                const uint32_t u = e_q[j];
+                const int t = (int)(u >> 24);
+                const int ax = (int)((u >> 16) & 255u), ay = (int)((u >> 8) & 255u), az = (int)(u & 255u);
+                const int gx = ax - sx < 0 ? ax - sx + nx : ax - sx;
+                const int gy = ay - sy < 0 ? ay - sy + ny : ay - sy;
+                const int gz = az - sz < 0 ? az - sz + nz : az - sz;
+                const double rv = rgrid[(size_t)t * V + ((size_t)gx * ny + gy) * nz + gz];
+                sum = __dadd_rn(sum, w64 ? __dmul_rn(w64[ent_idx[(size_t)q * n_ent + j]], rv) : rv);
+            }
+            for (int o = 16; o > 0; o >>= 1) sum = __dadd_rn(sum, __shfl_xor_sync(0xffffffffu, sum, o));
+        }
+        if (l == 0) score_s[c] = ok ? sum : INFINITY;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double sc[KC];
+        int of[KC];
+        for (int c = 0; c < KC; ++c) {
+            sc[c] = score_s[c];
+            of[c] = li_s[c];
+        }
+        for (int a2 = 1; a2 < KC; ++a2) {
+            const double s = sc[a2];
+            const int o = of[a2];
+            int b2 = a2 - 1;
+            while (b2 >= 0 && (sc[b2] > s || (sc[b2] == s && of[b2] > o))) {
+                sc[b2 + 1] = sc[b2];
+                of[b2 + 1] = of[b2];
+                --b2;
+            }
+            sc[b2 + 1] = s;
+            of[b2 + 1] = o;
+        }
+        int n = 0;
+        if (status[q] == 0) {
+            const int dims[3] = {nx, ny, nz};
+            for (int c = 0; c < KC && n < k_out; ++c) {
+                if (!(sc[c] < max_val) || of[c] < 0 || of[c] >= V) continue;
+                fftdock_peak pk;
+                pk.rot_id = first_rot_id + q;
+                pk.cell[0] = of[c] / (ny * nz);
+                pk.cell[1] = (of[c] / nz) % ny;
+                pk.cell[2] = of[c] % nz;
+                for (int d = 0; d < 3; ++d) {
+                    int yv = -pk.cell[d];
+                    if (yv < -(dims[d] / 2)) yv += dims[d];
+                    pk.t[d] = h * (double)yv;
+                }
+                pk.score = sc[c];
+                peaks[(size_t)q * peak_stride + n] = pk;
+                ++n;
+            }
+        }
+        n_peaks[q] = n;
+    }
+}
+
+size_t pencil_smem_bytes(int nx, int ny, int nz, int K, int n_ent, bool weighted) {
+    return (size_t)(nx + ny + nz) * sizeof(float2) + (size_t)kBoxWarps * 3 * nx * sizeof(float2) +
+           (size_t)n_ent * sizeof(uint32_t) * (weighted ? 2 : 1) + ((size_t)K * nx + 1) * sizeof(int32_t);
+}
+size_t plane_smem_bytes(int ny, int nz) {
+    const int hz = nz / 2 + 1, lmax = std::max(ny, nz);
+    return ((size_t)ny * hz + ny + nz + (size_t)kBoxWarps * 2 * lmax) * sizeof(float2);
+}
+size_t prep_smem_bytes(int nx, int K, int n_ent) {
+    return ((size_t)K * nx + 1) * sizeof(int32_t) + (size_t)n_ent * sizeof(uint32_t);
+}
+
+cudaError_t set_smem(const void* fn, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+cudaError_t box_prep(const BatchArgs& a, cudaStream_t s) {
+    const int nb = a.n_rot;
+    if (nb <= 0) return cudaSuccess;
+    const size_t sm = prep_smem_bytes(a.box.n[0], a.K, a.n_ent);
+    cudaError_t e = set_smem((const void*)box_prep_kernel, sm);
+    if (e != cudaSuccess) return e;
+    box_prep_kernel<<<nb, 256, sm, s>>>(a.rot, a.lig_xyz, a.lig_term, a.n_ent, a.K, a.box, a.ent, a.offs, a.status,
+                                        a.lig_w32, a.lig_w32 ? a.ent_w : nullptr, a.ent_idx);
+    return cudaGetLastError();
+}
+
+cudaError_t box_middle(const BatchArgs& a, cudaStream_t s) {
+    const int nb = a.n_rot;
+    if (nb <= 0) return cudaSuccess;
+    const int nx = a.box.n[0], ny = a.box.n[1], nz = a.box.n[2];
+    BoxPlan px, py, pz;
+    if (!factor_plan(nx, px) || !factor_plan(ny, py) || !factor_plan(nz, pz)) return cudaErrorInvalidValue;
+    const float2* twx = a.box_tw32;
+    const float2* twy = twx + nx;
+    const float2* twz = twy + ny;
+    cudaError_t e;
+    if (a.ev && (e = cudaEventRecord(a.ev[0], s)) != cudaSuccess) return e;
+    const bool weighted = a.lig_w32 != nullptr;
+    const size_t sm2 = pencil_smem_bytes(nx, ny, nz, a.K, a.n_ent, weighted);
+    const int np = ny * (nz / 2 + 1);
+    dim3 grid2(nb, (np + kBoxWarps - 1) / kBoxWarps);
+    if (weighted) {
+        if ((e = set_smem((const void*)box_pencil_kernel<true>, sm2)) != cudaSuccess) return e;
+        box_pencil_kernel<true><<<grid2, 32 * kBoxWarps, sm2, s>>>(static_cast<const float2*>(a.spec), a.ent, a.offs,
+                                                                  a.ent_w, twx, twy, twz, px, a.g2, a.K, a.n_ent, ny,
+                                                                  nz, a.PP);
+    } else {
+        if ((e = set_smem((const void*)box_pencil_kernel<false>, sm2)) != cudaSuccess) return e;
+        box_pencil_kernel<false><<<grid2, 32 * kBoxWarps, sm2, s>>>(static_cast<const float2*>(a.spec), a.ent,
+                                                                   a.offs, nullptr, twx, twy, twz, px, a.g2, a.K,
+                                                                   a.n_ent, ny, nz, a.PP);
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (a.ev && (e = cudaEventRecord(a.ev[1], s)) != cudaSuccess) return e;
+    const size_t sm3 = plane_smem_bytes(ny, nz);
+    dim3 grid3(nx, nb);
+    if (a.dbg_corr) {
+        if ((e = set_smem((const void*)box_plane_kernel<true>, sm3)) != cudaSuccess) return e;
+        box_plane_kernel<true><<<grid3, 32 * kBoxWarps, sm3, s>>>(a.g2, twy, twz, py, pz, nx, a.PP, a.cand_v,
+                                                                 a.cand_i, a.dbg_corr);
+    } else {
+        if ((e = set_smem((const void*)box_plane_kernel<false>, sm3)) != cudaSuccess) return e;
+        box_plane_kernel<false><<<grid3, 32 * kBoxWarps, sm3, s>>>(a.g2, twy, twz, py, pz, nx, a.PP, a.cand_v,
+                                                                  a.cand_i, nullptr);
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (a.ev && (e = cudaEventRecord(a.ev[2], s)) != cudaSuccess) return e;
+    return cudaSuccess;
+}
+
+cudaError_t box_finish(const BatchArgs& a, cudaStream_t s) {
+    const int nb = a.n_rot;
+    if (nb <= 0) return cudaSuccess;
+    box_finalize_kernel<<<nb, 256, 0, s>>>(a.cand_v, a.cand_i, a.ent, a.status, a.rgrid, a.n_ent, a.box.n[0],
+                                           a.box.n[1], a.box.n[2], a.peak_stride, a.k_out, a.max_val, a.h,
+                                           a.first_rot_id, a.peaks, a.n_peaks, a.pool_v, a.pool_i, a.lig_w64,
+                                           a.lig_w64 ? a.ent_idx : nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t box_scan_batch(const BatchArgs& a, cudaStream_t s) {
+    cudaError_t e = box_prep(a, s);
+    if (e != cudaSuccess) return e;
+    BatchArgs m = a;
+    m.ev = nullptr;
+    if ((e = box_middle(m, s)) != cudaSuccess) return e;
+    return box_finish(a, s);
+}
+
+size_t box_pencil_smem_unknown(int, int) { return 0; }
+
+cudaError_t box_load_kernels(int) {
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, (const void*)box_prep_kernel);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)box_pencil_kernel<false>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)box_plane_kernel<false>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)box_finalize_kernel);
+    return e;
+}
+
+}  // namespace
+
+bool box_plan(int n, BoxPlan* pl) { return factor_plan(n, *pl); }
+
+size_t box_pencil_smem(int nx, int ny, int nz, int K, int n_ent, bool weighted) {
+    return std::max(pencil_smem_bytes(nx, ny, nz, K, n_ent, weighted),
+                    std::max(plane_smem_bytes(ny, nz), prep_smem_bytes(nx, K, n_ent)));
+}
+
+// Forward transform of one real FP64 term grid [Nx][Ny][Nz] into spec_t
+// ([Nx][PP] float2, scaled 1 / V): complex z transforms, the half spectrum
+// kz < Hz, then y and x transforms, each a batch of line FFTs.
+cudaError_t box_receptor_fft(const double* rgrid_t, double2* cbuf, double2* hbuf, const double2* tw64,
+                             const int dims[3], void* spec_t, int PP, cudaStream_t s) {
+    const int nx = dims[0], ny = dims[1], nz = dims[2], hz = nz / 2 + 1;
+    BoxPlan px, py, pz;
+    if (!factor_plan(nx, px) || !factor_plan(ny, py) || !factor_plan(nz, pz)) return cudaErrorInvalidValue;
+    const double2* twx = tw64;
+    const double2* twy = twx + nx;
+    const double2* twz = twy + ny;
+    const size_t V = (size_t)nx * ny * nz;
+    complexify_kernel<<<(unsigned)((V + 255) / 256), 256, 0, s>>>(rgrid_t, cbuf, V);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    auto lines = [&](double2* data, const double2* tw, const BoxPlan& pl, long n_lines, long es, long ic, long is,
+                     long os) -> cudaError_t {
+        const size_t sm = ((size_t)pl.n + (size_t)kBoxWarps * 2 * pl.n) * sizeof(double2);
+        cudaError_t e2 = set_smem((const void*)box_line_fft64_kernel, sm);
+        if (e2 != cudaSuccess) return e2;
+        const long blocks = (n_lines + kBoxWarps - 1) / kBoxWarps;
+        box_line_fft64_kernel<<<(unsigned)blocks, 32 * kBoxWarps, sm, s>>>(data, tw, pl, n_lines, es, ic, is, os);
+        return cudaGetLastError();
+    };
+    // z: lines (x, y), contiguous
+    if ((e = lines(cbuf, twz, pz, (long)nx * ny, 1, 1, 0, nz)) != cudaSuccess) return e;
+    const size_t nh = (size_t)nx * ny * hz;
+    box_half_extract_kernel<<<(unsigned)((nh + 255) / 256), 256, 0, s>>>(cbuf, hbuf, nx, ny, nz, hz);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // y: lines (x, kz) of [Nx][Ny][Hz]
+    if ((e = lines(hbuf, twy, py, (long)nx * hz, hz, hz, 1, (long)ny * hz)) != cudaSuccess) return e;
+    // x: lines p = (ky, kz)
+    if ((e = lines(hbuf, twx, px, (long)ny * hz, (long)ny * hz, (long)ny * hz, 1, 0)) != cudaSuccess) return e;
+    const size_t tot = (size_t)nx * PP;
+    pack_spectrum_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(hbuf, static_cast<float2*>(spec_t), nx,
+                                                                       ny * hz, PP, 1.0 / (double)V);
+    return cudaGetLastError();
+}
+
+const SizeOps* box_ops() {
+    static const SizeOps o{0, nullptr, nullptr, false, &box_scan_batch, &box_pencil_smem_unknown, &box_prep,
+                           &box_middle, &box_finish, &box_load_kernels};
+    return &o;
+}
+
+}  // namespace fftdock

@@ -135,7 +135,7 @@ template <int N> struct SizeOpsImpl {
     static cudaError_t prep(const BatchArgs& a, cudaStream_t s) {
         const int nb = a.n_rot;
         if (nb <= 0) return cudaSuccess;
-        Geo geo{a.h, a.zero_h, a.center0, N};
+        const Geo geo = make_geo(a.h, N, N, N);
         const size_t sm1 = ((size_t)a.K * N + 1) * sizeof(int32_t) + (size_t)a.n_ent * sizeof(uint32_t);
         cudaError_t e = set_smem((const void*)ligand_prep_kernel<N>, sm1);
         if (e != cudaSuccess) return e;

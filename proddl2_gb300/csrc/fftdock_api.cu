@@ -45,6 +45,13 @@ struct fftdock_ctx {
     int N = 0, H = 0, PP = 0, K = 0, B = 0;
     size_t V = 0;
     double h = 0, zero_h = 0, center0 = 0;
+    // per-axis sizes and geometry (all N on a cubic grid); box: the box-grid
+    // path (box_grid.cu) with its per-axis twiddle tables [Nx | Ny | Nz]
+    int dims[3] = {0, 0, 0};
+    fftdock::Geo geo{};
+    bool box = false;
+    float2* btw32 = nullptr;
+    double2* btw64 = nullptr;
     cudaStream_t stream = nullptr;
     std::string err;
 
@@ -212,6 +219,8 @@ BatchArgs batch_args(fftdock_ctx* ctx) {
     a.n_pad = ctx->n_pad;
     a.err = ctx->err_dev;
     a.wide = ctx->wide;
+    a.box = ctx->box ? ctx->geo : fftdock::Geo{};
+    a.box_tw32 = ctx->btw32;
     return a;
 }
 
@@ -400,6 +409,7 @@ int ctx_scan_inputs(fftdock_ctx* ctx, ScanInputs* in) {
     in->B = ctx->B;
     in->n_ent = ctx->n_ent;
     in->noalloc_scratch = ctx->noalloc_scratch;
+    in->box = ctx->box;
     return FFTDOCK_OK;
 }
 
@@ -459,6 +469,22 @@ const char* fftdock_last_error(const fftdock_ctx* ctx) { return ctx ? ctx->err.c
 
 int fftdock_grid_n(const fftdock_ctx* ctx) { return ctx ? ctx->N : 0; }
 
+int fftdock_grid_dims(const fftdock_ctx* ctx, int32_t* dims3) {
+    if (!ctx || !dims3) return FFTDOCK_EINVAL;
+    for (int d = 0; d < 3; ++d) dims3[d] = ctx->dims[d];
+    return FFTDOCK_OK;
+}
+
+int fftdock_supported_dims(int32_t nx, int32_t ny, int32_t nz) {
+    if (nx == ny && ny == nz && fftdock::size_ops(nx)) return 1;
+    const int n[3] = {nx, ny, nz};
+    for (int d = 0; d < 3; ++d) {
+        fftdock::BoxPlan pl;
+        if (n[d] < fftdock::kBoxMin || n[d] > fftdock::kBoxMax || !fftdock::box_plan(n[d], &pl)) return 0;
+    }
+    return 1;
+}
+
 int fftdock_get_scan_info(const fftdock_ctx* ctx, fftdock_scan_info* out) {
     if (!ctx || !out) return FFTDOCK_EINVAL;
     out->grid_n = ctx->N;
@@ -476,6 +502,8 @@ void fftdock_destroy(fftdock_ctx* ctx) {
     if (!ctx) return;
     dfree(ctx->tw32);
     dfree(ctx->tw64);
+    dfree(ctx->btw32);
+    dfree(ctx->btw64);
     dfree(ctx->spec);
     dfree(ctx->rgrid);
     dfree(ctx->emat);
@@ -523,11 +551,36 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
         return fail(ctx, FFTDOCK_EINVAL, "fftdock_config.struct_size does not match this library");
     fftdock_config& c = ctx->cfg;
     c = *cfg_in;
-    ctx->ops = fftdock::size_ops(c.grid_n);
-    if (!ctx->ops) return fail(ctx, FFTDOCK_EUNSUPPORTED, "grid_n " + std::to_string(c.grid_n) + " is not built");
+    // FFT sizes per axis: a compiled cubic edge runs the cubic kernels, any
+    // other sizes the box-grid kernels
+    int dims[3] = {c.grid_n, c.grid_n, c.grid_n};
+    if (c.grid_nx != 0 || c.grid_ny != 0 || c.grid_nz != 0) {
+        dims[0] = c.grid_nx;
+        dims[1] = c.grid_ny;
+        dims[2] = c.grid_nz;
+    }
+    const std::string dims_s = std::to_string(dims[0]) + " x " + std::to_string(dims[1]) + " x " +
+                               std::to_string(dims[2]);
+    if (dims[0] == dims[1] && dims[1] == dims[2]) ctx->ops = fftdock::size_ops(dims[0]);
+    if (!ctx->ops) {
+        if (!fftdock_supported_dims(dims[0], dims[1], dims[2]))
+            return fail(ctx, FFTDOCK_EUNSUPPORTED, "grid " + dims_s + " is not supported: each size must be in [" +
+                                                       std::to_string(fftdock::kBoxMin) + ", " +
+                                                       std::to_string(fftdock::kBoxMax) +
+                                                       "] with no prime factor above 13");
+        ctx->ops = fftdock::box_ops();
+        ctx->box = true;
+        if (c.pencil_mode == FFTDOCK_PENCIL_TENSOR)
+            return fail(ctx, FFTDOCK_EUNSUPPORTED, "box grids (" + dims_s + ") run the FFT pencil stage");
+        if (c.precision != FFTDOCK_PREC_FP32)
+            return fail(ctx, FFTDOCK_EUNSUPPORTED, "box grids keep FP32 receptor spectra");
+        if (c.cluster_trans || c.peaks_per_rot > fftdock::kKC)
+            return fail(ctx, FFTDOCK_EUNSUPPORTED,
+                        "box grids keep up to 16 peaks per rotation without clustering (grid " + dims_s + ")");
+    }
     if (!(c.grid_step > 0.0) || !std::isfinite(c.grid_step)) return fail(ctx, FFTDOCK_EINVAL, "grid_step must be > 0");
-    if (c.peaks_per_rot < 1 || c.peaks_per_rot > fftdock::kKC)
-        return fail(ctx, FFTDOCK_EINVAL, "peaks_per_rot must be in [1, 16]");
+    if (c.peaks_per_rot < 1 || c.peaks_per_rot > FFTDOCK_MAX_PEAKS)
+        return fail(ctx, FFTDOCK_EINVAL, "peaks_per_rot must be in [1, " + std::to_string(FFTDOCK_MAX_PEAKS) + "]");
     if (c.max_trans_inp < 1) return fail(ctx, FFTDOCK_EINVAL, "max_trans_inp must be >= 1");
     if (c.rot_batch < 1 || c.rot_batch > 1024) return fail(ctx, FFTDOCK_EINVAL, "rot_batch must be in [1, 1024]");
     if (c.precision != FFTDOCK_PREC_FP32 && c.precision != FFTDOCK_PREC_BF16_SPECTRA)
@@ -583,11 +636,12 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
         return fail(ctx, FFTDOCK_EINVAL, "unknown term_set");
     }
     c.ace_matrix = nullptr;
-    const int N = c.grid_n;
+    const int N = dims[0];
     ctx->N = N;
-    ctx->H = N / 2 + 1;
-    ctx->PP = fftdock::pencil_pitch(N);
-    ctx->V = (size_t)N * N * N;
+    for (int d = 0; d < 3; ++d) ctx->dims[d] = dims[d];
+    ctx->H = dims[2] / 2 + 1;
+    ctx->PP = ctx->box ? (dims[1] * ctx->H + 31) / 32 * 32 : fftdock::pencil_pitch(N);
+    ctx->V = (size_t)dims[0] * dims[1] * dims[2];
     ctx->B = c.rot_batch;
     // the tensor stage takes rotations in groups of 128
     if (ctx->use_tc) ctx->B = (ctx->B + fftdock::kTcRot - 1) / fftdock::kTcRot * fftdock::kTcRot;
@@ -599,6 +653,7 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
     ctx->h = h;
     ctx->zero_h = zero - h;
     ctx->center0 = zero + h / 2.0;
+    ctx->geo = fftdock::make_geo(h, dims[0], dims[1], dims[2]);
 
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
@@ -628,6 +683,22 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
     CK(dalloc(&ctx->tw64, N));
     CK(cudaMemcpy(ctx->tw32, tw32.data(), N * sizeof(float2), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->tw64, tw64.data(), N * sizeof(double2), cudaMemcpyHostToDevice));
+    if (ctx->box) {
+        // one table per axis, e^{-2 pi i k / n_d}, concatenated [Nx | Ny | Nz]
+        const int nt = dims[0] + dims[1] + dims[2];
+        std::vector<float2> b32;
+        std::vector<double2> b64;
+        for (int d = 0; d < 3; ++d)
+            for (int k = 0; k < dims[d]; ++k) {
+                const double cr = fftdock::cos2pi(k, dims[d]), si = -fftdock::sin2pi(k, dims[d]);
+                b32.push_back(make_float2((float)cr, (float)si));
+                b64.push_back(make_double2(cr, si));
+            }
+        CK(dalloc(&ctx->btw32, nt));
+        CK(dalloc(&ctx->btw64, nt));
+        CK(cudaMemcpy(ctx->btw32, b32.data(), nt * sizeof(float2), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(ctx->btw64, b64.data(), nt * sizeof(double2), cudaMemcpyHostToDevice));
+    }
     if (!ctx->ace.empty()) {
         CK(dalloc(&ctx->emat, ctx->ace.size()));
         CK(cudaMemcpy(ctx->emat, ctx->ace.data(), ctx->ace.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -650,15 +721,20 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
         CK(dalloc(&ctx->circ, (size_t)ctx->K * N * ctx->H * N));
         CK(dalloc(&ctx->cscale, (size_t)N * ctx->H));
     }
-    if (c.cluster_trans) {
+    // more peaks per rotation than the per-plane pools hold: the exact-queue
+    // path, without clustering, over the first peaks_per_rot + 16 cells of
+    // the queue (CorrelationProcessor's queue of maxNTransInp cells, of which
+    // getTranValuesFilled keeps the first maxNTrans; docking_fft.hpp:430-468)
+    const bool deep = !c.cluster_trans && c.peaks_per_rot > fftdock::kKC;
+    if (c.cluster_trans || deep) {
         fftdock::WideArgs& w = ctx->wide;
         CK(dalloc(&w.corr, (size_t)ctx->B * ctx->V));
         CK(dalloc(&w.hist, (size_t)ctx->B * fftdock::kWideBins));
         CK(dalloc(&w.st, (size_t)ctx->B));
         CK(dalloc(&w.cand, (size_t)ctx->B * fftdock::kWideMax));
         CK(dalloc(&w.cnt, (size_t)ctx->B));
-        w.m = c.max_trans_inp;
-        w.order = c.cluster_order;
+        w.m = deep ? std::min(c.max_trans_inp, c.peaks_per_rot + fftdock::kKC) : c.max_trans_inp;
+        w.order = deep ? fftdock::kWideNoClustering : c.cluster_order;
         // ClusterMatrix::cluster: cutoff2 = r^2 * 3 columns, cutoff = sqrt,
         // compared as cutoff * cutoff (Geom/cluster.hpp:153-156)
         const double cut = std::sqrt((c.cluster_radius * c.cluster_radius) * 3.0);
@@ -686,7 +762,7 @@ int fftdock_set_receptor(fftdock_ctx* ctx, int32_t n, const double* xyz, const i
     const int N = ctx->N;
     const size_t V = ctx->V;
     cudaStream_t s = ctx->stream;
-    fftdock::Geo g{ctx->h, ctx->zero_h, ctx->center0, N};
+    const fftdock::Geo g = ctx->geo;
     double* d_xyz = nullptr;
     int32_t* d_type = nullptr;
     int* flags = nullptr;
@@ -766,13 +842,17 @@ int fftdock_set_receptor(fftdock_ctx* ctx, int32_t n, const double* xyz, const i
         CKR(fftdock::build_receptor_grids(ra, s));
     }
     CKR(dalloc(&cbuf, V));
-    CKR(dalloc(&hbuf, (size_t)N * N * ctx->H));
+    CKR(dalloc(&hbuf, (size_t)ctx->dims[0] * ctx->dims[1] * ctx->H));
     for (int t = 0; t < ctx->K; ++t) {
         const size_t elem = c.precision == FFTDOCK_PREC_BF16_SPECTRA ? 4 : 8;
-        CKR(ctx->ops->receptor_fft(ctx->rgrid + (size_t)t * V, cbuf, hbuf, ctx->tw64,
-                                   static_cast<unsigned char*>(ctx->spec) + (size_t)t * N * ctx->PP * elem,
-                                   c.precision == FFTDOCK_PREC_BF16_SPECTRA ? 1 : 0, ctx->PP,
-                                   ctx->use_tc ? ctx->circ + (size_t)t * N * ctx->H * N : nullptr, s));
+        void* spec_t = static_cast<unsigned char*>(ctx->spec) + (size_t)t * N * ctx->PP * elem;
+        if (ctx->box)
+            CKR(fftdock::box_receptor_fft(ctx->rgrid + (size_t)t * V, cbuf, hbuf, ctx->btw64, ctx->dims, spec_t,
+                                          ctx->PP, s));
+        else
+            CKR(ctx->ops->receptor_fft(ctx->rgrid + (size_t)t * V, cbuf, hbuf, ctx->tw64, spec_t,
+                                       c.precision == FFTDOCK_PREC_BF16_SPECTRA ? 1 : 0, ctx->PP,
+                                       ctx->use_tc ? ctx->circ + (size_t)t * N * ctx->H * N : nullptr, s));
     }
     if (ctx->use_tc) CKR(ctx->ops->circ_scales(ctx->circ, ctx->K, ctx->cscale, s));
     CKR(cudaStreamSynchronize(s));
@@ -798,7 +878,9 @@ int fftdock_set_ligand(fftdock_ctx* ctx, int32_t n, const double* xyz, const int
             term[i] = type[i];
         }
     }
-    if (ctx->ops->pencil_smem(ctx->K, n) > fftdock::kMaxSmem)
+    const size_t smem = ctx->box ? fftdock::box_pencil_smem(ctx->dims[0], ctx->dims[1], ctx->dims[2], ctx->K, n, false)
+                                 : ctx->ops->pencil_smem(ctx->K, n);
+    if (smem > fftdock::kMaxSmem)
         return fail(ctx, FFTDOCK_EINVAL, "ligand too large for the pencil kernel's shared memory");
     fftdock::DeviceScope dev_scope(c.device);
     CK(dev_scope.status());
@@ -812,7 +894,8 @@ int fftdock_set_ligand(fftdock_ctx* ctx, int32_t n, const double* xyz, const int
     CK(dalloc(&ctx->ent, (size_t)ctx->G * n));
     CK(cudaMemcpy(ctx->lig_xyz, xyz, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->lig_term, term.data(), (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice));
-    const fftdock::TcTables tt = fftdock::tc_tables(xyz, term.data(), n, ctx->K, ctx->N, ctx->h, ctx->zero_h);
+    const fftdock::TcTables tt = ctx->box ? fftdock::TcTables{}
+                                          : fftdock::tc_tables(xyz, term.data(), n, ctx->K, ctx->N, ctx->h, ctx->zero_h);
     ctx->x0 = tt.x0;
     ctx->W = tt.W;
     ctx->n_ent = n;
@@ -879,7 +962,10 @@ int fftdock_set_pair_lj(fftdock_ctx* ctx, int32_t n_rec, const double* rec_xyz, 
     const bool comp = c.term_set == FFTDOCK_TERMS_LJ_COMP;
     const int n_ent = comp ? 2 * n_lig : n_lig;
     if (n_ent > fftdock::kMaxEntries) return fail(ctx, FFTDOCK_EINVAL, "too many ligand entries (2 per atom for ljComp)");
-    if (ctx->ops->pencil_smem(ctx->K, n_ent) + (comp ? (size_t)n_ent * sizeof(float) : 0) > fftdock::kMaxSmem)
+    const size_t smem = ctx->box ? fftdock::box_pencil_smem(ctx->dims[0], ctx->dims[1], ctx->dims[2], ctx->K, n_ent,
+                                                            comp)
+                                 : ctx->ops->pencil_smem(ctx->K, n_ent) + (comp ? (size_t)n_ent * sizeof(float) : 0);
+    if (smem > fftdock::kMaxSmem)
         return fail(ctx, FFTDOCK_EINVAL, "ligand too large for the pencil kernel's shared memory");
 
     // receptor field constants
@@ -972,7 +1058,7 @@ int fftdock_set_pair_lj(fftdock_ctx* ctx, int32_t n_rec, const double* rec_xyz, 
         fftdock::ReceptorGridArgs ra{};
         ra.xyz = d_xyz;
         ra.n = n_rec;
-        ra.geo = fftdock::Geo{ctx->h, ctx->zero_h, ctx->center0, N};
+        ra.geo = ctx->geo;
         ra.term_set = c.term_set;
         ra.K = ctx->K;
         for (int d = 0; d < 3; ++d) {
@@ -989,11 +1075,16 @@ int fftdock_set_pair_lj(fftdock_ctx* ctx, int32_t n_rec, const double* rec_xyz, 
         CKR(fftdock::build_receptor_grids(ra, s));
     }
     CKR(dalloc(&cbuf, V));
-    CKR(dalloc(&hbuf, (size_t)N * N * ctx->H));
-    for (int t = 0; t < ctx->K; ++t)
-        CKR(ctx->ops->receptor_fft(ctx->rgrid + (size_t)t * V, cbuf, hbuf, ctx->tw64,
-                                   static_cast<unsigned char*>(ctx->spec) + (size_t)t * N * ctx->PP * 8, 0, ctx->PP,
-                                   nullptr, s));
+    CKR(dalloc(&hbuf, (size_t)ctx->dims[0] * ctx->dims[1] * ctx->H));
+    for (int t = 0; t < ctx->K; ++t) {
+        void* spec_t = static_cast<unsigned char*>(ctx->spec) + (size_t)t * N * ctx->PP * 8;
+        if (ctx->box)
+            CKR(fftdock::box_receptor_fft(ctx->rgrid + (size_t)t * V, cbuf, hbuf, ctx->btw64, ctx->dims, spec_t,
+                                          ctx->PP, s));
+        else
+            CKR(ctx->ops->receptor_fft(ctx->rgrid + (size_t)t * V, cbuf, hbuf, ctx->tw64, spec_t, 0, ctx->PP,
+                                       nullptr, s));
+    }
     CKR(cudaStreamSynchronize(s));
     cleanup();
 #undef CKR

@@ -38,13 +38,28 @@ class DeviceScope {
 __host__ __device__ constexpr int pencil_pitch(int n) { return (n * (n / 2 + 1) + 31) / 32 * 32; }
 
 // Grid geometry of the reference's centred UniformCubicGeometry
-// (include/PRODDL/Grid/gridcoord.hpp:127-191).
+// (include/PRODDL/Grid/gridcoord.hpp:127-191): cubic cells of step h, a
+// logical size per axis (fftSize, docking_fft.hpp:541-553), centred per axis.
 struct Geo {
-    double h;        // step
-    double zero_h;   // spatial zero - h (toLogical)
-    double center0;  // centre of cell 0 (toSpatial)
-    int n;
+    double h;           // step
+    double zero_h[3];   // per axis: spatial zero - h (toLogical)
+    double center0[3];  // per axis: centre of cell 0 (toSpatial)
+    int n[3];           // logical size per axis
 };
+// UniformCubicGeometry(step, logicalSize): per axis zero = -(h + h (n - 1)) / 2
+inline Geo make_geo(double h, int nx, int ny, int nz) {
+    Geo g{};
+    g.h = h;
+    const int n[3] = {nx, ny, nz};
+    for (int d = 0; d < 3; ++d) {
+        const double s_size = h + h * (double)(n[d] - 1);
+        const double zero = (-1.0 * s_size) / 2.0;
+        g.zero_h[d] = zero - h;
+        g.center0[d] = zero + h / 2.0;
+        g.n[d] = n[d];
+    }
+    return g;
+}
 
 // Receptor atoms sorted into cubic bins of edge >= the desolvation cutoff
 // (host-built counting sort, atoms in index order inside each bin), so that
@@ -114,6 +129,12 @@ struct WideState {
 };
 constexpr int kWideAll = 1;    // fewer than m cells pass: keep them all
 constexpr int kWideRadix = 2;  // the bound was too loose: radix path
+// The same exact queue without clustering serves more than KC peaks per
+// rotation: the whole queue (at most kWidePool cells) is rescored in FP64,
+// sorted by (energy, offset) and the first peaks_per_rot below maxValCorr
+// are kept, like the per-plane pool path does for up to KC peaks.
+constexpr int kWideNoClustering = -1;
+constexpr int kWidePool = 512;
 
 struct WideArgs {
     float* corr;               // [B][N^3] correlation grids (nullptr: wide path off)
@@ -122,9 +143,21 @@ struct WideArgs {
     unsigned long long* cand;  // [B][kWideMax] gathered keys
     int32_t* cnt;              // [B]
     int m;                     // queue bound, 1..kWideMax
-    int order;                 // FFTDOCK_CLUSTER_ORDER_*
+    int order;                 // FFTDOCK_CLUSTER_ORDER_*, or kWideNoClustering
     double rad2;               // squared neighbour radius of the clustering
 };
+
+// Mixed-radix plan of one transform length of the box-grid path: radices in
+// Stockham stage order (4, 2, 3, 5, 7, 11, 13).
+constexpr int kBoxMaxFactors = 12;
+struct BoxPlan {
+    int n;
+    int nf;
+    int f[kBoxMaxFactors];
+};
+// Box-grid sizes each axis may take: [kBoxMin, kBoxMax], factors 2..13.
+constexpr int kBoxMin = 8;
+constexpr int kBoxMax = 256;
 
 // Everything one device batch of rotations needs.
 struct BatchArgs {
@@ -179,6 +212,10 @@ struct BatchArgs {
     int n_pad;                  // entries per rotation with every term padded to a multiple of 8
     int* err;                   // device word: nonzero after a pipeline timeout
     WideArgs wide;              // queue + clustering path (wide.corr != nullptr)
+    // box-grid path (box.n[0] > 0): per-axis geometry and the FP32 twiddle
+    // tables of the three axes, [Nx | Ny | Nz]
+    Geo box;
+    const float2* box_tw32;
 };
 
 // The tensor pencil stage's per-ligand tables: the x window [x0, x0 + W)
@@ -230,6 +267,17 @@ struct SizeOps {
 
 const SizeOps* size_ops(int n);
 
+// Box grids (box_grid.cu): sizes per axis, any length of factors 2..13 in
+// [kBoxMin, kBoxMax]; the pipeline's stages read the sizes from BatchArgs.box.
+const SizeOps* box_ops();
+bool box_plan(int n, BoxPlan* pl);
+// largest dynamic shared memory of the box-grid kernels for a ligand
+size_t box_pencil_smem(int nx, int ny, int nz, int K, int n_ent, bool weighted);
+// forward transform of one real FP64 term grid into spec_t ([Nx][PP] float2,
+// scaled 1/V); tw64 = the FP64 twiddle tables [Nx | Ny | Nz]
+cudaError_t box_receptor_fft(const double* rgrid_t, double2* cbuf, double2* hbuf, const double2* tw64,
+                             const int dims[3], void* spec_t, int PP, cudaStream_t s);
+
 // Read-only view of a ready context's scan inputs (receptor spectra and
 // grids, ligand, geometry); the work pointers of `args` are the context's own.
 struct ScanInputs {
@@ -239,6 +287,7 @@ struct ScanInputs {
     cudaStream_t stream;
     int N, K, PP, B, n_ent;
     void* noalloc_scratch;  // the no-allocation scan's array in the context's CUDA context
+    bool box;               // a box-grid context
 };
 int ctx_scan_inputs(fftdock_ctx* ctx, ScanInputs* in);
 // Device address, in the current CUDA context, of the no-allocation scan's

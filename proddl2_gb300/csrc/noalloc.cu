@@ -80,6 +80,8 @@ extern "C" int fftdock_scan_device_noalloc(fftdock_ctx* ctx, int32_t n_rot, cons
     if (in.args.lig_w32)
         return fftdock::ctx_fail(ctx, FFTDOCK_EUNSUPPORTED,
                                  "weighted ligand entries (ljComp) are not covered by the no-allocation scan");
+    if (in.box)
+        return fftdock::ctx_fail(ctx, FFTDOCK_EUNSUPPORTED, "box grids are not covered by the no-allocation scan");
     if (in.args.wide.corr)
         return fftdock::ctx_fail(ctx, FFTDOCK_EUNSUPPORTED,
                                  "translational clustering needs a full correlation grid per rotation; the "

@@ -227,7 +227,7 @@ cudaError_t enqueue_pair(Run& r, const fftdock_pair& p, int i, Work& w, const Si
                          int rot_n, cudaStream_t s) {
     const fftdock_config& c = r.cfg;
     const int N = sd.N;
-    fftdock::Geo g{c.grid_step, sd.zero_h, sd.center0, N};
+    const fftdock::Geo g = fftdock::make_geo(c.grid_step, N, N, N);
     fftdock::ReceptorGridArgs ra{};
     ra.xyz = r.st.rec_xyz + 3 * r.st.rec_off[i];
     ra.type = r.ace ? r.st.rec_type + r.st.rec_off[i] : nullptr;

@@ -21,19 +21,19 @@ struct Box {
 };
 __device__ __forceinline__ bool projection_box(const double* c, double cut, const Geo& g, Box& b) {
     for (int d = 0; d < 3; ++d) {
-        int lo = logical_q(__dsub_rn(c[d], cut), g) - 1;
-        int hi = logical_q(__dadd_rn(c[d], cut), g) - 1;
+        int lo = logical_q(__dsub_rn(c[d], cut), g, d) - 1;
+        int hi = logical_q(__dadd_rn(c[d], cut), g, d) - 1;
         b.lo[d] = max(lo, 0);
-        b.hi[d] = min(hi, g.n - 1);
+        b.hi[d] = min(hi, g.n[d] - 1);
         if (b.lo[d] > b.hi[d]) return false;
     }
     return true;
 }
 
 __device__ __forceinline__ double dist2(const double* c, int ix, int iy, int iz, const Geo& g) {
-    const double dx = __dsub_rn(cell_centre(ix, g), c[0]);
-    const double dy = __dsub_rn(cell_centre(iy, g), c[1]);
-    const double dz = __dsub_rn(cell_centre(iz, g), c[2]);
+    const double dx = __dsub_rn(cell_centre(ix, g, 0), c[0]);
+    const double dy = __dsub_rn(cell_centre(iy, g, 1), c[1]);
+    const double dz = __dsub_rn(cell_centre(iz, g, 2), c[2]);
     return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
 
@@ -51,7 +51,7 @@ __global__ void shape_flags_kernel(const double* __restrict__ xyz, int n, Geo g,
         const int ix = b.lo[0] + i / (ny * nz), iy = b.lo[1] + (i / nz) % ny, iz = b.lo[2] + i % nz;
         const double r2 = dist2(c, ix, iy, iz, g);
         const int f = r2 <= rc2 ? 2 : (r2 <= rs2 ? 1 : 0);
-        if (f) atomicMax(&flags[((size_t)ix * g.n + iy) * g.n + iz], f);
+        if (f) atomicMax(&flags[((size_t)ix * g.n[1] + iy) * g.n[2] + iz], f);
     }
 }
 
@@ -78,14 +78,15 @@ __global__ void atom_box_kernel(const double* __restrict__ xyz, int n, Geo g, do
 __global__ void ace_density_kernel(const double* __restrict__ xyz, const int32_t* __restrict__ type,
                                    const int* __restrict__ box, AtomBins bins, Geo g, double cut2, double mind2,
                                    double ab, double ak, double aa, double* __restrict__ dens) {
-    const size_t V = (size_t)g.n * g.n * g.n;
+    const size_t V = (size_t)g.n[0] * g.n[1] * g.n[2];
     const size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (cell >= V) return;
-    const int ix = (int)(cell / ((size_t)g.n * g.n)), iy = (int)((cell / g.n) % g.n), iz = (int)(cell % g.n);
+    const int ix = (int)(cell / ((size_t)g.n[1] * g.n[2])), iy = (int)((cell / g.n[2]) % g.n[1]),
+              iz = (int)(cell % g.n[2]);
     const int ic[3] = {ix, iy, iz};
     int b0[3];
     for (int d = 0; d < 3; ++d) {
-        const double t = floor((cell_centre(ic[d], g) - bins.lo[d]) / bins.size);
+        const double t = floor((cell_centre(ic[d], g, d) - bins.lo[d]) / bins.size);
         b0[d] = t < -2.0 ? -2 : (t > (double)bins.nb[d] + 1.0 ? bins.nb[d] + 1 : (int)t);
     }
     for (int bx = max(b0[0] - 1, 0); bx <= min(b0[0] + 1, bins.nb[0] - 1); ++bx)
@@ -120,14 +121,15 @@ template <int K>
 __global__ void lj_field_kernel(const double* __restrict__ xyz, const double* __restrict__ lc,
                                 const int* __restrict__ box, AtomBins bins, Geo g, double cut2, double mind2,
                                 double* __restrict__ rgrid) {
-    const size_t V = (size_t)g.n * g.n * g.n;
+    const size_t V = (size_t)g.n[0] * g.n[1] * g.n[2];
     const size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (cell >= V) return;
-    const int ix = (int)(cell / ((size_t)g.n * g.n)), iy = (int)((cell / g.n) % g.n), iz = (int)(cell % g.n);
+    const int ix = (int)(cell / ((size_t)g.n[1] * g.n[2])), iy = (int)((cell / g.n[2]) % g.n[1]),
+              iz = (int)(cell % g.n[2]);
     const int ic[3] = {ix, iy, iz};
     int b0[3];
     for (int d = 0; d < 3; ++d) {
-        const double t = floor((cell_centre(ic[d], g) - bins.lo[d]) / bins.size);
+        const double t = floor((cell_centre(ic[d], g, d) - bins.lo[d]) / bins.size);
         b0[d] = t < -2.0 ? -2 : (t > (double)bins.nb[d] + 1.0 ? bins.nb[d] + 1 : (int)t);
     }
     double acc0 = 0.0, acc1 = 0.0;
@@ -183,7 +185,7 @@ __global__ void mix_terms_kernel(const int* __restrict__ flags, const double* __
 }  // namespace
 
 cudaError_t build_receptor_grids(const ReceptorGridArgs& a, cudaStream_t s) {
-    const size_t V = (size_t)a.geo.n * a.geo.n * a.geo.n;
+    const size_t V = (size_t)a.geo.n[0] * a.geo.n[1] * a.geo.n[2];
     if (a.term_set == FFTDOCK_TERMS_LJ_COMP || a.term_set == FFTDOCK_TERMS_LJ_AVG) {
         const double md = a.geo.h / 4.0;
         cudaError_t e = cudaSuccess;

@@ -55,11 +55,11 @@ template <> struct PencilTraits<144> { static constexpr int BUFS = 2, MINB = 2; 
 
 // toLogical: int((x - zero_h) / h) - 1, truncation toward zero, no FMA.
 // Returns the truncated quotient; the cell is q - 1.
-__device__ __forceinline__ int logical_q(double x, const Geo& g) {
-    return __double2int_rz(__ddiv_rn(__dsub_rn(x, g.zero_h), g.h));
+__device__ __forceinline__ int logical_q(double x, const Geo& g, int d) {
+    return __double2int_rz(__ddiv_rn(__dsub_rn(x, g.zero_h[d]), g.h));
 }
-__device__ __forceinline__ double cell_centre(int i, const Geo& g) {
-    return __dadd_rn(g.center0, __dmul_rn(g.h, (double)i));
+__device__ __forceinline__ double cell_centre(int i, const Geo& g, int d) {
+    return __dadd_rn(g.center0[d], __dmul_rn(g.h, (double)i));
 }
 
 // ---------------------------------------------------------------------------
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(256) ligand_prep_kernel(
         const double p0 = __dadd_rn(__dadd_rn(__dmul_rn(m00, x0), __dmul_rn(m01, x1)), __dmul_rn(m02, x2));
         const double p1 = __dadd_rn(__dadd_rn(__dmul_rn(m10, x0), __dmul_rn(m11, x1)), __dmul_rn(m12, x2));
         const double p2 = __dadd_rn(__dadd_rn(__dmul_rn(m20, x0), __dmul_rn(m21, x1)), __dmul_rn(m22, x2));
-        int c0 = logical_q(p0, geo), c1 = logical_q(p1, geo), c2 = logical_q(p2, geo);
+        int c0 = logical_q(p0, geo, 0), c1 = logical_q(p1, geo, 1), c2 = logical_q(p2, geo, 2);
         const bool ok = c0 >= 1 && c0 <= N && c1 >= 1 && c1 <= N && c2 >= 1 && c2 <= N;
         if (!ok) atomicOr(&bad, 1);
         c0 = min(max(c0 - 1, 0), N - 1);

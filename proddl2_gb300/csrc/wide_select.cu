@@ -45,7 +45,8 @@ constexpr int kPassThreads = 256;
 constexpr int kDigitBits = 12;
 constexpr int kMaxPasses = 6;  // 5 x 12 + 4 = 64 key bits
 constexpr int kFinishThreads = 1024;
-constexpr int kMaxLeaders = 16;
+constexpr int kMaxLeaders = FFTDOCK_MAX_PEAKS;
+static_assert(kMaxLeaders <= kWidePool, "the leader arrays hold at most kWidePool entries");
 constexpr int kPoolPerPlane = 16;  // KC of the plane kernel
 constexpr int kPoolMax = 4096;     // >= 16 * largest grid edge, power of two
 
@@ -309,13 +310,15 @@ __device__ __forceinline__ double dist2(const double* a, double bx, double by, d
 __global__ void __launch_bounds__(kFinishThreads) wide_finish_kernel(
     const u64* __restrict__ cand, const int32_t* __restrict__ cnt, const uint32_t* __restrict__ ent,
     const int32_t* __restrict__ status, const double* __restrict__ rgrid, int n_ent, int N, int m, int order,
-    double rad2, int max_out, int peak_stride, double h, int first_rot_id, fftdock_peak* __restrict__ peaks,
-    int32_t* __restrict__ n_peaks, const double* __restrict__ w64, const int32_t* __restrict__ ent_idx) {
+    double rad2, int max_out, int k_out, double max_val, int peak_stride, double h, int first_rot_id,
+    fftdock_peak* __restrict__ peaks, int32_t* __restrict__ n_peaks, const double* __restrict__ w64,
+    const int32_t* __restrict__ ent_idx) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     u64* keys = reinterpret_cast<u64*>(smem_raw);  // [kWideMax]
-    __shared__ int lead_pos[kMaxLeaders];
+    __shared__ int lead_pos[kWidePool];
     __shared__ double lead_t[kMaxLeaders][3];
-    __shared__ double score_s[kMaxLeaders];
+    __shared__ double score_s[kWidePool];
+    __shared__ int off_s[kWidePool];
     __shared__ int n_lead_s;
     const int q = blockIdx.x;
     const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
@@ -344,7 +347,12 @@ __global__ void __launch_bounds__(kFinishThreads) wide_finish_kernel(
         }
     }
     const int me = n < m ? n : m;  // the queue: the first me keys, ascending
-    if (w == 0) {
+    if (order == kWideNoClustering) {
+        // no clustering: every queue entry is a candidate
+        const int nq = me < kWidePool ? me : kWidePool;
+        for (int c = tid; c < nq; c += blockDim.x) lead_pos[c] = c;
+        if (tid == 0) n_lead_s = nq;
+    } else if (w == 0) {
         int nl = 0;
         for (int base = 0; base < me && nl < max_out; base += 32) {
             const int k = base + l;
@@ -381,8 +389,8 @@ __global__ void __launch_bounds__(kFinishThreads) wide_finish_kernel(
     const int nl = n_lead_s;
     // FP64 direct-space rescoring, one warp per leader (same summation as
     // the finalize kernel of the default path)
-    if (w < nl) {
-        const int off = (int)(uint32_t)keys[lead_pos[w]];
+    for (int c = w; c < nl; c += kFinishThreads / 32) {
+        const int off = (int)(uint32_t)keys[lead_pos[c]];
         const uint32_t* e_q = ent + (size_t)q * n_ent;
         const int sx = off / (N * N), sy = (off / N) % N, sz = off % N;
         double sum = 0.0;
@@ -397,9 +405,54 @@ __global__ void __launch_bounds__(kFinishThreads) wide_finish_kernel(
             sum = __dadd_rn(sum, w64 ? __dmul_rn(w64[ent_idx[(size_t)q * n_ent + j]], rv) : rv);
         }
         for (int o = 16; o > 0; o >>= 1) sum = __dadd_rn(sum, __shfl_xor_sync(0xffffffffu, sum, o));
-        if (l == 0) score_s[w] = sum;
+        if (l == 0) score_s[c] = sum;
     }
     __syncthreads();
+    if (order == kWideNoClustering) {
+        // sort the rescored queue by (energy, offset), then the first k_out
+        // below maxValCorr are the peaks, ascending
+        int P2 = 1;
+        while (P2 < nl) P2 <<= 1;
+        for (int i = tid; i < P2; i += blockDim.x) {
+            off_s[i] = i < nl ? (int)(uint32_t)keys[lead_pos[i]] : 0x7fffffff;
+            if (i >= nl) score_s[i] = INFINITY;
+        }
+        __syncthreads();
+        for (int kk = 2; kk <= P2; kk <<= 1)
+            for (int j = kk >> 1; j > 0; j >>= 1) {
+                for (int i = tid; i < P2; i += blockDim.x) {
+                    const int ixj = i ^ j;
+                    if (ixj > i) {
+                        const double a = score_s[i], b = score_s[ixj];
+                        const int oa = off_s[i], ob = off_s[ixj];
+                        const bool a_after = a > b || (a == b && oa > ob);
+                        if (a_after == ((i & kk) == 0)) {
+                            score_s[i] = b;
+                            score_s[ixj] = a;
+                            off_s[i] = ob;
+                            off_s[ixj] = oa;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        if (tid == 0) {
+            int np = 0;
+            if (status[q] == 0) {
+                for (int c = 0; c < nl && np < k_out; ++c) {
+                    if (!(score_s[c] < max_val)) continue;
+                    fftdock_peak pk;
+                    pk.rot_id = first_rot_id + q;
+                    translation_of(off_s[c], N, h, pk.cell, pk.t);
+                    pk.score = score_s[c];
+                    peaks[(size_t)q * peak_stride + np] = pk;
+                    ++np;
+                }
+            }
+            n_peaks[q] = np;
+        }
+        return;
+    }
     if (tid == 0) {
         int np = 0;
         if (status[q] == 0) {
@@ -450,8 +503,9 @@ cudaError_t wide_select_batch(const BatchArgs& a, int N, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     const int max_out = a.k_out < kMaxLeaders ? a.k_out : kMaxLeaders;
     wide_finish_kernel<<<nb, kFinishThreads, sm, s>>>(w.cand, w.cnt, a.ent, a.status, a.rgrid, a.n_ent, N, w.m,
-                                                      w.order, w.rad2, max_out, a.peak_stride, a.h, a.first_rot_id,
-                                                      a.peaks, a.n_peaks, a.lig_w64, a.lig_w64 ? a.ent_idx : nullptr);
+                                                      w.order, w.rad2, max_out, a.k_out, a.max_val, a.peak_stride,
+                                                      a.h, a.first_rot_id, a.peaks, a.n_peaks, a.lig_w64,
+                                                      a.lig_w64 ? a.ent_idx : nullptr);
     return cudaGetLastError();
 }
 

@@ -51,6 +51,7 @@ class ScanConfig:
     lj_mix: int = 1                 # LJ sets: sigma rule (0 arithmetic, 1 geometric; ljComp needs 1)
     lj_cut: float = 9.0             # LJ sets: cutOffFft
     tc_terms_per_sum: int = 0       # tensor form: terms per tensor-memory sum (0: library default)
+    grid_dims: tuple | None = None  # FFT sizes per axis (the reference's fftSize); None: grid_n on every axis
 
     @classmethod
     def from_options(cls, opts: dict, **kw):
@@ -114,6 +115,9 @@ def native_config(config: ScanConfig):
     cfg.lj_mix = int(config.lj_mix)
     cfg.lj_cut = float(config.lj_cut)
     cfg.tc_terms_per_sum = int(config.tc_terms_per_sum)
+    if config.grid_dims is not None:
+        cfg.grid_nx, cfg.grid_ny, cfg.grid_nz = (int(v) for v in config.grid_dims)
+        cfg.grid_n = int(config.grid_dims[0])
     return cfg, ace
 
 
@@ -161,6 +165,13 @@ class FFTScan:
     @property
     def grid_n(self):
         return self.lib.fftdock_grid_n(self._h)
+
+    @property
+    def grid_dims(self):
+        """FFT sizes (nx, ny, nz)."""
+        d = (C.c_int32 * 3)()
+        self._check(self.lib.fftdock_grid_dims(self._h, d))
+        return tuple(int(v) for v in d)
 
     @property
     def n_terms(self):
@@ -235,15 +246,13 @@ class FFTScan:
         return {name: (int(st.launches[i]), float(st.total_ms[i])) for i, name in enumerate(_lib.KERNEL_NAMES)}
 
     def receptor_grid(self, term):
-        n = self.grid_n
-        out = np.empty((n, n, n), dtype=np.float64)
+        out = np.empty(self.grid_dims, dtype=np.float64)
         self._check(self.lib.fftdock_get_receptor_grid(self._h, int(term), _ptr(out)))
         return out
 
     def correlation_grid(self, rotation):
-        n = self.grid_n
         rot = np.ascontiguousarray(rotation, dtype=np.float64).reshape(9)
-        out = np.empty((n, n, n), dtype=np.float32)
+        out = np.empty(self.grid_dims, dtype=np.float32)
         self._check(self.lib.fftdock_correlation_grid(self._h, _ptr(rot), _ptr(out)))
         return out
 
@@ -257,7 +266,14 @@ class FFTScan:
 
 
 def supported_grid(n):
+    """A cubic edge with compiled plans."""
     return bool(_lib.lib().fftdock_supported_grid(int(n)))
+
+
+def supported_dims(dims):
+    """Per-axis FFT sizes the library scans (a compiled cubic edge or box-grid sizes)."""
+    nx, ny, nz = (int(v) for v in dims)
+    return bool(_lib.lib().fftdock_supported_dims(nx, ny, nz))
 
 
 def find_best_size(start_n):

@@ -169,6 +169,10 @@ WORKLOADS = {
     # the reference's default potential (ljComp, K = 2) at the same size
     "ljcomp128": dict(n_rec=4000, n_lig=1500, grid_n=128, grid_step=1.2, term_set="lj_comp",
                       n_rot=9000, rot_batch=64, peaks=4, top=100),
+    # precision study: the 64^3 workload's molecules at 128^3, FP32 vs BF16-stored
+    # receptor spectra, every rotation's 16 best cells rescored in FP64
+    "precision128": dict(n_rec=1800, n_lig=450, grid_n=128, grid_step=1.2, term_set="shape",
+                         n_rot=20000, rot_batch=64, peaks=16, top=100),
     # many uneven pairs: receptors 800-6000 / ligands 300-2000 atoms (log-uniform),
     # grid edge per pair from pair_grid (48-144), shape + 18 desolvation terms
     "pairs256": dict(n_pairs=256, grid_step=1.2, term_set="shape_ace", n_rot=3000, rot_batch=64, peaks=4),

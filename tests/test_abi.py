@@ -105,9 +105,14 @@ def test_create_fails_loudly_without_gpu(built_lib):
 def test_create_rejects_bad_config(built_lib):
     from proddl2_gb300 import FFTScan, ScanConfig, FFTDockError, _lib
     bad = [
-        (dict(grid_n=100), _lib.FFTDOCK_EUNSUPPORTED),
+        (dict(grid_n=97), _lib.FFTDOCK_EUNSUPPORTED),           # prime: no FFT plan
+        (dict(grid_n=300), _lib.FFTDOCK_EUNSUPPORTED),          # beyond the box-grid sizes
+        (dict(grid_dims=(90, 96, 100), pencil_mode="tensor"), _lib.FFTDOCK_EUNSUPPORTED),
+        (dict(grid_dims=(90, 96, 100), cluster_trans=True), _lib.FFTDOCK_EUNSUPPORTED),
+        (dict(grid_dims=(90, 96, 100), peaks_per_rot=17), _lib.FFTDOCK_EUNSUPPORTED),
+        (dict(grid_dims=(90, 96, 102)), _lib.FFTDOCK_EUNSUPPORTED),  # 102 = 2 * 3 * 17
         (dict(grid_n=32, peaks_per_rot=0), _lib.FFTDOCK_EINVAL),
-        (dict(grid_n=32, peaks_per_rot=17), _lib.FFTDOCK_EINVAL),
+        (dict(grid_n=32, peaks_per_rot=257), _lib.FFTDOCK_EINVAL),
         (dict(grid_n=32, grid_step=0.0), _lib.FFTDOCK_EINVAL),
         (dict(grid_n=32, rot_batch=0), _lib.FFTDOCK_EINVAL),
         (dict(grid_n=32, term_set="shape_ace", ace_matrix=None), _lib.FFTDOCK_EINVAL),

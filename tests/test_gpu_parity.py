@@ -335,6 +335,46 @@ def test_out_of_grid_rotations_are_reported(mode):
         assert np.array_equal(alone.peaks[0], res.peaks[1])
 
 
+@pytest.mark.parametrize("mode", ["fft", "tensor"])
+def test_more_than_16_peaks_per_rotation(mode):
+    """peaks_per_rot 32 and 100, above the per-plane pools' 16: the scan
+    keeps each rotation's exact queue; peaks tie-aware against the live FP64
+    oracle's top k; a queue bound (maxNTransInp) below k keeps that many."""
+    from proddl2_gb300 import synth
+    n = 48
+    pair = synth.make_pair(700, 150, 4, seed=41)
+    geom, rg, w = _oracle_setup(n, O.TERMS_SHAPE_ACE, pair.ace, pair.receptor.xyz, pair.receptor.ace_type,
+                                pair.ligand.ace_type)
+    rs = O.receptor_spectra(rg, workers=8)
+    for k in (32, 100):
+        with _scan(n, O.TERMS_SHAPE_ACE, pair.ace, k=k, mode=mode) as s:
+            s.set_receptor(pair.receptor.xyz, pair.receptor.ace_type)
+            s.set_ligand(pair.ligand.xyz, pair.ligand.ace_type)
+            res = s.scan(pair.rotations)
+        assert np.all(res.n_peaks == k)
+        for i, rot in enumerate(pair.rotations):
+            ref = O.scan_rotation(geom, rg, rs, pair.ligand.xyz, w, rot, k, workers=8)
+            cells, _ = O.bin_ligand(geom, rot, pair.ligand.xyz)
+            cell, t, score = res.rotation(i)
+            assert np.all(np.diff(score) >= 0)
+            assert np.array_equal(t, O.translation(cell, geom))
+            off = (cell[:, 0] * n + cell[:, 1]) * n + cell[:, 2]
+            exact = lambda o: O.direct_score(rg, cells, w, O.offsets_to_cells([o], n)[0])  # noqa: E731
+            assert_peaks_match(off, score, ref.offsets, ref.scores, exact)
+    with _scan(n, O.TERMS_SHAPE_ACE, pair.ace, k=32, mode=mode, max_trans_inp=20) as s:
+        s.set_receptor(pair.receptor.xyz, pair.receptor.ace_type)
+        s.set_ligand(pair.ligand.xyz, pair.ligand.ace_type)
+        res = s.scan(pair.rotations)
+    assert np.all(res.n_peaks == 20)
+    for i, rot in enumerate(pair.rotations):
+        ref = O.scan_rotation(geom, rg, rs, pair.ligand.xyz, w, rot, 20, workers=8)
+        cells, _ = O.bin_ligand(geom, rot, pair.ligand.xyz)
+        cell, t, score = res.rotation(i)
+        off = (cell[:, 0] * n + cell[:, 1]) * n + cell[:, 2]
+        exact = lambda o: O.direct_score(rg, cells, w, O.offsets_to_cells([o], n)[0])  # noqa: E731
+        assert_peaks_match(off, score, ref.offsets, ref.scores, exact)
+
+
 def test_value_limit_and_queue_bound():
     f = _fixture("scan_shape_ace_n32")
     sc = f["scores"]

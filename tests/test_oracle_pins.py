@@ -86,6 +86,44 @@ def test_grid_domain_conventions():
         assert int(g.to_logical(-lo + 1e-9)) >= n
 
 
+def test_box_grid_domain_conventions():
+    # src/PRODDL/Grid/test_grid.cpp:65-76 itself: step 20, shape (50, 51, 51)
+    # -> spatial domain [-500, 500] x [-510, 510] x [-510, 510]
+    g = O.Geometry.centred(20.0, (50, 51, 51))
+    lo, hi = g.spatial_domain()
+    assert list(lo) == [-500.0, -510.0, -510.0] and list(hi) == [500.0, 510.0, 510.0]
+    p = np.array([[-500 + 1e-9, -510 + 1e-9, 510 - 1e-9], [500 - 1e-9, 0.0, -510 - 1e-9]])
+    assert g.to_logical(p).tolist() == [[0, 0, 50], [49, 25, -1]]
+    assert g.to_spatial(0, 1) == -500.0 and g.to_spatial(0, 0) == -490.0
+
+
+def test_box_grid_fft_correlation_equals_direct_scores():
+    """On a grid whose three sizes differ (FFT sizes chosen per axis), the
+    oracle's FFT correlation equals its exact direct-space energies, and a
+    translation stands for h * unwrap(cell) per axis."""
+    from proddl2_gb300 import synth
+    pair = synth.make_pair(220, 50, 2, seed=61)
+    geom = O.Geometry.centred(1.2, (24, 30, 28))
+    tp = O.TermParams(term_set=O.TERMS_SHAPE_ACE, ace_matrix=pair.ace)
+    rg = O.receptor_terms(geom, pair.receptor.xyz, pair.receptor.ace_type, tp)
+    assert rg.shape == (18, 24, 30, 28)
+    rs = O.receptor_spectra(rg)
+    w = O.ligand_term_weights(pair.ligand.ace_type, tp)
+    for rot in pair.rotations:
+        res = O.scan_rotation(geom, rg, rs, pair.ligand.xyz, w, rot, 6, keep_corr=True)
+        assert res.in_grid
+        cells, _ = O.bin_ligand(geom, rot, pair.ligand.xyz)
+        for off, c, s in zip(res.offsets, res.cells, res.scores):
+            assert np.array_equal(O.offsets_to_cells([off], geom.dims)[0], c)
+            assert abs(O.direct_score(rg, cells, w, c) - s) <= 1e-9 * max(1.0, abs(s))
+        # a few arbitrary cells of the whole correlation grid
+        rng = np.random.default_rng(1)
+        for c in rng.integers(0, [24, 30, 28], size=(5, 3)):
+            assert abs(O.direct_score(rg, cells, w, c) - res.corr[tuple(c)]) <= 1e-9 * max(1.0, abs(res.corr[tuple(c)]))
+        t = O.translation(res.cells, geom)
+        assert np.all(t / 1.2 >= -np.array([12, 15, 14])) and np.all(t / 1.2 < np.array([12, 15, 14]))
+
+
 def test_scan_record_roundtrip():
     # src/PRODDL/IO/test_dock_io_bin.cpp:41-104 (identity rotation, 2 records)
     rot = np.eye(3)

@@ -239,8 +239,8 @@ int run_rot_scan(std::map<std::string, std::string>& a) {
     int n = (int)num(opt, "gridN", 0);
     if (n <= 0) {
         // the reference's rule: padded receptor box (docking_molstruct.hpp:
-        // 232-244), FFTW-friendly size per axis (docking_fft.hpp:541-553); the
-        // kernels are cubic, so take the largest axis and the next built size
+        // 232-244), FFTW-friendly size per axis (docking_fft.hpp:541-553),
+        // each axis sized on its own
         double lig = 0.0;
         const size_t nl = p.lig_xyz.size() / 3;
         for (size_t i = 0; i < nl; ++i)
@@ -249,21 +249,27 @@ int run_rot_scan(std::map<std::string, std::string>& a) {
                 for (int k = 0; k < 3; ++k) d2 += std::pow(p.lig_xyz[3 * i + k] - p.lig_xyz[3 * j + k], 2);
                 lig = std::max(lig, d2);
             }
-        const double pad = cfg.grid_step * 2.0 + std::sqrt(lig) / 2.0 + num(opt, "cutOffFft", 9.0);
-        double ext = 0.0;
+        const double pad = (cfg.grid_step * 2.0 + std::sqrt(lig) / 2.0) + num(opt, "cutOffFft", 9.0);
+        int32_t dims[3] = {0, 0, 0};
         for (int k = 0; k < 3; ++k) {
             double lo = INFINITY, hi = -INFINITY;
             for (size_t i = 0; i < p.rec_xyz.size() / 3; ++i) {
                 lo = std::min(lo, p.rec_xyz[3 * i + k]);
                 hi = std::max(hi, p.rec_xyz[3 * i + k]);
             }
-            ext = std::max(ext, hi - lo + 2 * pad);
+            lo -= pad;
+            hi += pad;
+            // findBestSize(Geom(h, lo).toLogical(hi))
+            const double zero_h = lo - cfg.grid_step;
+            fftdock_find_best_size((int32_t)((hi - zero_h) / cfg.grid_step) - 1, &dims[k]);
         }
-        int32_t best = 0;
-        fftdock_find_best_size((int32_t)std::ceil(ext / cfg.grid_step) + 1, &best);
-        n = best;
-        while (n <= 1024 && !fftdock_supported_grid(n)) ++n;
-        if (n > 1024) die("no built grid size covers the receptor box");
+        if (!fftdock_supported_dims(dims[0], dims[1], dims[2]))
+            die("the receptor box needs a grid of " + std::to_string(dims[0]) + " x " + std::to_string(dims[1]) +
+                " x " + std::to_string(dims[2]) + ", beyond the supported sizes");
+        cfg.grid_nx = dims[0];
+        cfg.grid_ny = dims[1];
+        cfg.grid_nz = dims[2];
+        n = dims[0];
     }
     cfg.grid_n = n;
 

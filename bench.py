@@ -63,6 +63,8 @@ def parse_args():
                    help="queue bound with --cluster (maxNTransInp; default: the reference's maxNTrans * 100)")
     p.add_argument("--cluster-radius", type=float, default=5.0, help="clusterRadiusTrans with --cluster")
     p.add_argument("--n-pairs", type=int, default=0, help="pairs of the pairs256 workload (default 256)")
+    p.add_argument("--grid-dims", default="",
+                   help="FFT sizes per axis 'nx,ny,nz' instead of the workload's cubic edge (box grids)")
     return p.parse_args()
 
 
@@ -359,10 +361,11 @@ def run_ours(args):
     pair = synth.make_pair(w["n_rec"], w["n_lig"], w["n_rot"], seed=1)
     n_rot = w["n_rot"]
     queue = (args.cluster_queue or 100 * w["peaks"]) if args.cluster else 10000
+    dims = tuple(int(v) for v in args.grid_dims.split(",")) if args.grid_dims else None
     cfg = ScanConfig(grid_n=w["grid_n"], grid_step=w["grid_step"], term_set=w["term_set"], peaks_per_rot=w["peaks"],
                      rot_batch=w["rot_batch"], ace_matrix=pair.ace, device=local, pencil_mode=args.pencil,
                      precision=args.precision, cluster_trans=args.cluster, max_trans_inp=queue,
-                     cluster_radius=args.cluster_radius)
+                     cluster_radius=args.cluster_radius, grid_dims=dims)
     scan = FFTScan(cfg)
     t0 = time.perf_counter()
     if w["term_set"].startswith("lj"):
@@ -529,6 +532,7 @@ def run_ours(args):
                          % (k_terms * n * n * (n // 2 + 1) * 8 / 1e6, batch * n * n * (n // 2 + 1) * 8 / 1e6),
                    "receptor_setup_ms": receptor_ms,
                    "pencil_stage": info["pencil_path"],
+                   "grid_dims": list(scan.grid_dims),
                    "precision": ("split-FP16 tcgen05 GEMM with FP32 accumulation (hi*hi+hi*lo+lo*hi) for the x stage, "
                                  "FP32 FFTs elsewhere" if info["pencil_path"] == "tensor" else "FP32 FFTs")
                                 + (", BF16-stored receptor spectra" if args.precision == "bf16" else "")

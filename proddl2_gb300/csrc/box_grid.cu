@@ -14,7 +14,7 @@
 // run the same line FFT in FP64.
 //
 // Layout (Hz = Nz/2 + 1, pencil p = ky Hz + kz, PP = Ny Hz rounded up to 32):
-//   spec  [K][Nx][PP]  float2  R^_t(kx, p) / V
+//   spec  [K][PP][Nx]  float2  R^_t(kx, p) / V (pencil-major: coalesced along kx)
 //   rgrid [K][V]       double  real-space receptor terms (FP64 rescoring)
 //   ent   [B][n_ent]   uint32  t << 24 | x << 16 | y << 8 | z, sorted by (t, x)
 //   offs  [B][K Nx+1]  int32   start of bin (t, x)
@@ -64,29 +64,63 @@ template <typename T2, int SIGN> __device__ __forceinline__ T2 tw_at(const T2* t
 
 // one Stockham stage of radix R over a line of n points held in src:
 // butterfly j reads src[j + r n/R], applies the twiddles W^(j mod Ns) r n/(Ns R),
-// and writes its R-point DFT to dst[(j / Ns) Ns R + j mod Ns + k Ns]
+// and writes its R-point DFT to dst[(j / Ns) Ns R + j mod Ns + k Ns].  The
+// twiddle index (j mod Ns) r n/(Ns R) stays below n; the R-th roots of unity
+// are held in registers for the whole stage, radices 2 and 4 need none.
 template <typename T2, int SIGN, int R>
 __device__ __forceinline__ void stockham_stage(const T2* src, T2* dst, const T2* tw, int n, int ns, int lane) {
-    const int nb = n / R, nr = n / R;
+    const int nb = n / R;
+    const int tstep = n / (ns * R);
+    T2 root[R];
+#pragma unroll
+    for (int m = 1; m < R; ++m) root[m] = tw_at<T2, SIGN>(tw, m * nb);
     for (int j = lane; j < nb; j += 32) {
         T2 v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) v[r] = src[j + r * nb];
-        const int jm = j % ns;
-        const int step = jm * (n / (ns * R));
+        const int jq = j / ns;
+        const int jm = j - jq * ns;
+        const int step = jm * tstep;
 #pragma unroll
-        for (int r = 1; r < R; ++r) v[r] = c_mul(v[r], tw_at<T2, SIGN>(tw, (step * r) % n));
-        const int base = (j / ns) * ns * R + jm;
+        for (int r = 1; r < R; ++r) v[r] = c_mul(v[r], tw_at<T2, SIGN>(tw, step * r));
+        T2* out = dst + jq * ns * R + jm;
+        if constexpr (R == 2) {
+            T2 o0 = v[0], o1 = v[0];
+            o0.x += v[1].x; o0.y += v[1].y;
+            o1.x -= v[1].x; o1.y -= v[1].y;
+            out[0] = o0;
+            out[ns] = o1;
+        } else if constexpr (R == 4) {
+            // W4 = e^(SIGN i pi / 2): out1 = (v0 - v2) + W4 (v1 - v3), out3 = (v0 - v2) - W4 (v1 - v3)
+            T2 a, b, c, d, e;
+            a.x = v[0].x + v[2].x; a.y = v[0].y + v[2].y;
+            b.x = v[0].x - v[2].x; b.y = v[0].y - v[2].y;
+            c.x = v[1].x + v[3].x; c.y = v[1].y + v[3].y;
+            e.x = v[1].x - v[3].x; e.y = v[1].y - v[3].y;
+            if (SIGN < 0) { d.x = e.y; d.y = -e.x; } else { d.x = -e.y; d.y = e.x; }
+            T2 o;
+            o.x = a.x + c.x; o.y = a.y + c.y; out[0] = o;
+            o.x = b.x + d.x; o.y = b.y + d.y; out[ns] = o;
+            o.x = a.x - c.x; o.y = a.y - c.y; out[2 * ns] = o;
+            o.x = b.x - d.x; o.y = b.y - d.y; out[3 * ns] = o;
+        } else {
 #pragma unroll
-        for (int k = 0; k < R; ++k) {
-            T2 acc = v[0];
+            for (int k = 0; k < R; ++k) {
+                T2 acc = v[0];
 #pragma unroll
-            for (int r = 1; r < R; ++r) {
-                const T2 p = c_mul(v[r], tw_at<T2, SIGN>(tw, ((r * k) % R) * nr));
-                acc.x += p.x;
-                acc.y += p.y;
+                for (int r = 1; r < R; ++r) {
+                    const int m = (r * k) % R;
+                    if (m == 0) {
+                        acc.x += v[r].x;
+                        acc.y += v[r].y;
+                    } else {
+                        const T2 pr = c_mul(v[r], root[m]);
+                        acc.x += pr.x;
+                        acc.y += pr.y;
+                    }
+                }
+                out[k * ns] = acc;
             }
-            dst[base + k * ns] = acc;
         }
     }
 }
@@ -144,6 +178,24 @@ __global__ void __launch_bounds__(32 * kBoxWarps) box_line_fft64_kernel(double2*
     for (int e = lane; e < n; e += 32) a[e] = line[(long)e * elem_stride];
     const double2* r = warp_fft<double2, -1>(a, b, tws, pl, lane);
     for (int e = lane; e < n; e += 32) line[(long)e * elem_stride] = r[e];
+}
+
+// half spectrum [Nx][Ny Hz] (FP64) -> the pencil stage's spectra [PP][Nx]
+// (FP32, scaled; pencils past Ny Hz are zero): a warp reads one pencil's
+// kx values as consecutive words
+__global__ void box_pack_spectrum_kernel(const double2* __restrict__ half, float2* __restrict__ spec, int nx,
+                                         int nh, int pp, double scale) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t tot = (size_t)nx * pp;
+    if (i >= tot) return;
+    const size_t p = i / nx;
+    const int kx = (int)(i - p * nx);
+    float2 o = make_float2(0.f, 0.f);
+    if (p < (size_t)nh) {
+        const double2 v = half[(size_t)kx * nh + p];
+        o = make_float2((float)(v.x * scale), (float)(v.y * scale));
+    }
+    spec[i] = o;
 }
 
 // [Nx][Ny][Nz] complex -> [Nx][Ny][Hz]
@@ -256,21 +308,29 @@ __global__ void __launch_bounds__(256) box_prep_kernel(const double* __restrict_
 //   F(x) = sum over entries of bin (t, x) of w e^{-2 pi i (ky y / Ny + kz z / Nz)}
 //   S(kx) += conj(R^_t(kx)) FFT_x(F)(kx)   over the terms
 //   g2[x][p] = IFFT_x(S)(x)
+// The warp first tabulates its pencil's phases along y and z (Ny + Nz
+// values), so an entry costs two lookups and a complex product.  The lanes
+// take a term's entries 32 at a time; entries are sorted by x, so a
+// segmented scan over the lanes sums each x bin's entries and the last lane
+// of each bin adds the sum into F(x): every lane has work whatever the bin
+// sizes, and the additions happen in one fixed order.
 // ---------------------------------------------------------------------------
 template <bool WEIGHTED>
-__global__ void __launch_bounds__(32 * kBoxWarps) box_pencil_kernel(
+__global__ void __launch_bounds__(32 * kBoxWarps, 2) box_pencil_kernel(
     const float2* __restrict__ spec, const uint32_t* __restrict__ ent, const int32_t* __restrict__ offs,
     const float* __restrict__ ent_w, const float2* __restrict__ twx_g, const float2* __restrict__ twy_g,
     const float2* __restrict__ twz_g, BoxPlan plx, float2* __restrict__ g2, int K, int n_ent, int ny, int nz, int pp) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nx = plx.n, hz = nz / 2 + 1, np = ny * hz;
+    const int wstride = ny + nz + 3 * nx;
     float2* twx = reinterpret_cast<float2*>(smem_raw);  // [nx]
     float2* twy = twx + nx;                             // [ny]
     float2* twz = twy + ny;                             // [nz]
-    float2* wbuf = twz + nz;                            // [8][3][nx]
-    uint32_t* ent_s = reinterpret_cast<uint32_t*>(wbuf + kBoxWarps * 3 * nx);  // [n_ent]: y << 16 | z
-    float* w_s = reinterpret_cast<float*>(ent_s + n_ent);                      // WEIGHTED: [n_ent]
-    int32_t* offs_s = reinterpret_cast<int32_t*>(w_s + (WEIGHTED ? n_ent : 0));  // [K*Nx + 1]
+    float2* wbuf = twz + nz;                            // [8][ny + nz + 3 nx]
+    float2* otile = wbuf + kBoxWarps * wstride;         // [nx][8]
+    uint32_t* ent_s = reinterpret_cast<uint32_t*>(otile + kBoxWarps * nx);  // [n_ent]
+    float* w_s = reinterpret_cast<float*>(ent_s + n_ent);                     // WEIGHTED: [n_ent]
+    int32_t* tstart = reinterpret_cast<int32_t*>(w_s + (WEIGHTED ? n_ent : 0));  // [K + 1]
 
     const int q = blockIdx.x;
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
@@ -279,52 +339,86 @@ __global__ void __launch_bounds__(32 * kBoxWarps) box_pencil_kernel(
     for (int i = tid; i < nz; i += blockDim.x) twz[i] = twz_g[i];
     const uint32_t* eq = ent + (size_t)q * n_ent;
     for (int i = tid; i < n_ent; i += blockDim.x) {
-        const uint32_t u = eq[i];
-        ent_s[i] = (((u >> 8) & 255u) << 16) | (u & 255u);
+        ent_s[i] = eq[i];
         if (WEIGHTED) w_s[i] = ent_w[(size_t)q * n_ent + i];
     }
+    // entries of term t: [tstart[t], tstart[t + 1]) (sorted by (t, x))
     const int32_t* oq = offs + (size_t)q * (K * nx + 1);
-    for (int i = tid; i <= K * nx; i += blockDim.x) offs_s[i] = oq[i];
+    for (int t = tid; t <= K; t += blockDim.x) tstart[t] = t < K ? oq[t * nx] : n_ent;
     __syncthreads();
 
     const int p = blockIdx.y * kBoxWarps + w;
-    if (p >= np) return;
-    const int ky = p / hz, kz = p - (p / hz) * hz;
-    float2* a = wbuf + (size_t)w * 3 * nx;
-    float2* b = a + nx;
-    float2* acc = b + nx;
-    for (int x = lane; x < nx; x += 32) acc[x] = make_float2(0.f, 0.f);
-    for (int t = 0; t < K; ++t) {
-        __syncwarp();
-        for (int x = lane; x < nx; x += 32) {
-            const int j0 = offs_s[t * nx + x], j1 = offs_s[t * nx + x + 1];
-            float2 f = make_float2(0.f, 0.f);
-            for (int j = j0; j < j1; ++j) {
-                const uint32_t e = ent_s[j];
-                const int y = (int)(e >> 16), z = (int)(e & 0xffffu);
-                const float2 ph = c_mul(twy[(ky * y) % ny], twz[(kz * z) % nz]);
-                const float wj = WEIGHTED ? w_s[j] : 1.f;
-                f.x = fmaf(wj, ph.x, f.x);
-                f.y = fmaf(wj, ph.y, f.y);
+    if (p < np) {
+        const int ky = p / hz, kz = p - (p / hz) * hz;
+        float2* phy = wbuf + (size_t)w * wstride;  // [ny] e^{-2 pi i ky y / Ny}
+        float2* phz = phy + ny;                     // [nz] e^{-2 pi i kz z / Nz}
+        float2* a = phz + nz;
+        float2* b = a + nx;
+        float2* acc = b + nx;
+        for (int y = lane; y < ny; y += 32) phy[y] = twy[(ky * y) % ny];
+        for (int z = lane; z < nz; z += 32) phz[z] = twz[(kz * z) % nz];
+        for (int x = lane; x < nx; x += 32) acc[x] = make_float2(0.f, 0.f);
+        for (int t = 0; t < K; ++t) {
+            for (int x = lane; x < nx; x += 32) a[x] = make_float2(0.f, 0.f);
+            __syncwarp();
+            const int j1 = tstart[t + 1];
+            for (int base = tstart[t]; base < j1; base += 32) {
+                const int j = base + lane;
+                const bool act = j < j1;
+                const uint32_t e = act ? ent_s[j] : 0u;
+                const int xk = act ? (int)((e >> 16) & 255u) : -1;
+                float2 v = make_float2(0.f, 0.f);
+                if (act) {
+                    v = c_mul(phy[(e >> 8) & 255u], phz[e & 255u]);
+                    if (WEIGHTED) {
+                        const float wj = w_s[j];
+                        v.x *= wj;
+                        v.y *= wj;
+                    }
+                }
+                // segmented inclusive scan over lanes with equal x (contiguous: sorted)
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const float ux = __shfl_up_sync(0xffffffffu, v.x, o);
+                    const float uy = __shfl_up_sync(0xffffffffu, v.y, o);
+                    const int uk = __shfl_up_sync(0xffffffffu, xk, o);
+                    if (lane >= o && uk == xk) {
+                        v.x += ux;
+                        v.y += uy;
+                    }
+                }
+                const int nk = __shfl_down_sync(0xffffffffu, xk, 1);
+                if (act && (lane == 31 || nk != xk)) {
+                    float2 f = a[xk];
+                    f.x += v.x;
+                    f.y += v.y;
+                    a[xk] = f;
+                }
+                __syncwarp();
             }
-            a[x] = f;
+            const float2* fx = warp_fft<float2, -1>(a, b, twx, plx, lane);
+            const float2* sp = spec + ((size_t)t * pp + p) * nx;
+            for (int kx = lane; kx < nx; kx += 32) {
+                const float2 f = fx[kx];
+                const float2 rv = __ldg(sp + kx);
+                float2 s = acc[kx];
+                s.x += f.x * rv.x + f.y * rv.y;
+                s.y += f.y * rv.x - f.x * rv.y;
+                acc[kx] = s;
+            }
+            __syncwarp();
         }
-        const float2* fx = warp_fft<float2, -1>(a, b, twx, plx, lane);
-        const float2* sp = spec + (size_t)t * nx * pp + p;
-        for (int kx = lane; kx < nx; kx += 32) {
-            const float2 f = fx[kx];
-            const float2 rv = __ldg(sp + (size_t)kx * pp);
-            float2 s = acc[kx];
-            s.x += f.x * rv.x + f.y * rv.y;
-            s.y += f.y * rv.x - f.x * rv.y;
-            acc[kx] = s;
-        }
+        for (int x = lane; x < nx; x += 32) a[x] = acc[x];
+        const float2* out = warp_fft<float2, +1>(a, b, twx, plx, lane);
+        for (int x = lane; x < nx; x += 32) otile[x * kBoxWarps + w] = out[x];
     }
-    __syncwarp();
-    for (int x = lane; x < nx; x += 32) a[x] = acc[x];
-    const float2* out = warp_fft<float2, +1>(a, b, twx, plx, lane);
-    float2* dst = g2 + (size_t)q * nx * pp + p;
-    for (int x = lane; x < nx; x += 32) dst[(size_t)x * pp] = out[x];
+    __syncthreads();
+    // the CTA's 8 pencils of every x plane: 64 contiguous bytes per plane
+    float2* dst = g2 + (size_t)q * nx * pp + (size_t)blockIdx.y * kBoxWarps;
+    for (int i = tid; i < nx * kBoxWarps; i += blockDim.x) {
+        const int x = i / kBoxWarps, ww = i - x * kBoxWarps;
+        if (blockIdx.y * kBoxWarps + ww < np) dst[(size_t)x * pp + ww] = otile[i];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -335,7 +429,7 @@ __global__ void __launch_bounds__(32 * kBoxWarps) box_pencil_kernel(
 // warp 0 merges them into the plane's pool.
 // ---------------------------------------------------------------------------
 template <bool DBG>
-__global__ void __launch_bounds__(32 * kBoxWarps) box_plane_kernel(const float2* __restrict__ g2,
+__global__ void __launch_bounds__(32 * kBoxWarps, 2) box_plane_kernel(const float2* __restrict__ g2,
                                                                   const float2* __restrict__ twy_g,
                                                                   const float2* __restrict__ twz_g, BoxPlan ply,
                                                                   BoxPlan plz, int nx, int pp,
@@ -518,8 +612,9 @@ __global__ void __launch_bounds__(256) box_finalize_kernel(
 }
 
 size_t pencil_smem_bytes(int nx, int ny, int nz, int K, int n_ent, bool weighted) {
-    return (size_t)(nx + ny + nz) * sizeof(float2) + (size_t)kBoxWarps * 3 * nx * sizeof(float2) +
-           (size_t)n_ent * sizeof(uint32_t) * (weighted ? 2 : 1) + ((size_t)K * nx + 1) * sizeof(int32_t);
+    return (size_t)(nx + ny + nz) * sizeof(float2) + (size_t)kBoxWarps * (ny + nz + 3 * nx) * sizeof(float2) +
+           (size_t)kBoxWarps * nx * sizeof(float2) + (size_t)n_ent * sizeof(uint32_t) * (weighted ? 2 : 1) +
+           ((size_t)K + 1) * sizeof(int32_t);
 }
 size_t plane_smem_bytes(int ny, int nz) {
     const int hz = nz / 2 + 1, lmax = std::max(ny, nz);
@@ -662,8 +757,8 @@ cudaError_t box_receptor_fft(const double* rgrid_t, double2* cbuf, double2* hbuf
     // x: lines p = (ky, kz)
     if ((e = lines(hbuf, twx, px, (long)ny * hz, (long)ny * hz, (long)ny * hz, 1, 0)) != cudaSuccess) return e;
     const size_t tot = (size_t)nx * PP;
-    pack_spectrum_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(hbuf, static_cast<float2*>(spec_t), nx,
-                                                                       ny * hz, PP, 1.0 / (double)V);
+    box_pack_spectrum_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(hbuf, static_cast<float2*>(spec_t), nx,
+                                                                           ny * hz, PP, 1.0 / (double)V);
     return cudaGetLastError();
 }
 

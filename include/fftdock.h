@@ -343,8 +343,19 @@ int fftdock_write_scan_records(const char* path, int32_t n_rot, const double* ro
  * ------------------------------------------------------------------------ */
 enum {
     FFTDOCK_BOX_AXES = 0,
-    FFTDOCK_BOX_GIVEN = 1
+    FFTDOCK_BOX_GIVEN = 1,
+    FFTDOCK_BOX_MIN_VOLUME = 2   /* the minimum-volume box computed by fftdock_min_volume_box (grid 5) */
 };
+
+/* Minimum-volume bounding box of n points (the receptor), as the reference's
+ * Geom::Bounding::Box computes it through gdiam's grid search
+ * (include/PRODDL/Geom/bounding.hpp:137-172): Barequet and Har-Peled's
+ * approximation -- a box on the diameter and the projected diameter, boxes
+ * from the minimum-area rectangles of the points projected across each box
+ * direction, and a search over the primitive integer combinations of the box
+ * directions up to `grid` (the reference uses 5).  dirs: 3 direction rows;
+ * corners: vertex (0,0,0) then vertex (1,1,1), in the points' frame. */
+int fftdock_min_volume_box(int32_t n, const double* xyz, int32_t grid, double* dirs, double* corners);
 
 typedef struct fftdock_frame_setup_in {
     int32_t n_rec;

@@ -75,6 +75,7 @@ class Config(C.Structure):
 
 FFTDOCK_BOX_AXES = 0
 FFTDOCK_BOX_GIVEN = 1
+FFTDOCK_BOX_MIN_VOLUME = 2
 
 
 class FrameIn(C.Structure):
@@ -195,6 +196,7 @@ SIGNATURES = {
     "fftdock_write_rigid": (C.c_int, [C.c_char_p, _P, C.c_int32, _P, _P, C.c_int32]),
     "fftdock_write_scan_records": (C.c_int, [C.c_char_p, C.c_int32, _P, C.c_int32, _P, _P, C.c_int32]),
     "fftdock_frame_setup": (C.c_int, [C.POINTER(FrameIn), _P, _P, C.POINTER(Frame)]),
+    "fftdock_min_volume_box": (C.c_int, [C.c_int32, _P, C.c_int32, _P, _P]),
     "fftdock_scan_pairs": (C.c_int, [C.POINTER(Config), C.c_int32, C.POINTER(PairDesc), C.c_int32,
                                      C.POINTER(PairsReport)]),
     "fftdock_pairs_last_error": (C.c_char_p, []),

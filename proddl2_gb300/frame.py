@@ -28,8 +28,9 @@ class PairFrame:
 
 def frame_setup(rec_xyz, lig_xyz, grid_step=1.2, cut_off_fft=9.0, starting_spin=23.3734432, lig_mass=None,
                 box=None, lig_diam=None):
-    """``box``: None (axis-aligned receptor box) or (directions 3x3 rows,
-    corner (0,0,0), corner (1,1,1)) in the original frame."""
+    """``box``: None (axis-aligned receptor box), "min_volume" (the
+    minimum-volume box, computed as the reference's Box does) or (directions
+    3x3 rows, corner (0,0,0), corner (1,1,1)) in the original frame."""
     rec = np.ascontiguousarray(rec_xyz, dtype=np.float64).reshape(-1, 3)
     lig = np.ascontiguousarray(lig_xyz, dtype=np.float64).reshape(-1, 3)
     mass = None if lig_mass is None else np.ascontiguousarray(lig_mass, dtype=np.float64)
@@ -41,6 +42,10 @@ def frame_setup(rec_xyz, lig_xyz, grid_step=1.2, cut_off_fft=9.0, starting_spin=
     keep = []
     if box is None:
         a.box_mode = _lib.FFTDOCK_BOX_AXES
+    elif isinstance(box, str):
+        if box != "min_volume":
+            raise ValueError("box: None, 'min_volume' or (dirs, corner0, corner1)")
+        a.box_mode = _lib.FFTDOCK_BOX_MIN_VOLUME
     else:
         dirs = np.ascontiguousarray(box[0], dtype=np.float64).reshape(9)
         corners = np.ascontiguousarray(np.concatenate([np.ravel(box[1]), np.ravel(box[2])]), dtype=np.float64)
@@ -61,3 +66,16 @@ def frame_setup(rec_xyz, lig_xyz, grid_step=1.2, cut_off_fft=9.0, starting_spin=
     fr = lambda t: (np.array(t[:9]).reshape(3, 3), np.array(t[9:12]))  # noqa: E731
     return PairFrame(rec_out, lig_out, fr(f.rec_frame), fr(f.lig_frame), float(f.lig_size),
                      np.array(f.min_box).reshape(2, 3), tuple(int(v) for v in f.fft_size), int(f.grid_n))
+
+
+def min_volume_box(xyz, grid=5):
+    """Minimum-volume bounding box of the points (``fftdock_min_volume_box``):
+    (direction rows 3x3, corner (0,0,0), corner (1,1,1))."""
+    pts = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    dirs = np.zeros(9)
+    corners = np.zeros(6)
+    rc = _lib.lib().fftdock_min_volume_box(len(pts), C.c_void_p(pts.ctypes.data), int(grid),
+                                           C.c_void_p(dirs.ctypes.data), C.c_void_p(corners.ctypes.data))
+    if rc:
+        raise FFTDockError(rc, "minimum-volume box: bad input")
+    return dirs.reshape(3, 3), corners[:3].copy(), corners[3:].copy()

@@ -88,6 +88,49 @@ def test_diameter_matches_reference_gdiam(built_lib):
         assert {tuple(out[:3]), tuple(out[3:])} == {tuple(p), tuple(q)}
 
 
+@pytest.mark.parametrize("seed,n,stretch", [(7, 900, (1.0, 1.0, 1.0)), (9, 1500, (1.5, 1.0, 0.8)),
+                                            (10, 2000, (2.0, 1.2, 0.7))])
+def test_min_volume_box_matches_reference_gdiam(built_lib, seed, n, stretch):
+    """The library's minimum-volume box against the reference's own gdiam
+    (grid 5, every point, as Geom::Bounding::Box calls it): the same volume
+    to 1e-4 (never larger by more), the same three axes up to their order and
+    sign, every point inside."""
+    lib = _gdiam()
+    from proddl2_gb300 import synth
+    from proddl2_gb300.frame import min_volume_box
+    x = synth.molecule(n, seed).xyz * np.array(stretch)
+    R = synth.quaternion_rotations(1, seed + 50)[0]
+    x = np.ascontiguousarray(x @ R.T)
+    D, c0, c1 = min_volume_box(x)
+    corners, dirs = np.zeros(6), np.zeros(9)
+    lib.ref_mvbb(x.ctypes.data, len(x), 5, len(x), corners.ctypes.data, dirs.ctypes.data)
+    Dr = dirs.reshape(3, 3)
+    vol = lambda d, a, b: abs(np.prod(d @ (b - a)))  # noqa: E731
+    v, vr = vol(D, c0, c1), vol(Dr, corners[:3], corners[3:])
+    assert abs(v / vr - 1.0) <= 1e-4 and v <= vr * (1.0 + 1e-9), (v, vr)
+    assert np.allclose(D @ D.T, np.eye(3), atol=1e-12)
+    match = np.abs(D @ Dr.T)
+    assert np.all(np.sort(match.max(axis=1)) >= 0.999), match
+    proj = x @ D.T
+    lo, hi = D @ c0, D @ c1
+    assert np.all(proj >= lo - 1e-9) and np.all(proj <= hi + 1e-9)
+    # no larger than the axis-aligned box
+    assert v <= np.prod(x.max(0) - x.min(0)) * (1.0 + 1e-12)
+
+
+def test_frame_on_the_library_minimum_volume_box(built_lib):
+    """box='min_volume' is the frame built on the library's own minimum-volume
+    box (the same as passing that box in)."""
+    from proddl2_gb300.frame import frame_setup, min_volume_box
+    rec, lig = _pair(8, n_rec=600)
+    a = frame_setup(rec, lig, 1.2, 9.0, box="min_volume")
+    b = frame_setup(rec, lig, 1.2, 9.0, box=min_volume_box(rec))
+    assert np.array_equal(a.rec_xyz, b.rec_xyz) and np.array_equal(a.min_box, b.min_box)
+    assert np.array_equal(a.rec_frame[0], b.rec_frame[0]) and list(a.fft_size) == list(b.fft_size)
+    vol = lambda f: np.prod(f.min_box[1] - f.min_box[0])  # noqa: E731
+    assert vol(a) <= vol(frame_setup(rec, lig, 1.2, 9.0)) * 1.0001
+
+
 def test_frame_on_the_reference_minimum_volume_box(built_lib):
     """Box directions and corners from the reference's own gdiam MVBB (grid
     5, every point sampled, as Geom::Bounding::Box does) give the same frame

@@ -502,6 +502,12 @@ int fftdock_proposal_predict_device(fftdock_proposal* p, int32_t lig, int32_t n,
  * histogram (1.5 A shells about the bounding-box centre, the last shell
  * open-ended) divided by the atom count.  Host only. */
 int fftdock_receptor_descriptor(int32_t n, const double* xyz, const int32_t* element, float* out);
+/* Oriented alternative (no counterpart in the reference): the receptor's
+ * occupancy in the scan frame, 4 x 4 x 4 cells of the cube about its box
+ * centre (half-width = the box's largest half-extent), all atoms (values
+ * 0..63) and the outer atoms (64..127), as fractions of the atom count; with
+ * it the network sees both molecules in one frame. */
+int fftdock_receptor_descriptor_oriented(int32_t n, const double* xyz, float* out);
 
 #ifdef __cplusplus
 }

@@ -93,6 +93,26 @@ def descriptor(xyz, element):
     return out / float(len(xyz))
 
 
+def descriptor_oriented(xyz):
+    """Scan-frame occupancy, 4^3 cells of all and of outer atoms
+    (fftdock_receptor_descriptor_oriented)."""
+    xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros(DESC)
+    if len(xyz) == 0:
+        return out
+    lo, hi = xyz.min(axis=0), xyz.max(axis=0)
+    c = 0.5 * (lo + hi)
+    L = float((0.5 * (hi - lo)).max())
+    L = L if L > 0 else 1.0
+    t = xyz - c
+    r = np.sqrt((t[:, 0] * t[:, 0] + t[:, 1] * t[:, 1]) + t[:, 2] * t[:, 2])
+    k = np.clip(np.floor((xyz - (c - L)) / (0.5 * L)).astype(np.int64), 0, 3)
+    cell = (k[:, 0] * 4 + k[:, 1]) * 4 + k[:, 2]
+    np.add.at(out, cell, 1.0)
+    np.add.at(out, 64 + cell[r > 0.7 * r.max()], 1.0)
+    return out / float(len(xyz))
+
+
 def _taps(x, dout):
     """Patches of a stride-2, pad-1, 3^3 convolution: k -> [C, dout^3]."""
     c, d = x.shape[0], x.shape[1]

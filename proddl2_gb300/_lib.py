@@ -215,6 +215,7 @@ SIGNATURES = {
     "fftdock_proposal_predict": (C.c_int, [_P, C.c_int32, C.c_int32, _P, _P]),
     "fftdock_proposal_predict_device": (C.c_int, [_P, C.c_int32, C.c_int32, _P, _P, _P]),
     "fftdock_receptor_descriptor": (C.c_int, [C.c_int32, _P, _P, _P]),
+    "fftdock_receptor_descriptor_oriented": (C.c_int, [C.c_int32, _P, _P]),
 }
 
 _lib = None

@@ -912,4 +912,49 @@ int fftdock_receptor_descriptor(int32_t n, const double* xyz, const int32_t* ele
     return FFTDOCK_OK;
 }
 
+// occupancy of the receptor in the scan frame: the cube of half-width L (the
+// box's largest half-extent) about the box centre in 4 x 4 x 4 cells; values
+// 0..63 the fraction of all atoms per cell, 64..127 the fraction of the outer
+// atoms (distance from the centre above 0.7 of the largest) per cell
+int fftdock_receptor_descriptor_oriented(int32_t n, const double* xyz, float* out) {
+    if (n < 0 || (n > 0 && !xyz) || !out) return FFTDOCK_EINVAL;
+    for (int i = 0; i < DESC; ++i) out[i] = 0.f;
+    if (n == 0) return FFTDOCK_OK;
+    double lo[3], hi[3], c[3];
+    for (int d = 0; d < 3; ++d) lo[d] = hi[d] = xyz[d];
+    for (int i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d) {
+            const double v = xyz[3 * i + d];
+            if (!std::isfinite(v)) return FFTDOCK_EINVAL;
+            lo[d] = std::min(lo[d], v);
+            hi[d] = std::max(hi[d], v);
+        }
+    double L = 0.0, rmax = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        c[d] = 0.5 * (lo[d] + hi[d]);
+        L = std::max(L, 0.5 * (hi[d] - lo[d]));
+    }
+    std::vector<double> r(n);
+    for (int i = 0; i < n; ++i) {
+        double r2 = 0.0;
+        for (int d = 0; d < 3; ++d) r2 += (xyz[3 * i + d] - c[d]) * (xyz[3 * i + d] - c[d]);
+        r[i] = std::sqrt(r2);
+        rmax = std::max(rmax, r[i]);
+    }
+    if (!(L > 0.0)) L = 1.0;
+    std::vector<double> h(DESC, 0.0);
+    for (int i = 0; i < n; ++i) {
+        int cell = 0;
+        for (int d = 0; d < 3; ++d) {
+            int k = (int)std::floor((xyz[3 * i + d] - (c[d] - L)) / (0.5 * L));
+            k = std::min(std::max(k, 0), 3);
+            cell = cell * 4 + k;
+        }
+        h[cell] += 1.0;
+        if (r[i] > 0.7 * rmax) h[64 + cell] += 1.0;
+    }
+    for (int i = 0; i < DESC; ++i) out[i] = (float)(h[i] / (double)n);
+    return FFTDOCK_OK;
+}
+
 }  // extern "C"

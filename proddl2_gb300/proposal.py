@@ -33,6 +33,17 @@ def receptor_descriptor(xyz, element):
     return out
 
 
+def receptor_descriptor_oriented(xyz):
+    """Receptor occupancy in the scan frame (128 floats: 4^3 cells, all and
+    outer atoms), so that the network sees both molecules in one frame."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros(DESC, dtype=np.float32)
+    rc = _lib.lib().fftdock_receptor_descriptor_oriented(len(xyz), _ptr(xyz), _ptr(out))
+    if rc:
+        raise FFTDockError(rc, "oriented receptor descriptor: non-finite coordinate")
+    return out
+
+
 class Proposal:
     """One network on one GPU."""
 

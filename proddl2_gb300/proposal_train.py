@@ -22,7 +22,8 @@ import time
 import numpy as np
 
 from . import synth
-from .proposal import Proposal, best_scores, keep_best, recall, standardize, top_poses
+from .proposal import (Proposal, best_scores, keep_best, recall, receptor_descriptor,
+                       receptor_descriptor_oriented, standardize, top_poses)
 from .scan import FFTScan, ScanConfig
 
 
@@ -65,11 +66,13 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--out", default="")
     ap.add_argument("--load", default="", help="skip training: load weights saved by --out")
+    ap.add_argument("--descriptor", choices=("radial", "oriented"), default="radial",
+                    help="receptor input: radial element histograms or scan-frame occupancy")
     args = ap.parse_args(argv)
 
     rotations = synth.quaternion_rotations(args.n_rot, seed=args.seed * 31 + 7)
     report = {"pairs": args.pairs, "heldout": args.heldout, "n_rot": args.n_rot, "grid": args.grid,
-              "keep": args.keep, "top": args.top}
+              "keep": args.keep, "top": args.top, "descriptor": args.descriptor}
     net = Proposal(seed=args.seed)
     with FFTScan(scan_config(args.grid, 4)) as scan:
         if args.load:
@@ -81,7 +84,7 @@ def main(argv=None):
                 pair = make_pair(i, args.seed, rotations)
                 res = exhaustive(scan, pair, rotations)
                 n_rot_scanned += len(rotations)
-                pid = net.add_pair(pair.ligand.xyz, pair.receptor.xyz, pair.receptor.element)
+                pid = net.add_pair(pair.ligand.xyz, desc=describe(pair, args.descriptor))
                 net.add_samples(pid, rotations, standardize(best_scores(res)))
             report["label_scan_s"] = time.perf_counter() - t0
             t0 = time.perf_counter()
@@ -102,6 +105,9 @@ def main(argv=None):
         rng = np.random.Generator(np.random.PCG64(args.seed + 99))
         rec_l, rec_r, t_ex, t_pr, t_pred = [], [], 0.0, 0.0, 0.0
         rho = []
+        fracs = (0.2, 0.33, 0.5)
+        sweep = {k: {f: [] for f in fracs} for k in ("learned", "random", "neighbour")}
+        nearest = nearest_rotation(rotations)
         for j in range(args.heldout):
             pair = make_pair(100000 + j, args.seed, rotations)
             scan.set_receptor(pair.receptor.xyz)
@@ -111,7 +117,7 @@ def main(argv=None):
             full = scan.scan(rotations, raise_out_of_grid=False)
             t_ex += time.perf_counter() - t0
             ref_top = top_poses(full, np.arange(len(rotations)), args.top)
-            pid = net.add_pair(pair.ligand.xyz, pair.receptor.xyz, pair.receptor.element)
+            pid = net.add_pair(pair.ligand.xyz, desc=describe(pair, args.descriptor))
             t0 = time.perf_counter()
             pred = net.predict(pid, rotations)
             keep = keep_best(pred, args.keep)
@@ -126,6 +132,16 @@ def main(argv=None):
             best = best_scores(full)
             fin = np.isfinite(best)
             rho.append(_spearman(pred[fin], best[fin]))
+            # the same recall at other kept fractions, read off the exhaustive
+            # scan (a rotation's peaks do not depend on the others scanned);
+            # "neighbour" ranks each rotation by the true best score of its
+            # nearest other rotation: a predictor that knows the score field
+            # exactly at the set's spacing
+            for f in fracs:
+                for kind, score in (("learned", pred), ("random", rng.random(len(rotations))),
+                                    ("neighbour", best[nearest])):
+                    idx = keep_best(score, f)
+                    sweep[kind][f].append(recall(ref_top, top_poses(_subset(full, idx), idx, args.top)))
         report.update({
             "recall_learned_mean": float(np.mean(rec_l)), "recall_learned_min": float(np.min(rec_l)),
             "recall_random_mean": float(np.mean(rec_r)),
@@ -134,10 +150,30 @@ def main(argv=None):
             "pruned_rot_per_s_equiv": args.heldout * len(rotations) / t_pr,
             "speedup": t_ex / t_pr,
             "predict_ms_per_pair": 1000.0 * t_pred / args.heldout,
+            "recall_by_keep": {kind: {str(f): float(np.mean(v)) for f, v in d.items()} for kind, d in sweep.items()},
         })
     net.close()
     print(json.dumps(report))
     return report
+
+
+def nearest_rotation(rotations, chunk=1024):
+    """Index of each rotation's nearest other rotation (largest trace of
+    R_i^T R_j, i.e. smallest rotation angle between them)."""
+    r = np.asarray(rotations, dtype=np.float64).reshape(-1, 9)
+    out = np.empty(len(r), dtype=np.int64)
+    for a in range(0, len(r), chunk):
+        t = r[a:a + chunk] @ r.T
+        t[np.arange(len(t)), np.arange(a, a + len(t))] = -np.inf
+        out[a:a + len(t)] = np.argmax(t, axis=1)
+    return out
+
+
+def describe(pair, kind):
+    """The receptor input of the network for one pair."""
+    if kind == "oriented":
+        return receptor_descriptor_oriented(pair.receptor.xyz)
+    return receptor_descriptor(pair.receptor.xyz, pair.receptor.element)
 
 
 def _subset(result, idx):

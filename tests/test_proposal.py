@@ -98,6 +98,20 @@ def test_descriptor_matches_oracle(built_lib):
     assert abs(d.sum() - 1.0) < 1e-5
 
 
+def test_oriented_descriptor_matches_oracle(built_lib):
+    from proddl2_gb300 import synth
+    from proddl2_gb300.proposal import receptor_descriptor_oriented
+    rec = synth.molecule(2500, 78)
+    d = receptor_descriptor_oriented(rec.xyz)
+    ref = PO.descriptor_oriented(rec.xyz)
+    assert np.allclose(d, ref, rtol=0, atol=1e-7)
+    assert abs(d[:64].sum() - 1.0) < 1e-5 and 0 < d[64:].sum() < 1
+    # the frame matters: a rotated receptor gives a different input
+    R = np.array([[0.0, -1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+    assert not np.allclose(receptor_descriptor_oriented(rec.xyz @ R.T), d)
+    assert np.all(receptor_descriptor_oriented(np.zeros((0, 3))) == 0)
+
+
 def test_pruning_helpers():
     from proddl2_gb300.proposal import keep_best, recall, standardize
     z = standardize(np.array([-5.0, -1.0, np.inf, -3.0]))

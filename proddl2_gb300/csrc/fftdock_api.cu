@@ -7,6 +7,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <mutex>
 #include <vector>
 
 #include "fft_core.cuh"
@@ -95,6 +96,8 @@ struct fftdock_ctx {
     bool use_tc = false;
     float2* circ = nullptr;
     int8_t* cscale = nullptr;
+    float2* tc_slots = nullptr;  // running sums of the tensor stage (tc_slot_count slots of 128 x 128)
+    int tc_n_slots = 0;
     int* err_dev = nullptr;
     int x0 = 0, W = 0;
     bool tc_ready = false;       // the ligand fits the tensor stage (window, terms, unweighted)
@@ -216,6 +219,8 @@ BatchArgs batch_args(fftdock_ctx* ctx) {
     a.tpad = ctx->tpad;
     a.n_tc_terms = ctx->n_tc_terms;
     a.tc_group = ctx->cfg.tc_terms_per_sum;
+    a.tc_slots = ctx->tc_slots;
+    a.tc_n_slots = ctx->tc_n_slots;
     a.n_pad = ctx->n_pad;
     a.err = ctx->err_dev;
     a.wide = ctx->wide;
@@ -349,6 +354,38 @@ __global__ void fill_u32_kernel(uint32_t* p, uint32_t v, size_t n) {
 cudaError_t fill_padding(uint32_t* ent_t, int W, size_t n, cudaStream_t s) {
     fill_u32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(ent_t, (uint32_t)W << 24, n);
     return cudaGetLastError();
+}
+
+namespace {
+__global__ void nsmid_kernel(int* out) {
+    uint32_t v;
+    asm volatile("mov.u32 %0, %%nsmid;" : "=r"(v));
+    *out = (int)v;
+}
+}  // namespace
+
+cudaError_t tc_slot_count(int* n_slots) {
+    static std::mutex mu;
+    static std::vector<int> cache;  // per device ordinal
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    if ((int)cache.size() <= dev) cache.resize(dev + 1, 0);
+    if (cache[dev] == 0) {
+        int* d = nullptr;
+        if ((e = cudaMalloc(&d, sizeof(int))) != cudaSuccess) return e;
+        nsmid_kernel<<<1, 1>>>(d);
+        int h = 0;
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost);
+        cudaFree(d);
+        if (e != cudaSuccess) return e;
+        if (h < 1) return cudaErrorUnknown;
+        cache[dev] = h;
+    }
+    *n_slots = 2 * cache[dev];
+    return cudaSuccess;
 }
 
 TcTables tc_tables(const double* xyz, const int32_t* term, int n, int K, int N, double h, double zero_h) {
@@ -526,6 +563,7 @@ void fftdock_destroy(fftdock_ctx* ctx) {
     dfree(ctx->status_dev);
     dfree(ctx->circ);
     dfree(ctx->cscale);
+    dfree(ctx->tc_slots);
     dfree(ctx->ent_t);
     dfree(ctx->tinfo);
     dfree(ctx->tpad);
@@ -720,6 +758,8 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
     if (ctx->use_tc) {
         CK(dalloc(&ctx->circ, (size_t)ctx->K * N * ctx->H * N));
         CK(dalloc(&ctx->cscale, (size_t)N * ctx->H));
+        CK(fftdock::tc_slot_count(&ctx->tc_n_slots));
+        CK(dalloc(&ctx->tc_slots, (size_t)ctx->tc_n_slots * fftdock::kTcRot * 128));
     }
     // more peaks per rotation than the per-plane pools hold: the exact-queue
     // path, without clustering, over the first peaks_per_rot + 16 cells of

@@ -209,6 +209,8 @@ struct BatchArgs {
     const int32_t* tpad;        // [K] padded start - start of each term's entries
     int n_tc_terms;
     int tc_group;               // terms per tensor-memory sum (<= 0: FFTDOCK_TC_TERMS_PER_SUM_DEFAULT)
+    float2* tc_slots;           // [tc_n_slots][128][128] running sums of the tensor stage's CTAs
+    int tc_n_slots;             // 2 per SM id (tc_slot_count)
     int n_pad;                  // entries per rotation with every term padded to a multiple of 8
     int* err;                   // device word: nonzero after a pipeline timeout
     WideArgs wide;              // queue + clustering path (wide.corr != nullptr)
@@ -234,6 +236,9 @@ TcTables tc_tables(const double* xyz, const int32_t* term, int n, int K, int N, 
 // the padding rows of the transposed entries: x' = W (the tensor stage's
 // dummy staging row), y = z = 0
 cudaError_t fill_padding(uint32_t* ent_t, int W, size_t n, cudaStream_t s);
+// slots of the tensor stage's running sums on the current device: two per SM
+// id (%nsmid, which bounds %smid), one per tensor-memory half
+cudaError_t tc_slot_count(int* n_slots);
 // AUTO selection of the tensor form: grid edge <= 128 (has_tc), FP32
 // spectra, an unweighted term set with at least kTcMinTerms terms (at 64^3
 // with the single shape term the FFT form measured faster)

@@ -162,7 +162,12 @@ struct Run {
     std::vector<std::vector<Work>> work;  // [queue][slot]
     Staged st;
     std::string err;
+    // running sums of the tensor stage: shared by every queue (a slot is
+    // owned by the CTA holding that SM's tensor-memory half)
+    float2* tc_slots = nullptr;
+    int tc_n_slots = 0;
     ~Run() {
+        dfree(tc_slots);
         for (auto& q : work)
             for (auto& w : q) w.release();
         for (auto& kv : sizes) {
@@ -303,6 +308,8 @@ cudaError_t enqueue_pair(Run& r, const fftdock_pair& p, int i, Work& w, const Si
         a.use_tc = 1;
         a.circ = w.circ;
         a.cscale = w.cscale;
+        a.tc_slots = r.tc_slots;
+        a.tc_n_slots = r.tc_n_slots;
         a.x0 = tt.x0;
         a.W = tt.W;
         a.ent_t = w.ent_t;
@@ -685,6 +692,10 @@ int fftdock_scan_pairs(const fftdock_config* cfg, int32_t n_pairs, const fftdock
         return fail(FFTDOCK_EUNSUPPORTED, std::string("libfftdock is built for sm_103a only; device is ") + prop.name);
 
     const auto t_setup = std::chrono::steady_clock::now();
+    if (r.tc) {
+        PCK(fftdock::tc_slot_count(&r.tc_n_slots));
+        PCK(dalloc(&r.tc_slots, (size_t)r.tc_n_slots * fftdock::kTcRot * 128));
+    }
     int rc = setup_sizes(r, n_pairs, pairs);
     if (!rc) rc = stage(r, n_pairs, pairs);
     if (rc) return rc;

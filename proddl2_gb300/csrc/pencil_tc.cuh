@@ -15,9 +15,13 @@
 // per-pencil power-of-two scales keep both parts in the normal range.  The
 // tensor core's FP32 accumulation does not round to nearest, and its error
 // grows with the length of the chain of MMAs into one accumulator (270 at
-// 18 terms and a 40-cell window), so the accumulator is restarted every `tg`
-// terms and each group's sum is added in FP32 (round to nearest) into the
-// output, which holds the running sum between groups.
+// 18 terms and a 40-cell window), so the terms are split into
+// ceil(Ka / tg) groups of as equal a size as possible (at most tg terms), the
+// accumulator restarts at each group, and the groups' sums are added in FP32
+// (round to nearest).  The running sum between groups lives in a dense
+// 128 KB slot buffer of the CTA's (SM, tensor-memory half), which stays in L2
+// (one slot per CTA that can be resident: the two CTAs of an SM hold
+// different tensor-memory columns), and the output is written once.
 //
 // Operands.  C is Toeplitz: the tile of window chunk n0 = 8c is
 //   C_c[x][i] = c_t((x0 + 8c + i - x) mod N) = E[x + W - 8 - 8c][i],
@@ -100,6 +104,18 @@ __device__ __forceinline__ float2 ld_shared_f2_const(uint32_t addr) {
     return v;
 }
 __device__ __forceinline__ uint32_t h2u(__half2 h) { return *reinterpret_cast<uint32_t*>(&h); }
+
+// Running-sum slot accesses: relaxed at GPU scope, like the atomic adds
+// between them, so that one thread's accesses to a cell stay in program
+// order (coherence of morally strong operations on one location).
+__device__ __forceinline__ void st_relaxed_f2(float2* p, float2 v) {
+    asm volatile("st.relaxed.gpu.global.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(v.x), "f"(v.y) : "memory");
+}
+__device__ __forceinline__ float2 ld_relaxed_f2(const float2* p) {
+    float2 v;
+    asm volatile("ld.relaxed.gpu.global.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p) : "memory");
+    return v;
+}
 
 // 8-row groups of the extended circulant tile E for a window of 8 n_chunks cells
 __host__ __device__ constexpr int tc_ext_groups(int n_chunks) { return 15 + n_chunks; }
@@ -193,7 +209,7 @@ template <int N>
 __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
     const float2* __restrict__ circ, const int8_t* __restrict__ cscale, const uint32_t* __restrict__ ent_t,
     const int32_t* __restrict__ tinfo, int Ka, const float2* __restrict__ tw, float2* __restrict__ g2t, int n_pad,
-    int n_rot, int x0, int W, int tg, int* __restrict__ err) {
+    int n_rot, int x0, int W, int tg, float2* __restrict__ slots, int n_slots, int* __restrict__ err) {
     static_assert(N <= 128, "the tensor pencil stage covers x in one 128-row tile");
     constexpr int H = N / 2 + 1;
     constexpr int NH = N * H;
@@ -244,6 +260,10 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = tmem_base;
+    // group of processing step k: ng groups, sizes differing by at most one
+    const int ng = (Ka + tg - 1) / tg;
+    auto group_of = [&](int k) { return (k * ng) / Ka; };
+    auto starts_group = [&](int k) { return k == 0 || group_of(k) != group_of(k - 1); };
     const uint32_t fb = tc::smem_u32(fbuf);
     const uint32_t ab = tc::smem_u32(abuf);
 
@@ -261,8 +281,8 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
             const uint64_t cim_l = tc::smem_desc(ab + 3 * RG * 256 + ao, TC_LBO, TC_SBO);
             const uint64_t f_h = tc::smem_desc(fb + c * TC_FCHUNK, TC_LBO, TC_SBO);
             const uint64_t f_l = tc::smem_desc(fb + c * TC_FCHUNK + TC_FTILE, TC_LBO, TC_SBO);
-            // each group of tg terms starts a fresh accumulator
-            const uint32_t acc = (k % tg == 0 && c == 0) ? 0u : 1u;
+            // each group of terms starts a fresh accumulator
+            const uint32_t acc = (starts_group(k) && c == 0) ? 0u : 1u;
             tc::mma_f16(d_re, cre_h, f_h, idesc, acc);
             tc::mma_f16(d_re, cre_h, f_l, idesc, 1u);
             tc::mma_f16(d_re, cre_l, f_h, idesc, 1u);
@@ -273,19 +293,29 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
         tc::mma_commit(&empty_bar);
     };
 
-    // TMEM -> x-quads g2t[rot][x/4][p][x%4] (a warp access covers 8 whole
-    // sectors): thread (warp, lane) holds output row x = 32 (warp % 4) +
-    // lane of the rotations [64 half, 64 half + 64).  The first group is
-    // stored; every later group is added with fire-and-forget FP32 atomic
-    // adds (round to nearest, performed in L2), so no thread waits for the
-    // running sum.  All accesses to one element come from one thread in
-    // program order, which fixes the order of the additions: the result is
-    // the same in every run.
-    const float inv = 1.0f / (c_scale * TC_F_SCALE);
-    auto drain = [&](bool first) {
-        const int xo = 32 * (warp & 3) + lane;  // TMEM lane = output row x
-        const uint32_t trow = (uint32_t)(32 * (warp & 3)) << 16;
-        const int half = tid >> 7;
+    // Thread (warp, lane) holds output row x = 32 (warp % 4) + lane of the
+    // rotations [64 half, 64 half + 64) (its TMEM lane and columns).
+    // Running sum of the completed groups: this CTA's slot, [rotation][x]
+    // raw accumulator values (a warp access covers 256 consecutive bytes).
+    // The first group's sum is stored, later ones are added with FP32
+    // atomic adds (round to nearest, performed in L2, no wait), and the last
+    // group's sum is added by the output pass.  Every access to one element
+    // comes from one thread in program order, so the order of the additions
+    // is fixed ((S1 + S2) + S3 ...) and the result the same in every run.
+    uint32_t smid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    const int slot = (int)smid * 2 + (int)((tmem >> 8) & 1u);  // 256-column allocations start at column 0 or 256
+    const bool slot_ok = slot < n_slots;
+    if (ng > 1 && !slot_ok && tid == 0) {
+        atomicOr(err, 32);
+        abort_flag = 1;
+    }
+    const int xo = 32 * (warp & 3) + lane;  // TMEM lane = output row x
+    const uint32_t trow = (uint32_t)(32 * (warp & 3)) << 16;
+    const int half = tid >> 7;
+    float2* const sb = slots + (size_t)(slot_ok ? slot : 0) * (TC_ROT * 128) + xo;
+    auto drain_group = [&](bool first) {
+        if (!slot_ok) return;
 #pragma unroll 1
         for (int cb = 0; cb < 4; ++cb) {
             const int c0 = half * 64 + cb * 16;
@@ -293,18 +323,40 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
             tc::tmem_ld_32x32b_x16(tmem + trow + c0, dre);
             tc::tmem_ld_32x32b_x16(tmem + trow + TC_ROT + c0, dim);
             tc::tmem_wait_ld();
-            if (xo < N) {
-                float2* ob = g2t + (size_t)(g * TC_ROT + c0) * NH * N + (size_t)(xo >> 2) * NH * 4 + (size_t)p * 4 +
-                             (xo & 3);
-                const int nj = min(16, n_rot - (g * TC_ROT + c0));
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const float2 v = make_float2(__uint_as_float(dre[j]) * inv, __uint_as_float(dim[j]) * inv);
-                    if (j < nj) {
-                        if (first) ob[(size_t)j * NH * N] = v;
-                        else atomicAdd(ob + (size_t)j * NH * N, v);
-                    }
-                }
+            for (int j = 0; j < 16; ++j) {
+                const float2 v = make_float2(__uint_as_float(dre[j]), __uint_as_float(dim[j]));
+                if (first) st_relaxed_f2(sb + (size_t)(c0 + j) * 128, v);
+                else atomicAdd(sb + (size_t)(c0 + j) * 128, v);
+            }
+        }
+    };
+    // TMEM (+ the running sum) -> x-quads g2t[rot][x/4][p][x%4] (a warp
+    // access covers 8 whole sectors), in blocks of 8 rotations.  The running
+    // sum of a block is loaded one block ahead; block 0's loads are issued
+    // before the wait for the last MMAs.
+    const float inv = 1.0f / (c_scale * TC_F_SCALE);
+    const bool with_sum = ng > 1 && slot_ok;
+    auto load_run = [&](int cb, float2 (&run)[8]) {
+        const int c0 = half * 64 + cb * 8;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) run[j] = ld_relaxed_f2(sb + (size_t)(c0 + j) * 128);
+    };
+    auto out_block = [&](int cb, const float2 (&run)[8]) {
+        const int c0 = half * 64 + cb * 8;
+        uint32_t dre[8], dim[8];
+        tc::tmem_ld_32x32b_x8(tmem + trow + c0, dre);
+        tc::tmem_ld_32x32b_x8(tmem + trow + TC_ROT + c0, dim);
+        tc::tmem_wait_ld();
+        if (xo < N) {
+            float2* ob = g2t + (size_t)(g * TC_ROT + c0) * NH * N + (size_t)(xo >> 2) * NH * 4 + (size_t)p * 4 +
+                         (xo & 3);
+            const int nj = min(8, n_rot - (g * TC_ROT + c0));
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                float2 v = make_float2(__uint_as_float(dre[j]), __uint_as_float(dim[j]));
+                if (with_sum) v = make_float2(run[j].x + v.x, run[j].y + v.y);
+                if (j < nj) ob[(size_t)j * NH * N] = make_float2(v.x * inv, v.y * inv);
             }
         }
     };
@@ -343,12 +395,12 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
                 atomicOr(err, 2);
                 abort_flag = 1;
             }
-            // a group of tg terms is complete in TMEM: add it into the output
+            // a group of terms is complete in TMEM: add it into the output
             // before term k restarts the accumulator (the loads have finished
             // when this thread arrives on full_bar below)
-            if (k >= 1 && k % tg == 0 && !*(volatile int*)&abort_flag) {
+            if (k >= 1 && starts_group(k) && !*(volatile int*)&abort_flag) {
                 tc::fence_after_sync();
-                drain(k == tg);
+                drain_group(group_of(k - 1) == 0);
                 tc::fence_before_sync();
             }
             // receptor circulant samples of the term, scaled and split
@@ -445,13 +497,21 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
         }
         // arrives when every MMA issued above has completed
         if (tid == 0) tc::mma_commit(&done_bar);
-        // ---- epilogue: TMEM -> x-quads g2t[rot][x/4][p][x%4] (a warp store fills 8 sectors) ----
+        // ---- epilogue: TMEM (+ running sum) -> x-quads g2t[rot][x/4][p][x%4] ----
+        float2 run_a[8], run_b[8];
+        if (with_sum) load_run(0, run_a);
         if (!*(volatile int*)&abort_flag && !tc::mbar_wait(&done_bar, 0, TC_WAIT_NS)) {
             atomicOr(err, 4);
             abort_flag = 1;
         }
         tc::fence_after_sync();
-        drain(Ka <= tg);
+#pragma unroll 1
+        for (int cb = 0; cb < 8; cb += 2) {
+            if (with_sum) load_run(cb + 1, run_b);
+            out_block(cb, run_a);
+            if (with_sum && cb + 2 < 8) load_run(cb + 2, run_a);
+            out_block(cb + 1, run_b);
+        }
     }
     // the MMA issuer's done barrier covers every MMA before TMEM is released
     if (tid == 0 && !tc::mbar_wait(&done_bar, 0, TC_WAIT_NS)) atomicOr(err, 16);

@@ -449,9 +449,12 @@ int fftdock_pair_grid(int32_t n_rec, const double* rec_xyz, int32_t n_lig, const
  * so that a caller can scan only the rotations it ranks best; the
  * exhaustive scan (fftdock_scan) stays the fallback and the measure of its
  * recall.  Network: three 3^3 stride-2 convolutions (16, 32, 64 channels,
- * ReLU) -> 512 features + descriptor -> 256 ReLU -> 1.  BF16 weights and
- * activations, FP32 accumulation, FP32 master weights trained with Adam; the
- * training step runs as one captured CUDA graph.
+ * ReLU) -> 512 features + descriptor -> 256 ReLU -> 1.  Every layer, forward
+ * and backward, is a batched BF16 tensor-core GEMM with FP32 accumulation
+ * (convolutions through im2col); BF16 weights, activations and activation
+ * gradients, FP32 master weights trained with Adam; the training step runs as
+ * one captured CUDA graph.  Calls on one network are ordered on its own
+ * stream (prediction on a caller's stream is fenced against it with events).
  * ------------------------------------------------------------------------ */
 #define FFTDOCK_PROPOSAL_DESC 128
 

@@ -7,8 +7,9 @@ The network, its parameter layout and its precision points are the ones
 the C ABI documents (``fftdock_proposal_*`` in include/fftdock.h).  This
 module computes the same forward and backward passes in float64 and rounds to
 BF16 exactly where the GPU stores BF16 (the weight copies, the occupancy grid,
-the ReLU outputs of every layer and the descriptor), so a GPU gradient must
-agree with it up to FP32 accumulation order.  With ``bf16=False`` everything
+the ReLU outputs of every layer, the descriptor, and the activation gradients
+dzf, dz3, dz2, dz1 that the backward GEMMs read), so a GPU gradient must agree
+with it up to FP32 accumulation order.  With ``bf16=False`` everything
 stays float64, which the finite-difference check of this module itself uses.
 
 The proposal has no counterpart in the reference; its occupancy grid uses the
@@ -179,17 +180,17 @@ def forward_backward(params, samples, targets, bf=True):
         # backward
         G["f2"] += dy * h1
         G["fb2"] += dy
-        dzf = np.where(h1 > 0, dy * W["f2"], 0.0)
+        dzf = rnd(np.where(h1 > 0, dy * W["f2"], 0.0))
         G["f1"] += np.outer(u, dzf)
         G["fb1"] += dzf
         du = W["f1"][:NA3] @ dzf
-        dz3 = np.where(a3.reshape(-1) > 0, du, 0.0).reshape(C3, -1)
+        dz3 = rnd(np.where(a3.reshape(-1) > 0, du, 0.0)).reshape(C3, -1)
         G["w3"] += np.stack([dz3 @ t3[k].T for k in range(27)], axis=-1).reshape(G["w3"].shape)
         G["b3"] += dz3.sum(axis=1)
-        dz2 = np.where(a2 > 0, _conv_bwd_data(dz3, W["w3"], D2), 0.0).reshape(C2, -1)
+        dz2 = rnd(np.where(a2 > 0, _conv_bwd_data(dz3, W["w3"], D2), 0.0)).reshape(C2, -1)
         G["w2"] += np.stack([dz2 @ t2[k].T for k in range(27)], axis=-1).reshape(G["w2"].shape)
         G["b2"] += dz2.sum(axis=1)
-        dz1 = np.where(a1 > 0, _conv_bwd_data(dz2, W["w2"], D1), 0.0).reshape(C1, -1)
+        dz1 = rnd(np.where(a1 > 0, _conv_bwd_data(dz2, W["w2"], D1), 0.0)).reshape(C1, -1)
         G["w1"] += np.stack([dz1 @ t1[k].T for k in range(27)], axis=-1).reshape(G["w1"].shape)
         G["b1"] += dz1.sum(axis=1)
     return loss, pack(G), np.array(preds)

@@ -3,9 +3,8 @@
 // A small network predicts, for one receptor/ligand pair and one rotation,
 // the best (lowest) correlation score the FFT scan would find for that
 // rotation, from a coarse occupancy grid of the rotated ligand and a
-// rotation-invariant receptor descriptor.  Rotations it ranks low are skipped
-// before the scan; the exhaustive scan stays the fallback and the judge of
-// its recall.
+// receptor descriptor.  Rotations it ranks low are skipped before the scan;
+// the exhaustive scan stays the fallback and the judge of its recall.
 //
 // Network (one sample):
 //   x0  16^3 occupancy of the rotated ligand (atom count / 4 per cell; the
@@ -17,15 +16,25 @@
 //   u  = [a3, receptor descriptor (128)]                  640
 //   h1 = relu(W1 u + b1)                                  256
 //   y  = w2 . h1 + b2
-// Precision: weights are used as BF16 copies of FP32 master weights;
-// activations x0, a1, a2, a3, u, h1 are stored as BF16; every sum is
-// accumulated in FP32; gradients are FP32; Adam updates the FP32 masters.
+//
+// Every contraction is a BF16 x BF16 -> FP32 GEMM on the tensor cores
+// (mma.sync m16n8k16), batched over the samples: each convolution is an
+// im2col matrix [samples x positions][taps x input channels] times the
+// weights [taps x input channels][output channels] (activations stored
+// channel-last), the fully connected layer [samples][640] x [640][256]; the
+// backward pass multiplies the BF16 activation gradients by the transposed
+// weights (input gradients, summed back over the taps by a gather: col2im)
+// and by the im2col matrices (weight gradients, reduced over samples and
+// positions with a deterministic split of K).
+// Precision: BF16 copies of the FP32 master weights (the convolution weights
+// also in [output channel][tap][input channel] order); activations x0, a1,
+// a2, a3, u, h1 and activation gradients dzf, dz3, dz2, dz1 stored as BF16;
+// every sum accumulated in FP32 in a fixed order; weight gradients FP32;
+// Adam updates the FP32 masters.
 //
 // Training step (captured once in a CUDA graph, replayed per step): sample
 // indices come from a hash of (seed, device step counter, slot), so a replay
-// needs no host input.  train_sample_kernel (forward + activation gradients,
-// one CTA per sample) -> conv/fc weight-gradient reductions over the batch ->
-// Adam (which advances the step counter).
+// needs no host input.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -50,9 +59,9 @@ constexpr int G0 = 16;
 constexpr int C1 = 16, C2 = 32, C3 = 64;
 constexpr int D1 = 8, D2 = 4, D3 = 2;
 constexpr int NX0 = G0 * G0 * G0;
-constexpr int NA1 = C1 * D1 * D1 * D1;
-constexpr int NA2 = C2 * D2 * D2 * D2;
-constexpr int NA3 = C3 * D3 * D3 * D3;
+constexpr int P1 = D1 * D1 * D1, P2 = D2 * D2 * D2, P3 = D3 * D3 * D3;  // output positions per layer
+constexpr int K1 = 32, K2 = 27 * C1, K3 = 27 * C2;                      // im2col widths (conv1: 27 taps padded)
+constexpr int NA3 = C3 * P3;
 constexpr int DESC = FFTDOCK_PROPOSAL_DESC;
 constexpr int NU = NA3 + DESC;
 constexpr int HID = 256;
@@ -69,9 +78,14 @@ constexpr int OFB1 = OF1 + NU * HID;
 constexpr int OF2 = OFB1 + HID;
 constexpr int OFB2 = OF2 + HID;
 constexpr int NPARAM = OFB2 + 1;
+// permuted BF16 convolution weights: wp1[co][K1], wp2[co][tap * C1 + ci], wp3[co][tap * C2 + ci]
+constexpr int OP1 = 0, OP2 = OP1 + C1 * K1, OP3 = OP2 + C2 * K2, NPERM = OP3 + C3 * K3;
 
 constexpr int THREADS = 256;
 constexpr int MAX_BATCH = 4096;
+constexpr int PREDICT_CHUNK = 4096;
+constexpr int WS_FLOATS = 1 << 19;  // split-K partial sums
+constexpr int kColsumParts = 64;    // row blocks of a bias-gradient column sum
 
 __device__ __forceinline__ float b2f(bf16 v) { return __bfloat162float(v); }
 __device__ __forceinline__ bf16 f2b(float v) { return __float2bfloat16_rn(v); }
@@ -85,8 +99,191 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
 }
 
 // ---------------------------------------------------------------------------
-// per-sample building blocks (THREADS threads, operands in shared memory)
+// GEMM: C[M][N] = A[M][K] x B[K][N], BF16 operands, FP32 accumulation on the
+// tensor cores.  A is row-major (AT = false: A[m * lda + k]) or stored
+// transposed (AT = true: A[k * lda + m]); B likewise ("KN", BT = false:
+// B[k * ldb + n]; "NK", BT = true: B[n * ldb + k]).  The contiguous extent of
+// each operand and its leading dimension are multiples of 8 and its base is
+// 16-byte aligned (checked by the host), so every global load is a uint4 of
+// 8 elements.  CTA tile 64 x 64 x 32, four warps of 32 x 32; tiles staged in
+// shared memory as [row][k] (pitch 40 elements: the fragment loads hit 32
+// distinct banks).  gridDim.z > 1 splits K into equal multiples of 32; each
+// split hands its partial sums to the epilogue with its index.
 // ---------------------------------------------------------------------------
+constexpr int GBM = 64, GBN = 64, GBK = 32, GPITCH = GBK + 8, GTHREADS = 128;
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+        "{%0, %1, %2, %3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// one 64 x 32 operand tile into smem[row][k]: rows r0.., k k0.. of a matrix
+// whose element (row, k) is at p[row * ld + k] (T = false) or p[k * ld + row]
+__device__ __forceinline__ void load_tile(bf16 (*s)[GPITCH], const bf16* __restrict__ p, int ld, bool T, int r0,
+                                          int rows, int k0, int k1) {
+    const int t = threadIdx.x;
+    if (!T) {
+        // 64 rows x 4 groups of 8 k
+        for (int e = t; e < 64 * 4; e += GTHREADS) {
+            const int rr = e >> 2, kk = (e & 3) * 8;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (r0 + rr < rows && k0 + kk < k1) v = *reinterpret_cast<const uint4*>(p + (size_t)(r0 + rr) * ld + k0 + kk);
+            *reinterpret_cast<uint4*>(&s[rr][kk]) = v;
+        }
+    } else {
+        // 32 k x 8 groups of 8 rows
+        for (int e = t; e < 32 * 8; e += GTHREADS) {
+            const int kk = e >> 3, rr = (e & 7) * 8;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (r0 + rr < rows && k0 + kk < k1) v = *reinterpret_cast<const uint4*>(p + (size_t)(k0 + kk) * ld + r0 + rr);
+            const uint32_t q[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                s[rr + i][kk] = __ushort_as_bfloat16((unsigned short)((q[i >> 1] >> (16 * (i & 1))) & 0xffffu));
+        }
+    }
+}
+
+template <bool AT, bool BT, class Epi>
+__global__ void __launch_bounds__(GTHREADS) gemm_kernel(int M, int N, int K, const bf16* __restrict__ A, int lda,
+                                                        const bf16* __restrict__ B, int ldb, int k_chunk, Epi epi) {
+    __shared__ __align__(16) bf16 As[GBM][GPITCH];
+    __shared__ __align__(16) bf16 Bs[GBN][GPITCH];
+    const int m0 = blockIdx.y * GBM, n0 = blockIdx.x * GBN;
+    const int kb = blockIdx.z * k_chunk, ke = min(K, kb + k_chunk);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+    const int gid = lane >> 2, tig = lane & 3;
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) acc[i][j][c] = 0.f;
+    for (int k0 = kb; k0 < ke; k0 += GBK) {
+        load_tile(As, A, lda, AT, m0, M, k0, ke);
+        load_tile(Bs, B, ldb, !BT, n0, N, k0, ke);
+        __syncthreads();
+#pragma unroll
+        for (int ks = 0; ks < GBK; ks += 16) {
+            uint32_t a[2][4], b[4][2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const int r = wm + 16 * i + gid;
+                a[i][0] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * tig]);
+                a[i][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * tig]);
+                a[i][2] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * tig + 8]);
+                a[i][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * tig + 8]);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int n = wn + 8 * j + gid;
+                b[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[n][ks + 2 * tig]);
+                b[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[n][ks + 2 * tig + 8]);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], a[i], b[j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int r = m0 + wm + 16 * i + gid + (c >= 2 ? 8 : 0);
+                const int n = n0 + wn + 8 * j + 2 * tig + (c & 1);
+                if (r < M && n < N) epi(r, n, acc[i][j][c], blockIdx.z);
+            }
+}
+
+// split-K partial sums ws[z][M][N] -> the epilogue, summed in split order
+template <class Epi>
+__global__ void splitk_reduce_kernel(const float* __restrict__ ws, int splits, int M, int N, Epi epi) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M * N) return;
+    float v = 0.f;
+    for (int z = 0; z < splits; ++z) v += ws[(size_t)z * M * N + i];
+    epi(i / N, i % N, v, 0);
+}
+
+struct EpiPartial {  // split-K: partial sums of split z
+    float* ws;
+    int M, N;
+    __device__ void operator()(int r, int c, float v, int z) const { ws[((size_t)z * M + r) * N + c] = v; }
+};
+struct EpiF32 {
+    float* out;
+    int ld;
+    __device__ void operator()(int r, int c, float v, int) const { out[(size_t)r * ld + c] = v; }
+};
+struct EpiBiasRelu {  // activations (channel-last rows)
+    bf16* out;
+    int ld;
+    const bf16* bias;
+    __device__ void operator()(int r, int c, float v, int) const {
+        v += b2f(bias[c]);
+        out[(size_t)r * ld + c] = f2b(v > 0.f ? v : 0.f);
+    }
+};
+struct EpiConv3 {  // row s * P3 + pos, column co -> u[s][co * P3 + pos]
+    bf16* u;
+    const bf16* bias;
+    __device__ void operator()(int r, int c, float v, int) const {
+        v += b2f(bias[c]);
+        u[(size_t)(r / P3) * NU + c * P3 + r % P3] = f2b(v > 0.f ? v : 0.f);
+    }
+};
+struct EpiDz3 {  // dU[s][i], i = co * P3 + pos < NA3 -> dz3[s * P3 + pos][co], masked by u > 0
+    bf16* dz3;
+    const bf16* u;
+    __device__ void operator()(int r, int c, float v, int) const {
+        const bool on = b2f(u[(size_t)r * NU + c]) > 0.f;
+        dz3[((size_t)r * P3 + c % P3) * C3 + c / P3] = f2b(on ? v : 0.f);
+    }
+};
+struct EpiWgrad {  // column tap * cin + ci of output channel r -> g[(r * cin + ci) * 27 + tap]
+    float* g;
+    int cin;
+    float* gbias;  // conv1: column 27 (the ones column of its im2col) is the bias gradient
+    __device__ void operator()(int r, int c, float v, int) const {
+        const int tap = c / cin, ci = c % cin;
+        if (tap < 27) g[((size_t)r * cin + ci) * 27 + tap] = v;
+        else if (gbias && tap == 27) gbias[r] = v;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// samples, occupancy and the im2col / col2im gathers
+// ---------------------------------------------------------------------------
+struct Ligands {
+    const double* xyz;    // all ligands' atoms, concatenated
+    const int* start;     // first atom of each ligand
+    const int* count;
+    const double* half;   // L of each ligand
+    const float* desc;    // [n_lig][DESC]
+};
+
+// where a batch's samples come from: hashed draws from the training set
+// (mode 0), the set's samples base.. in order (mode 1), or rotations
+// rot[base..] of one ligand (mode 2, prediction)
+struct SampleSrc {
+    int mode;
+    const int* lig;        // [n] (modes 0, 1)
+    const double* rot;     // [n][9]
+    int n;
+    int base;
+    int fixed_lig;         // mode 2
+    const uint32_t* step;  // mode 0
+    uint64_t seed;         // mode 0
+};
 
 // occupancy counts of the rotated ligand; p' = R p with the scan's operation
 // order (((r0 x0) + r1 x1) + r2 x2, no contraction), cell = floor((p' + L) /
@@ -111,298 +308,194 @@ __device__ void occupancy(const double* __restrict__ xyz, int n, double L, const
     __syncthreads();
 }
 
-// out = relu(conv(in) + b), 3^3 taps, stride 2, pad 1; out stored as BF16
-template <int CIN, int COUT, int DIN>
-__device__ void conv_fwd(const bf16* __restrict__ in, const bf16* __restrict__ w, const bf16* __restrict__ b,
-                         bf16* __restrict__ out) {
-    constexpr int DOUT = DIN / 2, P = DOUT * DOUT * DOUT, NIN = DIN * DIN * DIN;
-    for (int o = threadIdx.x; o < COUT * P; o += THREADS) {
-        const int co = o / P, r = o % P;
-        const int oz = r / (DOUT * DOUT), oy = (r / DOUT) % DOUT, ox = r % DOUT;
-        float acc = b2f(b[co]);
-        for (int ci = 0; ci < CIN; ++ci) {
-            const bf16* wk = w + (co * CIN + ci) * 27;
-            const bf16* ic = in + ci * NIN;
-#pragma unroll
-            for (int kz = 0; kz < 3; ++kz) {
-                const int z = 2 * oz - 1 + kz;
-                if (z < 0 || z >= DIN) continue;
-#pragma unroll
-                for (int ky = 0; ky < 3; ++ky) {
-                    const int y = 2 * oy - 1 + ky;
-                    if (y < 0 || y >= DIN) continue;
-#pragma unroll
-                    for (int kx = 0; kx < 3; ++kx) {
-                        const int x = 2 * ox - 1 + kx;
-                        if (x < 0 || x >= DIN) continue;
-                        acc += b2f(wk[(kz * 3 + ky) * 3 + kx]) * b2f(ic[(z * DIN + y) * DIN + x]);
-                    }
-                }
-            }
-        }
-        out[o] = f2b(acc > 0.f ? acc : 0.f);
-    }
+// input position of output position (oz, oy, ox) under tap t of a stride-2,
+// pad-1 3^3 convolution over a din^3 grid; -1 outside
+__device__ __forceinline__ int tap_source(int din, int oz, int oy, int ox, int t) {
+    const int z = 2 * oz - 1 + t / 9, y = 2 * oy - 1 + (t / 3) % 3, x = 2 * ox - 1 + t % 3;
+    if (z < 0 || z >= din || y < 0 || y >= din || x < 0 || x >= din) return -1;
+    return (z * din + y) * din + x;
 }
 
-// dz_in = conv^T(dout) masked by act_in > 0 (the ReLU of the layer below)
-template <int CIN, int COUT, int DIN>
-__device__ void conv_bwd_data(const float* __restrict__ dout, const bf16* __restrict__ w,
-                              const bf16* __restrict__ act_in, float* __restrict__ dz_in) {
-    constexpr int DOUT = DIN / 2, P = DOUT * DOUT * DOUT, NIN = DIN * DIN * DIN;
-    for (int e = threadIdx.x; e < CIN * NIN; e += THREADS) {
-        const int ci = e / NIN, r = e % NIN;
-        const int z = r / (DIN * DIN), y = (r / DIN) % DIN, x = r % DIN;
-        float acc = 0.f;
-        if (b2f(act_in[e]) > 0.f) {
-            for (int kz = 0; kz < 3; ++kz) {
-                const int tz = z + 1 - kz;
-                if (tz < 0 || (tz & 1) || (tz >> 1) >= DOUT) continue;
-                for (int ky = 0; ky < 3; ++ky) {
-                    const int ty = y + 1 - ky;
-                    if (ty < 0 || (ty & 1) || (ty >> 1) >= DOUT) continue;
-                    for (int kx = 0; kx < 3; ++kx) {
-                        const int tx = x + 1 - kx;
-                        if (tx < 0 || (tx & 1) || (tx >> 1) >= DOUT) continue;
-                        const int pos = ((tz >> 1) * DOUT + (ty >> 1)) * DOUT + (tx >> 1);
-                        const int k = (kz * 3 + ky) * 3 + kx;
-                        for (int co = 0; co < COUT; ++co) acc += b2f(w[(co * CIN + ci) * 27 + k]) * dout[co * P + pos];
-                    }
-                }
-            }
-        }
-        dz_in[e] = acc;
-    }
-}
-
-struct Ligands {
-    const double* xyz;    // all ligands' atoms, concatenated
-    const int* start;     // first atom of each ligand
-    const int* count;
-    const double* half;   // L of each ligand
-    const float* desc;    // [n_lig][DESC]
-};
-
-// shared memory of one sample's forward pass
-struct FwdSmem {
-    float occ[NX0];
-    bf16 x0[NX0];
-    bf16 a1[NA1];
-    bf16 a2[NA2];
-    bf16 u[NU];
-    bf16 h1[HID];
-    float red[THREADS / 32];
-};
-
-// forward of one sample; returns y on every thread
-__device__ float forward(const bf16* __restrict__ wb, const Ligands& lg, int lig, const double* rot, FwdSmem& s) {
-    occupancy(lg.xyz + 3 * (size_t)lg.start[lig], lg.count[lig], lg.half[lig], rot, s.occ);
-    for (int i = threadIdx.x; i < NX0; i += THREADS) s.x0[i] = f2b(0.25f * s.occ[i]);
-    for (int i = threadIdx.x; i < DESC; i += THREADS) s.u[NA3 + i] = f2b(lg.desc[(size_t)lig * DESC + i]);
-    __syncthreads();
-    conv_fwd<1, C1, G0>(s.x0, wb + OW1, wb + OB1, s.a1);
-    __syncthreads();
-    conv_fwd<C1, C2, D1>(s.a1, wb + OW2, wb + OB2, s.a2);
-    __syncthreads();
-    conv_fwd<C2, C3, D2>(s.a2, wb + OW3, wb + OB3, s.u);
-    __syncthreads();
-    {
-        const int j = threadIdx.x;  // THREADS == HID
-        float acc = b2f(wb[OFB1 + j]);
-        for (int i = 0; i < NU; ++i) acc += b2f(wb[OF1 + i * HID + j]) * b2f(s.u[i]);
-        s.h1[j] = f2b(acc > 0.f ? acc : 0.f);
-        float t = b2f(wb[OF2 + j]) * b2f(s.h1[j]);
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if ((j & 31) == 0) s.red[j >> 5] = t;
-    }
-    __syncthreads();
-    float y = b2f(wb[OFB2]);
-    for (int k = 0; k < THREADS / 32; ++k) y += s.red[k];
-    return y;
-}
-
-static_assert(THREADS == HID, "one thread per hidden unit");
-
-__global__ void __launch_bounds__(THREADS) predict_kernel(const bf16* __restrict__ wb, Ligands lg, int lig,
-                                                          const double* __restrict__ rot, int n,
-                                                          float* __restrict__ out) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    FwdSmem& s = *reinterpret_cast<FwdSmem*>(smem_raw);
+// one CTA per sample: occupancy -> x0 (BF16) -> conv1's im2col rows
+// x1c[s * P1 + pos][tap]: column 27 is 1 (its weight is zero, and the
+// weight-gradient GEMM gets the bias gradient there), 28..31 zero; the
+// descriptor -> u[s][NA3..]
+__global__ void __launch_bounds__(THREADS) prep_kernel(Ligands lg, SampleSrc src, bf16* __restrict__ x1c,
+                                                       bf16* __restrict__ u, int* __restrict__ sidx) {
+    __shared__ float occ[NX0];
+    __shared__ bf16 x0[NX0];
     const int b = blockIdx.x;
-    if (b >= n) return;
-    const float y = forward(wb, lg, lig, rot + 9 * (size_t)b, s);
-    if (threadIdx.x == 0) out[b] = y;
-}
-
-// activations and activation gradients of a batch, kept for the weight
-// gradients
-struct Store {
-    bf16* x0;     // [B][NX0]
-    bf16* a1;     // [B][NA1]
-    bf16* a2;     // [B][NA2]
-    bf16* u;      // [B][NU]
-    bf16* h1;     // [B][HID]
-    float* dz1;   // [B][NA1]
-    float* dz2;   // [B][NA2]
-    float* dz3;   // [B][NA3]
-    float* dzf;   // [B][HID]
-    float* dy;    // [B]
-};
-
-struct Samples {
-    const int* lig;        // [n]
-    const double* rot;     // [n][9]
-    const float* target;   // [n]
-    int n;
-};
-
-struct TrainSmem {
-    FwdSmem f;
-    float dzf[HID];
-    float dz3[NA3];
-    float dz2[NA2];
-};
-
-// one sample of a training batch: forward, loss, activation gradients.
-// explicit >= 0: sample b is explicit + b (no sampling)
-__global__ void __launch_bounds__(THREADS) train_sample_kernel(const bf16* __restrict__ wb, Ligands lg, Samples sm,
-                                                               const uint32_t* __restrict__ step_ctr, uint64_t seed,
-                                                               int batch, int explicit_base, Store st,
-                                                               double* __restrict__ loss_acc) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    TrainSmem& s = *reinterpret_cast<TrainSmem*>(smem_raw);
-    const int b = blockIdx.x;
-    int idx;
-    if (explicit_base >= 0) {
-        idx = explicit_base + b;
+    int idx, lig;
+    const double* rot;
+    if (src.mode == 2) {
+        idx = src.base + b;
+        lig = src.fixed_lig;
+        rot = src.rot + 9 * (size_t)idx;
     } else {
-        const uint64_t h = mix64(seed ^ mix64(((uint64_t)(*step_ctr) << 20) ^ (uint64_t)b));
-        idx = (int)(h % (uint64_t)sm.n);
+        if (src.mode == 1) {
+            idx = src.base + b;
+        } else {
+            const uint64_t h = mix64(src.seed ^ mix64(((uint64_t)(*src.step) << 20) ^ (uint64_t)b));
+            idx = (int)(h % (uint64_t)src.n);
+        }
+        lig = src.lig[idx];
+        rot = src.rot + 9 * (size_t)idx;
     }
-    const int lig = sm.lig[idx];
-    const float y = forward(wb, lg, lig, sm.rot + 9 * (size_t)idx, s.f);
-    const float t = sm.target[idx];
-    const float dy = 2.f * (y - t) / (float)batch;
-    const int tid = threadIdx.x;
-    if (tid == 0) {
-        st.dy[b] = dy;
+    if (threadIdx.x == 0 && sidx) sidx[b] = idx;
+    occupancy(lg.xyz + 3 * (size_t)lg.start[lig], lg.count[lig], lg.half[lig], rot, occ);
+    for (int i = threadIdx.x; i < NX0; i += THREADS) x0[i] = f2b(0.25f * occ[i]);
+    for (int i = threadIdx.x; i < DESC; i += THREADS) u[(size_t)b * NU + NA3 + i] = f2b(lg.desc[(size_t)lig * DESC + i]);
+    __syncthreads();
+    // rows of 32 taps as 4 groups of 8
+    for (int e = threadIdx.x; e < P1 * 4; e += THREADS) {
+        const int pos = e >> 2, t0 = (e & 3) * 8;
+        const int oz = pos / (D1 * D1), oy = (pos / D1) % D1, ox = pos % D1;
+        uint32_t q[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int t = t0 + i;
+            const int src_i = t < 27 ? tap_source(G0, oz, oy, ox, t) : -1;
+            const uint32_t h = t == 27 ? (uint32_t)__bfloat16_as_ushort(f2b(1.f))
+                                       : (src_i >= 0 ? (uint32_t)__bfloat16_as_ushort(x0[src_i]) : 0u);
+            q[i >> 1] |= h << (16 * (i & 1));
+        }
+        *reinterpret_cast<uint4*>(x1c + ((size_t)b * P1 + pos) * K1 + t0) = make_uint4(q[0], q[1], q[2], q[3]);
+    }
+}
+
+// im2col of a channel-last activation act[s * PIN + pos_in][CIN] into
+// col[s * POUT + pos][tap * CIN + ci]; one thread per (row, tap)
+template <int CIN, int DIN>
+__global__ void im2col_kernel(const bf16* __restrict__ act, bf16* __restrict__ col, int n_samples) {
+    constexpr int DOUT = DIN / 2, POUT = DOUT * DOUT * DOUT, PIN = DIN * DIN * DIN;
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)n_samples * POUT * 27) return;
+    const int t = (int)(e % 27);
+    const size_t row = e / 27;
+    const int s = (int)(row / POUT), pos = (int)(row % POUT);
+    const int src_i = tap_source(DIN, pos / (DOUT * DOUT), (pos / DOUT) % DOUT, pos % DOUT, t);
+    uint4* dst = reinterpret_cast<uint4*>(col + row * (27 * CIN) + t * CIN);
+    const uint4* sp = reinterpret_cast<const uint4*>(act + ((size_t)s * PIN + (src_i < 0 ? 0 : src_i)) * CIN);
+#pragma unroll
+    for (int i = 0; i < CIN / 8; ++i) dst[i] = src_i >= 0 ? sp[i] : make_uint4(0u, 0u, 0u, 0u);
+}
+
+// col2im: the input gradient of a convolution from the gradient of its
+// im2col matrix dcol[s * POUT + pos][tap * CIN + ci] (FP32), summed over the
+// taps in order, masked by act > 0 (the ReLU of the layer below), BF16
+template <int CIN, int DIN>
+__global__ void col2im_kernel(const float* __restrict__ dcol, const bf16* __restrict__ act, bf16* __restrict__ dz,
+                             int n_samples) {
+    constexpr int DOUT = DIN / 2, POUT = DOUT * DOUT * DOUT, PIN = DIN * DIN * DIN;
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)n_samples * PIN * CIN) return;
+    const int ci = (int)(e % CIN);
+    const size_t row = e / CIN;
+    const int s = (int)(row / PIN), p = (int)(row % PIN);
+    const int z = p / (DIN * DIN), y = (p / DIN) % DIN, x = p % DIN;
+    float acc = 0.f;
+    if (b2f(act[e]) > 0.f) {
+        for (int t = 0; t < 27; ++t) {
+            const int tz = z + 1 - t / 9, ty = y + 1 - (t / 3) % 3, tx = x + 1 - t % 3;
+            if (tz < 0 || ty < 0 || tx < 0 || (tz & 1) || (ty & 1) || (tx & 1)) continue;
+            if ((tz >> 1) >= DOUT || (ty >> 1) >= DOUT || (tx >> 1) >= DOUT) continue;
+            const int pos = ((tz >> 1) * DOUT + (ty >> 1)) * DOUT + (tx >> 1);
+            acc += dcol[((size_t)s * POUT + pos) * (27 * CIN) + t * CIN + ci];
+        }
+    }
+    dz[e] = f2b(acc);
+}
+
+// column sums out[c] = sum_r in[r * ld + c] (BF16 in, FP32 out) in a fixed
+// order: block (x, y) sums rows [y * chunk, (y + 1) * chunk) of columns
+// 32 x .. 32 x + 31 (lane = column, warps stride the rows) into
+// part[y][c]; colsum_final_kernel adds the parts in order
+__global__ void __launch_bounds__(THREADS) colsum_kernel(const bf16* __restrict__ in, int rows, int cols, int ld,
+                                                         int chunk, float* __restrict__ part) {
+    __shared__ float red[THREADS / 32][32];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    const int c = blockIdx.x * 32 + l;
+    const int r0 = blockIdx.y * chunk, r1 = min(rows, r0 + chunk);
+    float acc = 0.f;
+    if (c < cols)
+        for (int r = r0 + w; r < r1; r += THREADS / 32) acc += b2f(in[(size_t)r * ld + c]);
+    red[w][l] = acc;
+    __syncthreads();
+    if (w == 0 && c < cols) {
+        float v = 0.f;
+        for (int k = 0; k < THREADS / 32; ++k) v += red[k][l];
+        part[(size_t)blockIdx.y * cols + c] = v;
+    }
+}
+
+__global__ void colsum_final_kernel(const float* __restrict__ part, int parts, int cols, float* __restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cols) return;
+    float v = 0.f;
+    for (int k = 0; k < parts; ++k) v += part[(size_t)k * cols + c];
+    out[c] = v;
+}
+
+// head: y = w2 . h1 + b2 (one warp per sample).  Training (target != null):
+// loss, dy = 2 (y - t) / B and dzf = (h1 > 0) dy w2 (BF16)
+__global__ void __launch_bounds__(THREADS) head_kernel(const bf16* __restrict__ wb, const bf16* __restrict__ h1, int n,
+                                                       float* __restrict__ y_out, const float* __restrict__ target,
+                                                       const int* __restrict__ sidx, int batch, float* __restrict__ dy,
+                                                       bf16* __restrict__ dzf, double* __restrict__ loss_acc) {
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    const int s = blockIdx.x * (THREADS / 32) + w;
+    if (s >= n) return;
+    float acc = 0.f;
+    for (int j = l; j < HID; j += 32) acc += b2f(wb[OF2 + j]) * b2f(h1[(size_t)s * HID + j]);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    const float y = b2f(wb[OFB2]) + acc;
+    if (y_out && l == 0) y_out[s] = y;
+    if (!target) return;
+    const float t = target[sidx[s]];
+    const float d = 2.f * (y - t) / (float)batch;
+    if (l == 0) {
+        dy[s] = d;
         atomicAdd(loss_acc, (double)((y - t) * (y - t)) / (double)batch);
     }
-    // dz of the hidden layer (ReLU mask from h1)
-    {
-        const int j = tid;
-        const float g = b2f(s.f.h1[j]) > 0.f ? dy * b2f(wb[OF2 + j]) : 0.f;
-        s.dzf[j] = g;
-        st.dzf[(size_t)b * HID + j] = g;
-    }
-    __syncthreads();
-    // du for the conv features, masked by a3 > 0: one warp per input row
-    {
-        const int w = tid >> 5, l = tid & 31;
-        for (int i = w; i < NA3; i += THREADS / 32) {
-            float acc = 0.f;
-            for (int j = l; j < HID; j += 32) acc += b2f(wb[OF1 + i * HID + j]) * s.dzf[j];
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (l == 0) s.dz3[i] = b2f(s.f.u[i]) > 0.f ? acc : 0.f;
-        }
-    }
-    __syncthreads();
-    conv_bwd_data<C2, C3, D2>(s.dz3, wb + OW3, s.f.a2, s.dz2);
-    __syncthreads();
-    // dz1 goes straight to global memory
-    conv_bwd_data<C1, C2, D1>(s.dz2, wb + OW2, s.f.a1, st.dz1 + (size_t)b * NA1);
-    // stores for the weight gradients
-    for (int i = tid; i < NX0; i += THREADS) st.x0[(size_t)b * NX0 + i] = s.f.x0[i];
-    for (int i = tid; i < NA1; i += THREADS) st.a1[(size_t)b * NA1 + i] = s.f.a1[i];
-    for (int i = tid; i < NA2; i += THREADS) {
-        st.a2[(size_t)b * NA2 + i] = s.f.a2[i];
-        st.dz2[(size_t)b * NA2 + i] = s.dz2[i];
-    }
-    for (int i = tid; i < NU; i += THREADS) st.u[(size_t)b * NU + i] = s.f.u[i];
-    for (int i = tid; i < NA3; i += THREADS) st.dz3[(size_t)b * NA3 + i] = s.dz3[i];
-    st.h1[(size_t)b * HID + tid] = s.f.h1[tid];
+    for (int j = l; j < HID; j += 32)
+        dzf[(size_t)s * HID + j] = f2b(b2f(h1[(size_t)s * HID + j]) > 0.f ? d * b2f(wb[OF2 + j]) : 0.f);
 }
 
-// dW[co][ci][27] and db[co] of a conv layer, reduced over the batch; one
-// CTA per (co, ci)
-template <int CIN, int COUT, int DIN>
-__global__ void __launch_bounds__(THREADS) conv_wgrad_kernel(const bf16* __restrict__ act_in,
-                                                             const float* __restrict__ dz, int B,
-                                                             float* __restrict__ gw, float* __restrict__ gb) {
-    constexpr int DOUT = DIN / 2, P = DOUT * DOUT * DOUT, NIN = DIN * DIN * DIN;
-    __shared__ float red[28][THREADS / 32];
-    const int co = blockIdx.x / CIN, ci = blockIdx.x % CIN;
-    float acc[28];
-#pragma unroll
-    for (int k = 0; k < 28; ++k) acc[k] = 0.f;
-    for (int idx = threadIdx.x; idx < B * P; idx += THREADS) {
-        const int s = idx / P, pos = idx % P;
-        const float g = dz[((size_t)s * COUT + co) * P + pos];
-        if (g == 0.f) continue;
-        const int oz = pos / (DOUT * DOUT), oy = (pos / DOUT) % DOUT, ox = pos % DOUT;
-        const bf16* ic = act_in + ((size_t)s * CIN + ci) * NIN;
-#pragma unroll
-        for (int kz = 0; kz < 3; ++kz) {
-            const int z = 2 * oz - 1 + kz;
-#pragma unroll
-            for (int ky = 0; ky < 3; ++ky) {
-                const int y = 2 * oy - 1 + ky;
-#pragma unroll
-                for (int kx = 0; kx < 3; ++kx) {
-                    const int x = 2 * ox - 1 + kx;
-                    if (z >= 0 && z < DIN && y >= 0 && y < DIN && x >= 0 && x < DIN)
-                        acc[(kz * 3 + ky) * 3 + kx] += g * b2f(ic[(z * DIN + y) * DIN + x]);
-                }
-            }
-        }
-        acc[27] += g;
-    }
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-#pragma unroll
-    for (int k = 0; k < 28; ++k) {
-        float v = acc[k];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (l == 0) red[k][w] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < 28) {
-        float v = 0.f;
-        for (int k = 0; k < THREADS / 32; ++k) v += red[threadIdx.x][k];
-        if (threadIdx.x < 27) gw[(co * CIN + ci) * 27 + threadIdx.x] = v;
-        else if (ci == 0) gb[co] = v;
-    }
-}
-
-// fully connected gradients: blocks 0..NU-1 give dW1[i][*] (block 0 also
-// db1), block NU gives dw2 and db2
-__global__ void __launch_bounds__(THREADS) fc_wgrad_kernel(Store st, int B, float* __restrict__ g) {
+// dw2[j] = sum_s dy[s] h1[s][j], db2 = sum_s dy[s]
+__global__ void __launch_bounds__(THREADS) fc2_wgrad_kernel(const bf16* __restrict__ h1, const float* __restrict__ dy,
+                                                            int B, float* __restrict__ g) {
     const int j = threadIdx.x;
-    if (blockIdx.x < NU) {
-        const int i = blockIdx.x;
-        float acc = 0.f, accb = 0.f;
-        for (int s = 0; s < B; ++s) {
-            const float d = st.dzf[(size_t)s * HID + j];
-            acc += b2f(st.u[(size_t)s * NU + i]) * d;
-            accb += d;
-        }
-        g[OF1 + i * HID + j] = acc;
-        if (i == 0) g[OFB1 + j] = accb;
-    } else {
-        float acc = 0.f;
-        for (int s = 0; s < B; ++s) acc += b2f(st.h1[(size_t)s * HID + j]) * st.dy[s];
-        g[OF2 + j] = acc;
-        if (j == 0) {
-            float d = 0.f;
-            for (int s = 0; s < B; ++s) d += st.dy[s];
-            g[OFB2] = d;
-        }
+    float acc = 0.f;
+    for (int s = 0; s < B; ++s) acc += b2f(h1[(size_t)s * HID + j]) * dy[s];
+    g[OF2 + j] = acc;
+    if (j == 0) {
+        float d = 0.f;
+        for (int s = 0; s < B; ++s) d += dy[s];
+        g[OFB2] = d;
     }
 }
 
-// Adam on the FP32 masters (bias-corrected), BF16 copies refreshed; the last
-// thread of the grid advances the step counter
+// BF16 copies of master weight i: the master layout, and the permuted
+// convolution weights
+__device__ __forceinline__ void store_copies(int i, float w, bf16* __restrict__ wb, bf16* __restrict__ wp) {
+    const bf16 v = f2b(w);
+    wb[i] = v;
+    if (i >= OW1 && i < OB1) {
+        const int j = i - OW1;
+        wp[OP1 + (j / 27) * K1 + j % 27] = v;
+    } else if (i >= OW2 && i < OB2) {
+        const int j = i - OW2, co = j / (C1 * 27), ci = (j / 27) % C1, t = j % 27;
+        wp[OP2 + co * K2 + t * C1 + ci] = v;
+    } else if (i >= OW3 && i < OB3) {
+        const int j = i - OW3, co = j / (C2 * 27), ci = (j / 27) % C2, t = j % 27;
+        wp[OP3 + co * K3 + t * C2 + ci] = v;
+    }
+}
+
+// Adam on the FP32 masters (bias-corrected), BF16 copies refreshed
 __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
-                            const float* __restrict__ g, bf16* __restrict__ wb, uint32_t* __restrict__ step_ctr,
-                            float lr, float b1, float b2, float eps) {
+                            const float* __restrict__ g, bf16* __restrict__ wb, bf16* __restrict__ wp,
+                            const uint32_t* __restrict__ step_ctr, float lr, float b1, float b2, float eps) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t t = *step_ctr + 1u;
     if (i < NPARAM) {
@@ -415,15 +508,15 @@ __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float*
         const float vh = vi / (1.f - powf(b2, (float)t));
         const float wi = w[i] - lr * mh / (sqrtf(vh) + eps);
         w[i] = wi;
-        wb[i] = f2b(wi);
+        store_copies(i, wi, wb, wp);
     }
 }
 
 __global__ void step_advance_kernel(uint32_t* step_ctr) { *step_ctr += 1u; }
 
-__global__ void to_bf16_kernel(const float* __restrict__ w, bf16* __restrict__ wb, int n) {
+__global__ void to_bf16_kernel(const float* __restrict__ w, bf16* __restrict__ wb, bf16* __restrict__ wp) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) wb[i] = f2b(w[i]);
+    if (i < NPARAM) store_copies(i, w[i], wb, wp);
 }
 
 template <typename T> cudaError_t dalloc(T** p, size_t n) {
@@ -435,18 +528,67 @@ template <typename T> void dfree(T*& p) {
     p = nullptr;
 }
 
+// work buffers of a batch of up to cap samples
+struct Work {
+    int cap = 0;
+    bool grads = false;  // the backward buffers are allocated
+    bf16* x1c = nullptr;  // [cap * P1][K1]
+    bf16* a1 = nullptr;   // [cap * P1][C1]
+    bf16* x2c = nullptr;  // [cap * P2][K2]
+    bf16* a2 = nullptr;   // [cap * P2][C2]
+    bf16* x3c = nullptr;  // [cap * P3][K3]
+    bf16* u = nullptr;    // [cap][NU]
+    bf16* h1 = nullptr;   // [cap][HID]
+    int* sidx = nullptr;  // [cap] sample index of each slot
+    float* y = nullptr;   // [cap]
+    // backward
+    float* dy = nullptr;    // [cap]
+    bf16* dzf = nullptr;    // [cap][HID]
+    bf16* dz3 = nullptr;    // [cap * P3][C3]
+    float* dx3 = nullptr;   // [cap * P3][K3]
+    bf16* dz2 = nullptr;    // [cap * P2][C2]
+    float* dx2 = nullptr;   // [cap * P2][K2]
+    bf16* dz1 = nullptr;    // [cap * P1][C1]
+    float* ws = nullptr;    // [WS_FLOATS] split-K partial sums
+    float* cs = nullptr;    // [kColsumParts][HID] column-sum parts
+    void release() {
+        dfree(x1c);
+        dfree(a1);
+        dfree(x2c);
+        dfree(a2);
+        dfree(x3c);
+        dfree(u);
+        dfree(h1);
+        dfree(sidx);
+        dfree(y);
+        dfree(dy);
+        dfree(dzf);
+        dfree(dz3);
+        dfree(dx3);
+        dfree(dz2);
+        dfree(dx2);
+        dfree(dz1);
+        dfree(ws);
+        dfree(cs);
+        cap = 0;
+        grads = false;
+    }
+};
+
 }  // namespace
 
 struct fftdock_proposal {
     int device = 0;
     std::string err;
     cudaStream_t stream = nullptr;
+    cudaEvent_t ev = nullptr;
     // parameters
     float* w = nullptr;
     float* m = nullptr;
     float* v = nullptr;
     float* g = nullptr;
     bf16* wb = nullptr;
+    bf16* wp = nullptr;  // permuted convolution weights
     uint32_t* step = nullptr;
     double* loss = nullptr;
     // ligands (device copies grow by reallocation)
@@ -470,8 +612,7 @@ struct fftdock_proposal {
     int n_dev_samples = 0;
     bool samples_dirty = false;
     // batch work
-    int cap_batch = 0;
-    Store st{};
+    Work wk;
     // captured training step
     cudaGraphExec_t graph = nullptr;
     int graph_batch = 0;
@@ -494,8 +635,16 @@ int pfail(fftdock_proposal* p, int code, const std::string& msg) {
 
 Ligands ligands(const fftdock_proposal* p) { return Ligands{p->xyz, p->start, p->count, p->half, p->desc}; }
 
+void drop_graph(fftdock_proposal* p) {
+    if (p->graph) {
+        cudaGraphExecDestroy(p->graph);
+        p->graph = nullptr;
+    }
+}
+
 int sync_ligands(fftdock_proposal* p) {
     if (!p->lig_dirty) return FFTDOCK_OK;
+    PK(cudaStreamSynchronize(p->stream));
     dfree(p->xyz);
     dfree(p->start);
     dfree(p->count);
@@ -512,15 +661,13 @@ int sync_ligands(fftdock_proposal* p) {
     PK(cudaMemcpy(p->half, p->h_half.data(), p->h_half.size() * sizeof(double), cudaMemcpyHostToDevice));
     PK(cudaMemcpy(p->desc, p->h_desc.data(), p->h_desc.size() * sizeof(float), cudaMemcpyHostToDevice));
     p->lig_dirty = false;
-    if (p->graph) {
-        cudaGraphExecDestroy(p->graph);
-        p->graph = nullptr;
-    }
+    drop_graph(p);
     return FFTDOCK_OK;
 }
 
 int sync_samples(fftdock_proposal* p) {
     if (!p->samples_dirty) return FFTDOCK_OK;
+    PK(cudaStreamSynchronize(p->stream));
     dfree(p->s_lig);
     dfree(p->s_rot);
     dfree(p->s_target);
@@ -532,77 +679,145 @@ int sync_samples(fftdock_proposal* p) {
     PK(cudaMemcpy(p->s_target, p->h_target.data(), p->h_target.size() * sizeof(float), cudaMemcpyHostToDevice));
     p->n_dev_samples = (int)p->h_lig.size();
     p->samples_dirty = false;
-    if (p->graph) {
-        cudaGraphExecDestroy(p->graph);
-        p->graph = nullptr;
-    }
+    drop_graph(p);
     return FFTDOCK_OK;
 }
 
-void free_store(Store& s) {
-    dfree(s.x0);
-    dfree(s.a1);
-    dfree(s.a2);
-    dfree(s.u);
-    dfree(s.h1);
-    dfree(s.dz1);
-    dfree(s.dz2);
-    dfree(s.dz3);
-    dfree(s.dzf);
-    dfree(s.dy);
-}
-
-int grow_store(fftdock_proposal* p, int B) {
-    if (B <= p->cap_batch) return FFTDOCK_OK;
-    free_store(p->st);
-    p->cap_batch = 0;
-    Store& s = p->st;
-    PK(dalloc(&s.x0, (size_t)B * NX0));
-    PK(dalloc(&s.a1, (size_t)B * NA1));
-    PK(dalloc(&s.a2, (size_t)B * NA2));
-    PK(dalloc(&s.u, (size_t)B * NU));
-    PK(dalloc(&s.h1, (size_t)B * HID));
-    PK(dalloc(&s.dz1, (size_t)B * NA1));
-    PK(dalloc(&s.dz2, (size_t)B * NA2));
-    PK(dalloc(&s.dz3, (size_t)B * NA3));
-    PK(dalloc(&s.dzf, (size_t)B * HID));
-    PK(dalloc(&s.dy, (size_t)B));
-    p->cap_batch = B;
-    if (p->graph) {
-        cudaGraphExecDestroy(p->graph);
-        p->graph = nullptr;
+// work buffers for cap samples (backward buffers when grads)
+int grow_work(fftdock_proposal* p, int cap, bool grads) {
+    Work& w = p->wk;
+    if (cap <= w.cap && (!grads || w.grads)) return FFTDOCK_OK;
+    PK(cudaStreamSynchronize(p->stream));
+    const int c = std::max(cap, w.cap);
+    const bool gr = grads || w.grads;
+    w.release();
+    drop_graph(p);
+    PK(dalloc(&w.x1c, (size_t)c * P1 * K1));
+    PK(dalloc(&w.a1, (size_t)c * P1 * C1));
+    PK(dalloc(&w.x2c, (size_t)c * P2 * K2));
+    PK(dalloc(&w.a2, (size_t)c * P2 * C2));
+    PK(dalloc(&w.x3c, (size_t)c * P3 * K3));
+    PK(dalloc(&w.u, (size_t)c * NU));
+    PK(dalloc(&w.h1, (size_t)c * HID));
+    PK(dalloc(&w.sidx, (size_t)c));
+    PK(dalloc(&w.y, (size_t)c));
+    if (gr) {
+        PK(dalloc(&w.dy, (size_t)c));
+        PK(dalloc(&w.dzf, (size_t)c * HID));
+        PK(dalloc(&w.dz3, (size_t)c * P3 * C3));
+        PK(dalloc(&w.dx3, (size_t)c * P3 * K3));
+        PK(dalloc(&w.dz2, (size_t)c * P2 * C2));
+        PK(dalloc(&w.dx2, (size_t)c * P2 * K2));
+        PK(dalloc(&w.dz1, (size_t)c * P1 * C1));
+        PK(dalloc(&w.ws, (size_t)WS_FLOATS));
+        PK(dalloc(&w.cs, (size_t)kColsumParts * HID));
     }
+    w.cap = c;
+    w.grads = gr;
     return FFTDOCK_OK;
 }
 
-cudaError_t set_smem_attr() {
-    static std::once_flag once;
-    static cudaError_t res = cudaSuccess;
-    std::call_once(once, [] {
-        res = cudaFuncSetAttribute((const void*)predict_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)sizeof(FwdSmem));
-        if (res == cudaSuccess)
-            res = cudaFuncSetAttribute((const void*)train_sample_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TrainSmem));
-    });
-    return res;
-}
-
-// the batch's forward/backward and the weight gradients (no update)
-cudaError_t launch_gradients(fftdock_proposal* p, int B, uint64_t seed, int explicit_base, Samples sm,
-                             cudaStream_t s) {
-    train_sample_kernel<<<B, THREADS, sizeof(TrainSmem), s>>>(p->wb, ligands(p), sm, p->step, seed, B, explicit_base,
-                                                               p->st, p->loss);
+// C = A x B through gemm_kernel, K split into `splits` parts (partial sums
+// reduced in split order into the epilogue)
+template <bool AT, bool BT, class Epi>
+cudaError_t gemm(int M, int N, int K, const bf16* A, int lda, const bf16* B, int ldb, Epi epi, int splits, float* ws,
+                 cudaStream_t s) {
+    // the partial sums fit the workspace
+    splits = std::max(1, std::min(splits, (int)((size_t)WS_FLOATS / ((size_t)M * N))));
+    const int kc = ((K + splits * GBK - 1) / (splits * GBK)) * GBK;
+    splits = (K + kc - 1) / kc;
+    dim3 grid((N + GBN - 1) / GBN, (M + GBM - 1) / GBM, splits);
+    if (splits == 1) {
+        gemm_kernel<AT, BT, Epi><<<grid, GTHREADS, 0, s>>>(M, N, K, A, lda, B, ldb, kc, epi);
+        return cudaGetLastError();
+    }
+    gemm_kernel<AT, BT, EpiPartial><<<grid, GTHREADS, 0, s>>>(M, N, K, A, lda, B, ldb, kc, EpiPartial{ws, M, N});
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    conv_wgrad_kernel<1, C1, G0><<<C1 * 1, THREADS, 0, s>>>(p->st.x0, p->st.dz1, B, p->g + OW1, p->g + OB1);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    conv_wgrad_kernel<C1, C2, D1><<<C2 * C1, THREADS, 0, s>>>(p->st.a1, p->st.dz2, B, p->g + OW2, p->g + OB2);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    conv_wgrad_kernel<C2, C3, D2><<<C3 * C2, THREADS, 0, s>>>(p->st.a2, p->st.dz3, B, p->g + OW3, p->g + OB3);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    fc_wgrad_kernel<<<NU + 1, THREADS, 0, s>>>(p->st, B, p->g);
+    splitk_reduce_kernel<Epi><<<(M * N + 255) / 256, 256, 0, s>>>(ws, splits, M, N, epi);
     return cudaGetLastError();
+}
+
+// forward of n samples (n <= work capacity): u, h1 and y in the work buffers
+cudaError_t launch_forward(fftdock_proposal* p, int n, const SampleSrc& src, cudaStream_t s) {
+    Work& w = p->wk;
+    cudaError_t e;
+    prep_kernel<<<n, THREADS, 0, s>>>(ligands(p), src, w.x1c, w.u, w.sidx);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = gemm<false, true>(n * P1, C1, K1, w.x1c, K1, p->wp + OP1, K1, EpiBiasRelu{w.a1, C1, p->wb + OB1}, 1,
+                               nullptr, s)) != cudaSuccess)
+        return e;
+    const size_t c2 = (size_t)n * P2 * 27, c3 = (size_t)n * P3 * 27;
+    im2col_kernel<C1, D1><<<(unsigned)((c2 + 255) / 256), 256, 0, s>>>(w.a1, w.x2c, n);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = gemm<false, true>(n * P2, C2, K2, w.x2c, K2, p->wp + OP2, K2, EpiBiasRelu{w.a2, C2, p->wb + OB2}, 1,
+                               nullptr, s)) != cudaSuccess)
+        return e;
+    im2col_kernel<C2, D2><<<(unsigned)((c3 + 255) / 256), 256, 0, s>>>(w.a2, w.x3c, n);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = gemm<false, true>(n * P3, C3, K3, w.x3c, K3, p->wp + OP3, K3, EpiConv3{w.u, p->wb + OB3}, 1, nullptr,
+                               s)) != cudaSuccess)
+        return e;
+    return gemm<false, false>(n, HID, NU, w.u, NU, p->wb + OF1, HID, EpiBiasRelu{w.h1, HID, p->wb + OFB1}, 1, nullptr,
+                              s);
+}
+
+// K split of a weight gradient over rows samples x positions
+int wgrad_splits(int rows) { return std::max(1, std::min(256, rows / 1024)); }
+
+// bias gradient: column sums of a BF16 activation gradient [rows][cols]
+cudaError_t colsum(const bf16* in, int rows, int cols, float* part, float* out, cudaStream_t s) {
+    const int parts = std::max(1, std::min(kColsumParts, rows / 256));
+    const int chunk = (rows + parts - 1) / parts;
+    colsum_kernel<<<dim3((cols + 31) / 32, parts), THREADS, 0, s>>>(in, rows, cols, cols, chunk, part);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    colsum_final_kernel<<<(cols + 255) / 256, 256, 0, s>>>(part, parts, cols, out);
+    return cudaGetLastError();
+}
+
+// the batch's forward, loss, backward and weight gradients into p->g (no update)
+cudaError_t launch_gradients(fftdock_proposal* p, int B, const SampleSrc& src, const float* target, cudaStream_t s) {
+    Work& w = p->wk;
+    cudaError_t e = launch_forward(p, B, src, s);
+    if (e != cudaSuccess) return e;
+    float* g = p->g;
+    head_kernel<<<(B + 7) / 8, THREADS, 0, s>>>(p->wb, w.h1, B, w.y, target, w.sidx, B, w.dy, w.dzf, p->loss);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    fc2_wgrad_kernel<<<1, THREADS, 0, s>>>(w.h1, w.dy, B, g);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // fc1: dW1 = u^T dzf, db1 = column sums of dzf, du -> dz3 (masked by a3 > 0)
+    if ((e = gemm<true, false>(NU, HID, B, w.u, NU, w.dzf, HID, EpiF32{g + OF1, HID}, 1, nullptr, s)) != cudaSuccess)
+        return e;
+    if ((e = colsum(w.dzf, B, HID, w.cs, g + OFB1, s)) != cudaSuccess) return e;
+    if ((e = gemm<false, true>(B, NA3, HID, w.dzf, HID, p->wb + OF1, HID, EpiDz3{w.dz3, w.u}, 1, nullptr, s)) !=
+        cudaSuccess)
+        return e;
+    // conv3
+    const int r3 = B * P3, r2 = B * P2, r1 = B * P1;
+    if ((e = gemm<true, false>(C3, K3, r3, w.dz3, C3, w.x3c, K3, EpiWgrad{g + OW3, C2, nullptr}, wgrad_splits(r3),
+                               w.ws, s)) != cudaSuccess)
+        return e;
+    if ((e = colsum(w.dz3, r3, C3, w.cs, g + OB3, s)) != cudaSuccess) return e;
+    if ((e = gemm<false, false>(r3, K3, C3, w.dz3, C3, p->wp + OP3, K3, EpiF32{w.dx3, K3}, 1, nullptr, s)) !=
+        cudaSuccess)
+        return e;
+    const size_t e2 = (size_t)B * P2 * C2, e1 = (size_t)B * P1 * C1;
+    col2im_kernel<C2, D2><<<(unsigned)((e2 + 255) / 256), 256, 0, s>>>(w.dx3, w.a2, w.dz2, B);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // conv2
+    if ((e = gemm<true, false>(C2, K2, r2, w.dz2, C2, w.x2c, K2, EpiWgrad{g + OW2, C1, nullptr}, wgrad_splits(r2),
+                               w.ws, s)) != cudaSuccess)
+        return e;
+    if ((e = colsum(w.dz2, r2, C2, w.cs, g + OB2, s)) != cudaSuccess) return e;
+    if ((e = gemm<false, false>(r2, K2, C2, w.dz2, C2, p->wp + OP2, K2, EpiF32{w.dx2, K2}, 1, nullptr, s)) !=
+        cudaSuccess)
+        return e;
+    col2im_kernel<C1, D1><<<(unsigned)((e1 + 255) / 256), 256, 0, s>>>(w.dx2, w.a1, w.dz1, B);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // conv1 (the input needs no gradient; the bias gradient is column 27)
+    return gemm<true, false>(C1, K1, r1, w.dz1, C1, w.x1c, K1, EpiWgrad{g + OW1, 1, g + OB1}, wgrad_splits(r1), w.ws,
+                             s);
 }
 
 }  // namespace
@@ -629,13 +844,15 @@ int fftdock_proposal_create(int32_t device, uint64_t seed, fftdock_proposal** ou
     PK(cudaGetDeviceProperties(&prop, device));
     if (prop.major != 10 || prop.minor != 3)
         return pfail(p, FFTDOCK_EUNSUPPORTED, std::string("built for sm_103a only; device is ") + prop.name);
-    PK(set_smem_attr());
     PK(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+    PK(cudaEventCreateWithFlags(&p->ev, cudaEventDisableTiming));
     PK(dalloc(&p->w, NPARAM));
     PK(dalloc(&p->m, NPARAM));
     PK(dalloc(&p->v, NPARAM));
     PK(dalloc(&p->g, NPARAM));
     PK(dalloc(&p->wb, NPARAM));
+    PK(dalloc(&p->wp, NPERM));
+    PK(cudaMemset(p->wp, 0, NPERM * sizeof(bf16)));  // conv1's padding taps stay zero
     PK(dalloc(&p->step, 1));
     PK(dalloc(&p->loss, 1));
     // He-normal initial weights, zero biases
@@ -654,7 +871,7 @@ int fftdock_proposal_create(int32_t device, uint64_t seed, fftdock_proposal** ou
     PK(cudaMemset(p->m, 0, NPARAM * sizeof(float)));
     PK(cudaMemset(p->v, 0, NPARAM * sizeof(float)));
     PK(cudaMemset(p->step, 0, sizeof(uint32_t)));
-    to_bf16_kernel<<<(NPARAM + 255) / 256, 256, 0, p->stream>>>(p->w, p->wb, NPARAM);
+    to_bf16_kernel<<<(NPARAM + 255) / 256, 256, 0, p->stream>>>(p->w, p->wb, p->wp);
     PK(cudaGetLastError());
     PK(cudaStreamSynchronize(p->stream));
     return FFTDOCK_OK;
@@ -662,12 +879,14 @@ int fftdock_proposal_create(int32_t device, uint64_t seed, fftdock_proposal** ou
 
 void fftdock_proposal_destroy(fftdock_proposal* p) {
     if (!p) return;
+    if (p->stream) cudaStreamSynchronize(p->stream);
     if (p->graph) cudaGraphExecDestroy(p->graph);
     dfree(p->w);
     dfree(p->m);
     dfree(p->v);
     dfree(p->g);
     dfree(p->wb);
+    dfree(p->wp);
     dfree(p->step);
     dfree(p->loss);
     dfree(p->xyz);
@@ -678,7 +897,8 @@ void fftdock_proposal_destroy(fftdock_proposal* p) {
     dfree(p->s_lig);
     dfree(p->s_rot);
     dfree(p->s_target);
-    free_store(p->st);
+    p->wk.release();
+    if (p->ev) cudaEventDestroy(p->ev);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
 }
@@ -703,7 +923,7 @@ int fftdock_proposal_set_params(fftdock_proposal* p, const float* in) {
     PK(cudaMemset(p->m, 0, NPARAM * sizeof(float)));
     PK(cudaMemset(p->v, 0, NPARAM * sizeof(float)));
     PK(cudaMemset(p->step, 0, sizeof(uint32_t)));
-    to_bf16_kernel<<<(NPARAM + 255) / 256, 256, 0, p->stream>>>(p->w, p->wb, NPARAM);
+    to_bf16_kernel<<<(NPARAM + 255) / 256, 256, 0, p->stream>>>(p->w, p->wb, p->wp);
     PK(cudaGetLastError());
     PK(cudaStreamSynchronize(p->stream));
     return FFTDOCK_OK;
@@ -760,7 +980,7 @@ int fftdock_proposal_train(fftdock_proposal* p, int32_t steps, int32_t batch, fl
     fftdock::DeviceScope dev_scope(p->device);
     PK(dev_scope.status());
     int rc;
-    if ((rc = sync_ligands(p)) || (rc = sync_samples(p)) || (rc = grow_store(p, batch))) return rc;
+    if ((rc = sync_ligands(p)) || (rc = sync_samples(p)) || (rc = grow_work(p, batch, true))) return rc;
     if (p->n_dev_samples < 1) return pfail(p, FFTDOCK_ESTATE, "no training samples");
     if (p->graph && (p->graph_batch != batch || p->graph_lr != lr || p->graph_seed != seed)) {
         cudaGraphExecDestroy(p->graph);
@@ -768,12 +988,12 @@ int fftdock_proposal_train(fftdock_proposal* p, int32_t steps, int32_t batch, fl
     }
     cudaStream_t s = p->stream;
     if (!p->graph) {
-        Samples sm{p->s_lig, p->s_rot, p->s_target, p->n_dev_samples};
+        SampleSrc src{0, p->s_lig, p->s_rot, p->n_dev_samples, 0, 0, p->step, seed};
         cudaGraph_t g = nullptr;
         PK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = launch_gradients(p, batch, seed, -1, sm, s);
+        cudaError_t e = launch_gradients(p, batch, src, p->s_target, s);
         if (e == cudaSuccess) {
-            adam_kernel<<<(NPARAM + 255) / 256, 256, 0, s>>>(p->w, p->m, p->v, p->g, p->wb, p->step, lr, 0.9f,
+            adam_kernel<<<(NPARAM + 255) / 256, 256, 0, s>>>(p->w, p->m, p->v, p->g, p->wb, p->wp, p->step, lr, 0.9f,
                                                              0.999f, 1e-8f);
             e = cudaGetLastError();
         }
@@ -812,7 +1032,7 @@ int fftdock_proposal_gradients(fftdock_proposal* p, int32_t n, const int32_t* li
     fftdock::DeviceScope dev_scope(p->device);
     PK(dev_scope.status());
     int rc;
-    if ((rc = sync_ligands(p)) || (rc = grow_store(p, n))) return rc;
+    if ((rc = sync_ligands(p)) || (rc = grow_work(p, n, true))) return rc;
     cudaStream_t s = p->stream;
     int* d_lig = nullptr;
     double* d_rot = nullptr;
@@ -824,7 +1044,7 @@ int fftdock_proposal_gradients(fftdock_proposal* p, int32_t n, const int32_t* li
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_rot, rot, 9 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_t, target, n * sizeof(float), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(p->loss, 0, sizeof(double), s);
-    if (e == cudaSuccess) e = launch_gradients(p, n, 0, 0, Samples{d_lig, d_rot, d_t, n}, s);
+    if (e == cudaSuccess) e = launch_gradients(p, n, SampleSrc{1, d_lig, d_rot, n, 0, 0, nullptr, 0}, d_t, s);
     double l = 0.0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(grads, p->g, NPARAM * sizeof(float), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&l, p->loss, sizeof(double), cudaMemcpyDeviceToHost, s);
@@ -847,13 +1067,25 @@ int fftdock_proposal_predict_device(fftdock_proposal* p, int32_t lig, int32_t n,
     PK(dev_scope.status());
     int rc;
     if ((rc = sync_ligands(p))) return rc;
+    if ((rc = grow_work(p, std::min(n, PREDICT_CHUNK), false))) return rc;
     cudaStream_t s = stream ? (cudaStream_t)stream : p->stream;
     if (stream) {
-        // parameters may still be in flight on the library's own stream
-        PK(cudaStreamSynchronize(p->stream));
+        // parameters and work buffers are ordered on the library's stream
+        PK(cudaEventRecord(p->ev, p->stream));
+        PK(cudaStreamWaitEvent(s, p->ev, 0));
     }
-    predict_kernel<<<n, THREADS, sizeof(FwdSmem), s>>>(p->wb, ligands(p), lig, d_rot, n, d_out);
-    PK(cudaGetLastError());
+    for (int off = 0; off < n; off += PREDICT_CHUNK) {
+        const int nc = std::min(PREDICT_CHUNK, n - off);
+        PK(launch_forward(p, nc, SampleSrc{2, nullptr, d_rot, n, off, lig, nullptr, 0}, s));
+        head_kernel<<<(nc + 7) / 8, THREADS, 0, s>>>(p->wb, p->wk.h1, nc, d_out + off, nullptr, nullptr, nc, nullptr,
+                                                     nullptr, nullptr);
+        PK(cudaGetLastError());
+    }
+    if (stream) {
+        // later work on the library's stream reuses the buffers
+        PK(cudaEventRecord(p->ev, s));
+        PK(cudaStreamWaitEvent(p->stream, p->ev, 0));
+    }
     return FFTDOCK_OK;
 }
 

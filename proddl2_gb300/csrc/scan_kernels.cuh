@@ -696,28 +696,46 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     __syncthreads();
     const float tv = bound_v;
     const int ti = bound_i;
-    // every thread re-reads its own cells (the positions the row pass gave it)
+    auto offer = [&](float v, int i) {
+        if (!better(tv, ti, v, i)) {
+            const int at = atomicAdd(&n_cand, 1);
+            if (at < PCAND) { cand_sv[at] = v; cand_si[at] = i; }
+        }
+    };
+    if constexpr (WLR) {
+        // only a thread whose own minimum is at or below the bound holds
+        // cells at or below it (usually a few per plane): the warp re-reads
+        // each such lane's 64 cells together, two per lane (lane j: round
+        // j / 8, radix position j % 8 of the row pass)
+        unsigned qual = __ballot_sync(0xffffffffu, !better(tv, ti, bmin_v, bmin_i));
+        while (qual) {
+            const int L = __ffs(qual) - 1;
+            qual &= qual - 1u;
+            const int y = 32 * (l >> 3) + w + 8 * (L >> 3);
+            const int mm = (L & 7) + 8 * (l & 7);
+            const float2 o = plane[y * H + mm];
+            const int rowbase = (x * N + y) * N;
+            offer(o.x, rowbase + 2 * mm);
+            offer(o.y, rowbase + 2 * mm + 1);
+        }
+    } else {
+        // every thread re-reads its own cells (the positions the row pass gave it)
 #pragma unroll 1
-    for (int ro = 0; ro < ROUNDS; ++ro) {
-        const int y = row_of(ro);
-        if (y >= N) continue;
-        const float2* row = plane + y * H;
-        const int rowbase = (x * N + y) * N;
+        for (int ro = 0; ro < ROUNDS; ++ro) {
+            const int y = row_of(ro);
+            if (y >= N) continue;
+            const float2* row = plane + y * H;
+            const int rowbase = (x * N + y) * N;
 #pragma unroll
-        for (int i = 0; i < PR::NB; ++i)
+            for (int i = 0; i < PR::NB; ++i)
 #pragma unroll
-            for (int r = 0; r < GR; ++r) {
-                const int mm = m + GR * i + R1R * r;
-                const float2 o = row[mm];
-                if (!better(tv, ti, o.x, rowbase + 2 * mm)) {
-                    const int at = atomicAdd(&n_cand, 1);
-                    if (at < PCAND) { cand_sv[at] = o.x; cand_si[at] = rowbase + 2 * mm; }
+                for (int r = 0; r < GR; ++r) {
+                    const int mm = m + GR * i + R1R * r;
+                    const float2 o = row[mm];
+                    offer(o.x, rowbase + 2 * mm);
+                    offer(o.y, rowbase + 2 * mm + 1);
                 }
-                if (!better(tv, ti, o.y, rowbase + 2 * mm + 1)) {
-                    const int at = atomicAdd(&n_cand, 1);
-                    if (at < PCAND) { cand_sv[at] = o.y; cand_si[at] = rowbase + 2 * mm + 1; }
-                }
-            }
+        }
     }
     __syncthreads();
     const int nc = n_cand;

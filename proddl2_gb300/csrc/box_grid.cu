@@ -27,6 +27,7 @@
 
 #include "fft_core.cuh"
 #include "internal.h"
+#include "pencil_tc.cuh"
 #include "scan_kernels.cuh"
 
 namespace fftdock {
@@ -213,12 +214,15 @@ __global__ void box_half_extract_kernel(const double2* __restrict__ full, double
 // ligand prep: rotate (the reference's operation order, no FMA), toLogical
 // per axis, bins (t, x), stable sort (one CTA per rotation)
 // ---------------------------------------------------------------------------
+// ent_t (tensor form): the transposed entries of ligand_prep_kernel
 __global__ void __launch_bounds__(256) box_prep_kernel(const double* __restrict__ rot,
                                                        const double* __restrict__ lig_xyz,
                                                        const int32_t* __restrict__ lig_term, int n_ent, int K, Geo geo,
                                                        uint32_t* __restrict__ ent_out, int32_t* __restrict__ offs_out,
                                                        int32_t* __restrict__ status, const float* __restrict__ w_in,
-                                                       float* __restrict__ w_out, int32_t* __restrict__ idx_out) {
+                                                       float* __restrict__ w_out, int32_t* __restrict__ idx_out,
+                                                       uint32_t* __restrict__ ent_t, const int32_t* __restrict__ tpad,
+                                                       int n_pad, int x0, int W) {
     extern __shared__ unsigned char smem_raw[];
     const int nx = geo.n[0], ny = geo.n[1], nz = geo.n[2];
     const int nbins = K * nx;
@@ -292,6 +296,14 @@ __global__ void __launch_bounds__(256) box_prep_kernel(const double* __restrict_
             if (act) dst = cnt[bin] + rank;
             __syncwarp();
             if (act) ent[dst] = key;
+            // [q / 128][row / 4][q % 128][row % 4], x relative to x0 (cells
+            // outside the window at the dummy row W), as in ligand_prep_kernel
+            if (act && ent_t) {
+                const size_t row = (size_t)(dst + __ldg(tpad + (key >> 24)));
+                ent_t[(((size_t)(q >> 7) * (n_pad >> 2) + (row >> 2)) * 128 + (q & 127)) * 4 + (row & 3)] =
+                    (min(((key >> 16) - (uint32_t)x0) & 255u, (uint32_t)W) << 24) | (((key >> 8) & 255u) << 16) |
+                    (key & 255u);
+            }
             if (act && w_out) {
                 w_out[(size_t)q * n_ent + dst] = w_in[i];
                 idx_out[(size_t)q * n_ent + dst] = i;
@@ -428,14 +440,15 @@ __global__ void __launch_bounds__(32 * kBoxWarps, 2) box_pencil_kernel(
 // part); every warp keeps the KC smallest (value, offset) of its rows, and
 // warp 0 merges them into the plane's pool.
 // ---------------------------------------------------------------------------
-template <bool DBG>
+// QUAD: input = the tensor pencil stage's x-quads [B][nxp / 4][nh][4]
+template <bool DBG, bool QUAD>
 __global__ void __launch_bounds__(32 * kBoxWarps, 2) box_plane_kernel(const float2* __restrict__ g2,
                                                                   const float2* __restrict__ twy_g,
                                                                   const float2* __restrict__ twz_g, BoxPlan ply,
                                                                   BoxPlan plz, int nx, int pp,
                                                                   float* __restrict__ cand_v,
                                                                   int32_t* __restrict__ cand_i,
-                                                                  float* __restrict__ dbg) {
+                                                                  float* __restrict__ dbg, int nxp) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ny = ply.n, nz = plz.n, hz = nz / 2 + 1;
     const int lmax = ny > nz ? ny : nz;
@@ -450,8 +463,14 @@ __global__ void __launch_bounds__(32 * kBoxWarps, 2) box_plane_kernel(const floa
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     for (int i = tid; i < ny; i += blockDim.x) twy[i] = twy_g[i];
     for (int i = tid; i < nz; i += blockDim.x) twz[i] = twz_g[i];
-    const float2* src = g2 + ((size_t)q * nx + x) * pp;
-    for (int i = tid; i < ny * hz; i += blockDim.x) plane[i] = src[i];
+    if constexpr (QUAD) {
+        const size_t nh = (size_t)ny * hz;
+        const float2* src = g2 + (size_t)q * nxp * nh + (size_t)(x >> 2) * nh * 4 + (x & 3);
+        for (int i = tid; i < ny * hz; i += blockDim.x) plane[i] = src[(size_t)i * 4];
+    } else {
+        const float2* src = g2 + ((size_t)q * nx + x) * pp;
+        for (int i = tid; i < ny * hz; i += blockDim.x) plane[i] = src[i];
+    }
     __syncthreads();
     float2* a = wbuf + (size_t)w * 2 * lmax;
     float2* b = a + lmax;
@@ -636,7 +655,18 @@ cudaError_t box_prep(const BatchArgs& a, cudaStream_t s) {
     cudaError_t e = set_smem((const void*)box_prep_kernel, sm);
     if (e != cudaSuccess) return e;
     box_prep_kernel<<<nb, 256, sm, s>>>(a.rot, a.lig_xyz, a.lig_term, a.n_ent, a.K, a.box, a.ent, a.offs, a.status,
-                                        a.lig_w32, a.lig_w32 ? a.ent_w : nullptr, a.ent_idx);
+                                        a.lig_w32, a.lig_w32 ? a.ent_w : nullptr, a.ent_idx,
+                                        a.use_tc ? a.ent_t : nullptr, a.tpad, a.n_pad, a.x0, a.W);
+    return cudaGetLastError();
+}
+
+template <bool DBG, bool QUAD>
+cudaError_t box_plane(dim3 grid, size_t sm, const float2* src, const float2* twy, const float2* twz, const BoxPlan& py,
+                      const BoxPlan& pz, int nx, const BatchArgs& a, float* dbg, int nxp, cudaStream_t s) {
+    cudaError_t e = set_smem((const void*)box_plane_kernel<DBG, QUAD>, sm);
+    if (e != cudaSuccess) return e;
+    box_plane_kernel<DBG, QUAD><<<grid, 32 * kBoxWarps, sm, s>>>(src, twy, twz, py, pz, nx, a.PP, a.cand_v, a.cand_i,
+                                                                dbg, nxp);
     return cudaGetLastError();
 }
 
@@ -654,6 +684,28 @@ cudaError_t box_middle(const BatchArgs& a, cudaStream_t s) {
     const bool weighted = a.lig_w32 != nullptr;
     const size_t sm2 = pencil_smem_bytes(nx, ny, nz, a.K, a.n_ent, weighted);
     const int np = ny * (nz / 2 + 1);
+    const size_t sm3 = plane_smem_bytes(ny, nz);
+    dim3 grid3(nx, nb);
+    if (a.use_tc) {
+        // tensor form: the x stage as split-FP16 tcgen05 GEMMs over 128
+        // rotations per CTA, then the plane stage from its x-quads
+        const int nxp = (nx + 3) / 4 * 4;
+        const size_t smt = tc_smem_bytes_box(nx, ny, nz, a.W / 8, a.n_tc_terms);
+        if ((e = set_smem((const void*)pencil_tc_kernel<0>, smt)) != cudaSuccess) return e;
+        dim3 gridt(np, (nb + TC_ROT - 1) / TC_ROT);
+        const int tg = a.tc_group > 0 ? a.tc_group : FFTDOCK_TC_TERMS_PER_SUM_DEFAULT;
+        const TcBox bx{nx, ny, nz, nz / 2 + 1, np, nxp, twy, twz};
+        pencil_tc_kernel<0><<<gridt, TC_THREADS, smt, s>>>(a.circ, a.cscale, a.ent_t, a.tinfo, a.n_tc_terms, nullptr,
+                                                          a.g2t, a.n_pad, nb, a.x0, a.W, tg, a.tc_slots,
+                                                          a.tc_n_slots, bx, a.err);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (a.ev && (e = cudaEventRecord(a.ev[1], s)) != cudaSuccess) return e;
+        e = a.dbg_corr ? box_plane<true, true>(grid3, sm3, a.g2t, twy, twz, py, pz, nx, a, a.dbg_corr, nxp, s)
+                       : box_plane<false, true>(grid3, sm3, a.g2t, twy, twz, py, pz, nx, a, nullptr, nxp, s);
+        if (e != cudaSuccess) return e;
+        if (a.ev && (e = cudaEventRecord(a.ev[2], s)) != cudaSuccess) return e;
+        return cudaSuccess;
+    }
     dim3 grid2(nb, (np + kBoxWarps - 1) / kBoxWarps);
     if (weighted) {
         if ((e = set_smem((const void*)box_pencil_kernel<true>, sm2)) != cudaSuccess) return e;
@@ -668,18 +720,9 @@ cudaError_t box_middle(const BatchArgs& a, cudaStream_t s) {
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (a.ev && (e = cudaEventRecord(a.ev[1], s)) != cudaSuccess) return e;
-    const size_t sm3 = plane_smem_bytes(ny, nz);
-    dim3 grid3(nx, nb);
-    if (a.dbg_corr) {
-        if ((e = set_smem((const void*)box_plane_kernel<true>, sm3)) != cudaSuccess) return e;
-        box_plane_kernel<true><<<grid3, 32 * kBoxWarps, sm3, s>>>(a.g2, twy, twz, py, pz, nx, a.PP, a.cand_v,
-                                                                 a.cand_i, a.dbg_corr);
-    } else {
-        if ((e = set_smem((const void*)box_plane_kernel<false>, sm3)) != cudaSuccess) return e;
-        box_plane_kernel<false><<<grid3, 32 * kBoxWarps, sm3, s>>>(a.g2, twy, twz, py, pz, nx, a.PP, a.cand_v,
-                                                                  a.cand_i, nullptr);
-    }
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    e = a.dbg_corr ? box_plane<true, false>(grid3, sm3, a.g2, twy, twz, py, pz, nx, a, a.dbg_corr, nx, s)
+                   : box_plane<false, false>(grid3, sm3, a.g2, twy, twz, py, pz, nx, a, nullptr, nx, s);
+    if (e != cudaSuccess) return e;
     if (a.ev && (e = cudaEventRecord(a.ev[2], s)) != cudaSuccess) return e;
     return cudaSuccess;
 }
@@ -709,7 +752,7 @@ cudaError_t box_load_kernels(int) {
     cudaFuncAttributes fa;
     cudaError_t e = cudaFuncGetAttributes(&fa, (const void*)box_prep_kernel);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)box_pencil_kernel<false>);
-    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)box_plane_kernel<false>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)box_plane_kernel<false, false>);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)box_finalize_kernel);
     return e;
 }
@@ -727,7 +770,7 @@ size_t box_pencil_smem(int nx, int ny, int nz, int K, int n_ent, bool weighted) 
 // ([Nx][PP] float2, scaled 1 / V): complex z transforms, the half spectrum
 // kz < Hz, then y and x transforms, each a batch of line FFTs.
 cudaError_t box_receptor_fft(const double* rgrid_t, double2* cbuf, double2* hbuf, const double2* tw64,
-                             const int dims[3], void* spec_t, int PP, cudaStream_t s) {
+                             const int dims[3], void* spec_t, int PP, float2* circ_t, cudaStream_t s) {
     const int nx = dims[0], ny = dims[1], nz = dims[2], hz = nz / 2 + 1;
     BoxPlan px, py, pz;
     if (!factor_plan(nx, px) || !factor_plan(ny, py) || !factor_plan(nz, pz)) return cudaErrorInvalidValue;
@@ -754,12 +797,28 @@ cudaError_t box_receptor_fft(const double* rgrid_t, double2* cbuf, double2* hbuf
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     // y: lines (x, kz) of [Nx][Ny][Hz]
     if ((e = lines(hbuf, twy, py, (long)nx * hz, hz, hz, 1, (long)ny * hz)) != cudaSuccess) return e;
+    if (circ_t) {
+        // transformed along z and y only: the tensor stage's circulant samples
+        const size_t tot = (size_t)nx * ny * hz;
+        pack_circ_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(hbuf, circ_t, nx, ny * hz,
+                                                                     1.0 / ((double)ny * nz));
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
     // x: lines p = (ky, kz)
     if ((e = lines(hbuf, twx, px, (long)ny * hz, (long)ny * hz, (long)ny * hz, 1, 0)) != cudaSuccess) return e;
     const size_t tot = (size_t)nx * PP;
     box_pack_spectrum_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(hbuf, static_cast<float2*>(spec_t), nx,
                                                                            ny * hz, PP, 1.0 / (double)V);
     return cudaGetLastError();
+}
+
+cudaError_t box_circ_scales(const float2* circ, int K, int nh, int nx, int8_t* cscale, cudaStream_t s) {
+    circ_scale_box_kernel<<<(nh + 127) / 128, 128, 0, s>>>(circ, K, nh, nx, cscale);
+    return cudaGetLastError();
+}
+
+size_t box_tc_smem(const int dims[3], int n_chunks, int n_terms) {
+    return tc_smem_bytes_box(dims[0], dims[1], dims[2], n_chunks, n_terms);
 }
 
 const SizeOps* box_ops() {

@@ -164,7 +164,7 @@ template <int N> struct SizeOpsImpl {
                 const int tg = a.tc_group > 0 ? a.tc_group : FFTDOCK_TC_TERMS_PER_SUM_DEFAULT;
                 pencil_tc_kernel<N><<<gridt, TC_THREADS, smt, s>>>(a.circ, a.cscale, a.ent_t, a.tinfo,
                                                                   a.n_tc_terms, a.tw32, a.g2t, a.n_pad, nb, a.x0,
-                                                                  a.W, tg, a.tc_slots, a.tc_n_slots, a.err);
+                                                                  a.W, tg, a.tc_slots, a.tc_n_slots, TcBox{}, a.err);
                 if ((e = cudaGetLastError()) != cudaSuccess) return e;
             }
         }

@@ -608,8 +608,9 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
                                                        "] with no prime factor above 13");
         ctx->ops = fftdock::box_ops();
         ctx->box = true;
-        if (c.pencil_mode == FFTDOCK_PENCIL_TENSOR)
-            return fail(ctx, FFTDOCK_EUNSUPPORTED, "box grids (" + dims_s + ") run the FFT pencil stage");
+        if (c.pencil_mode == FFTDOCK_PENCIL_TENSOR && dims[0] > fftdock::kTcRot)
+            return fail(ctx, FFTDOCK_EUNSUPPORTED,
+                        "the tensor-core pencil stage covers x sizes up to 128 (grid " + dims_s + ")");
         if (c.precision != FFTDOCK_PREC_FP32)
             return fail(ctx, FFTDOCK_EUNSUPPORTED, "box grids keep FP32 receptor spectra");
         if (c.cluster_trans || c.peaks_per_rot > fftdock::kKC)
@@ -628,14 +629,16 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
         return fail(ctx, FFTDOCK_EINVAL, "unknown pencil_mode");
     if (c.tc_terms_per_sum < 0 || c.tc_terms_per_sum > fftdock::kTcMaxTerms)
         return fail(ctx, FFTDOCK_EINVAL, "tc_terms_per_sum must be in [0, 64]");
-    if (c.pencil_mode == FFTDOCK_PENCIL_TENSOR && !ctx->ops->has_tc)
+    // the tensor form: cubic edges up to 128, box grids with Nx up to 128
+    const bool has_tc = ctx->box ? dims[0] <= fftdock::kTcRot : ctx->ops->has_tc;
+    if (c.pencil_mode == FFTDOCK_PENCIL_TENSOR && !has_tc)
         return fail(ctx, FFTDOCK_EUNSUPPORTED, "the tensor-core pencil stage covers grid edges up to 128");
     // AUTO runs the tensor form where it applies (faster at 128^3 with 18
     // terms); the FFT form keeps the more accurate FP32 candidate values
     const bool lj_set = c.term_set == FFTDOCK_TERMS_LJ_COMP || c.term_set == FFTDOCK_TERMS_LJ_AVG;
     const int k_terms = c.term_set == FFTDOCK_TERMS_SHAPE_ACE ? c.n_types : 1;
     ctx->use_tc = c.pencil_mode == FFTDOCK_PENCIL_TENSOR ||
-                  (c.pencil_mode == FFTDOCK_PENCIL_AUTO && ctx->ops->has_tc && !lj_set &&
+                  (c.pencil_mode == FFTDOCK_PENCIL_AUTO && has_tc && !lj_set &&
                    c.precision == FFTDOCK_PREC_FP32 && k_terms >= fftdock::kTcMinTerms);
     if (!(c.shape_core_radius >= 0.0) || !(c.shape_surface_width >= 0.0))
         return fail(ctx, FFTDOCK_EINVAL, "shape radii must be >= 0");
@@ -750,14 +753,17 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
     CK(dalloc(&ctx->rgrid, (size_t)ctx->K * ctx->V));
     CK(dalloc(&ctx->offs, (size_t)ctx->G * (ctx->K * N + 1)));
     CK(dalloc(&ctx->g2, (size_t)ctx->B * N * ctx->PP));
-    if (ctx->use_tc) CK(dalloc(&ctx->g2t, (size_t)ctx->B * N * ctx->H * N));
+    // pencils (ky, kz) and the x extent of the tensor stage's x-quads
+    const size_t n_pencils = (size_t)dims[1] * ctx->H;
+    const size_t nx_quads = (size_t)(dims[0] + 3) / 4 * 4;
+    if (ctx->use_tc) CK(dalloc(&ctx->g2t, (size_t)ctx->B * nx_quads * n_pencils));
     CK(dalloc(&ctx->cand_v, (size_t)ctx->G * N * fftdock::kKC));
     CK(dalloc(&ctx->cand_i, (size_t)ctx->G * N * fftdock::kKC));
     CK(dalloc(&ctx->err_dev, 1));
     CK(cudaMemset(ctx->err_dev, 0, sizeof(int)));
     if (ctx->use_tc) {
-        CK(dalloc(&ctx->circ, (size_t)ctx->K * N * ctx->H * N));
-        CK(dalloc(&ctx->cscale, (size_t)N * ctx->H));
+        CK(dalloc(&ctx->circ, (size_t)ctx->K * n_pencils * dims[0]));
+        CK(dalloc(&ctx->cscale, n_pencils));
         CK(fftdock::tc_slot_count(&ctx->tc_n_slots));
         CK(dalloc(&ctx->tc_slots, (size_t)ctx->tc_n_slots * fftdock::kTcRot * 128));
     }
@@ -886,15 +892,21 @@ int fftdock_set_receptor(fftdock_ctx* ctx, int32_t n, const double* xyz, const i
     for (int t = 0; t < ctx->K; ++t) {
         const size_t elem = c.precision == FFTDOCK_PREC_BF16_SPECTRA ? 4 : 8;
         void* spec_t = static_cast<unsigned char*>(ctx->spec) + (size_t)t * N * ctx->PP * elem;
+        // the tensor stage's circulant samples of term t: [pencils][Nx]
+        float2* circ_t = ctx->use_tc ? ctx->circ + (size_t)t * ctx->dims[1] * ctx->H * ctx->dims[0] : nullptr;
         if (ctx->box)
             CKR(fftdock::box_receptor_fft(ctx->rgrid + (size_t)t * V, cbuf, hbuf, ctx->btw64, ctx->dims, spec_t,
-                                          ctx->PP, s));
+                                          ctx->PP, circ_t, s));
         else
             CKR(ctx->ops->receptor_fft(ctx->rgrid + (size_t)t * V, cbuf, hbuf, ctx->tw64, spec_t,
-                                       c.precision == FFTDOCK_PREC_BF16_SPECTRA ? 1 : 0, ctx->PP,
-                                       ctx->use_tc ? ctx->circ + (size_t)t * N * ctx->H * N : nullptr, s));
+                                       c.precision == FFTDOCK_PREC_BF16_SPECTRA ? 1 : 0, ctx->PP, circ_t, s));
     }
-    if (ctx->use_tc) CKR(ctx->ops->circ_scales(ctx->circ, ctx->K, ctx->cscale, s));
+    if (ctx->use_tc) {
+        if (ctx->box)
+            CKR(fftdock::box_circ_scales(ctx->circ, ctx->K, ctx->dims[1] * ctx->H, ctx->dims[0], ctx->cscale, s));
+        else
+            CKR(ctx->ops->circ_scales(ctx->circ, ctx->K, ctx->cscale, s));
+    }
     CKR(cudaStreamSynchronize(s));
     cleanup();
 #undef CKR
@@ -934,8 +946,9 @@ int fftdock_set_ligand(fftdock_ctx* ctx, int32_t n, const double* xyz, const int
     CK(dalloc(&ctx->ent, (size_t)ctx->G * n));
     CK(cudaMemcpy(ctx->lig_xyz, xyz, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->lig_term, term.data(), (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice));
-    const fftdock::TcTables tt = ctx->box ? fftdock::TcTables{}
-                                          : fftdock::tc_tables(xyz, term.data(), n, ctx->K, ctx->N, ctx->h, ctx->zero_h);
+    fftdock::TcTables tt = fftdock::tc_tables(xyz, term.data(), n, ctx->K, ctx->N, ctx->h, ctx->zero_h);
+    // box grids: the tensor stage's phase tables grow with Ny + Nz
+    if (ctx->box && tt.ok && fftdock::box_tc_smem(ctx->dims, tt.W / 8, tt.ka) > fftdock::kMaxSmem) tt.ok = false;
     ctx->x0 = tt.x0;
     ctx->W = tt.W;
     ctx->n_ent = n;
@@ -1120,7 +1133,7 @@ int fftdock_set_pair_lj(fftdock_ctx* ctx, int32_t n_rec, const double* rec_xyz, 
         void* spec_t = static_cast<unsigned char*>(ctx->spec) + (size_t)t * N * ctx->PP * 8;
         if (ctx->box)
             CKR(fftdock::box_receptor_fft(ctx->rgrid + (size_t)t * V, cbuf, hbuf, ctx->btw64, ctx->dims, spec_t,
-                                          ctx->PP, s));
+                                          ctx->PP, nullptr, s));
         else
             CKR(ctx->ops->receptor_fft(ctx->rgrid + (size_t)t * V, cbuf, hbuf, ctx->tw64, spec_t, 0, ctx->PP,
                                        nullptr, s));

@@ -279,9 +279,15 @@ bool box_plan(int n, BoxPlan* pl);
 // largest dynamic shared memory of the box-grid kernels for a ligand
 size_t box_pencil_smem(int nx, int ny, int nz, int K, int n_ent, bool weighted);
 // forward transform of one real FP64 term grid into spec_t ([Nx][PP] float2,
-// scaled 1/V); tw64 = the FP64 twiddle tables [Nx | Ny | Nz]
+// scaled 1/V); tw64 = the FP64 twiddle tables [Nx | Ny | Nz]; circ_t (tensor
+// form): the term's circulant samples [Ny Hz][Nx] (the grid transformed
+// along z and y only, conjugated, / (Ny Nz))
 cudaError_t box_receptor_fft(const double* rgrid_t, double2* cbuf, double2* hbuf, const double2* tw64,
-                             const int dims[3], void* spec_t, int PP, cudaStream_t s);
+                             const int dims[3], void* spec_t, int PP, float2* circ_t, cudaStream_t s);
+// per-pencil scale exponents of the box grid's circulant samples
+cudaError_t box_circ_scales(const float2* circ, int K, int nh, int nx, int8_t* cscale, cudaStream_t s);
+// dynamic shared memory of the tensor pencil stage on a box grid
+size_t box_tc_smem(const int dims[3], int n_chunks, int n_terms);
 
 // Read-only view of a ready context's scan inputs (receptor spectra and
 // grids, ligand, geometry); the work pointers of `args` are the context's own.

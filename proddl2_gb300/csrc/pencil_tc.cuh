@@ -120,6 +120,17 @@ __device__ __forceinline__ float2 ld_relaxed_f2(const float2* p) {
 // 8-row groups of the extended circulant tile E for a window of 8 n_chunks cells
 __host__ __device__ constexpr int tc_ext_groups(int n_chunks) { return 15 + n_chunks; }
 
+// Box grids (pencil_tc_kernel<0>): sizes per axis, nx <= 128 (one 128-row
+// tile), pencil p = ky hz + kz of nh = ny hz pencils, x-quads over nxp = nx
+// rounded up to 4, and the FP32 twiddle tables of the y and z axes
+// (e^{-2 pi i m / n}).  The phase of an entry is the product of its y and z
+// phases, from two tables per CTA (its pencil's ky and kz).
+struct TcBox {
+    int nx, ny, nz, hz, nh, nxp;
+    const float2* twy;
+    const float2* twz;
+};
+
 // dynamic shared memory of pencil_tc_kernel: F tiles / staging rows
 // [chunks][hi|lo], E tiles [4 parts][groups][256 B], phase table [N][32]
 // float2, staged samples [N], side slots [128] float2, term table; at least
@@ -127,6 +138,15 @@ __host__ __device__ constexpr int tc_ext_groups(int n_chunks) { return 15 + n_ch
 __host__ __device__ inline size_t tc_smem_bytes(int N, int n_chunks, int n_terms) {
     size_t b = (size_t)n_chunks * TC_FCHUNK + 1024 + (size_t)4 * tc_ext_groups(n_chunks) * 256 + (size_t)N * 32 * 8 +
                (size_t)N * sizeof(TcPair) + (size_t)TC_ROT * 8 + (size_t)(2 * n_terms + 1) * 4;
+    b = (b + 15) & ~(size_t)15;
+    return b < 76 * 1024 ? 76 * 1024 : b;
+}
+// box grids: the y and z phase tables per half-warp lane ([n][16] float2)
+// in place of the [N][32] table
+__host__ __device__ inline size_t tc_smem_bytes_box(int nx, int ny, int nz, int n_chunks, int n_terms) {
+    size_t b = (size_t)n_chunks * TC_FCHUNK + 1024 + (size_t)4 * tc_ext_groups(n_chunks) * 256 +
+               (size_t)(ny + nz) * 16 * 8 + (size_t)nx * sizeof(TcPair) + (size_t)TC_ROT * 8 +
+               (size_t)(2 * n_terms + 1) * 4;
     b = (b + 15) & ~(size_t)15;
     return b < 76 * 1024 ? 76 * 1024 : b;
 }
@@ -145,9 +165,11 @@ __device__ __forceinline__ unsigned tc_phase(uint32_t e, uint32_t kyz) {
     else return (((e & 0xffffffu) * kyz) >> 16) % (unsigned)N;
 }
 
+// N = 0 (box grids): twl and tzl are this lane's columns of the y and z
+// phase tables ([n][16] float2), and the phase is their complex product.
 template <bool SIDE, int N>
-__device__ __forceinline__ void tc_entries8(const uint32_t (&e)[8], uint32_t kyz, uint32_t twl, uint32_t stg,
-                                            uint32_t sd, unsigned first, unsigned& cur, float2& acc) {
+__device__ __forceinline__ void tc_entries8(const uint32_t (&e)[8], uint32_t kyz, uint32_t twl, uint32_t tzl,
+                                            uint32_t stg, uint32_t sd, unsigned first, unsigned& cur, float2& acc) {
     float2 z[8];
     unsigned xr[8];
 #pragma unroll
@@ -155,7 +177,13 @@ __device__ __forceinline__ void tc_entries8(const uint32_t (&e)[8], uint32_t kyz
         // x relative to the window start; padding and cells outside the
         // window carry x' = W, a dummy staging row
         xr[q] = e[q] >> 24;
-        z[q] = ld_shared_f2_const(twl + tc_phase<N>(e[q], kyz) * 256u);
+        if constexpr (N == 0) {
+            const float2 a = ld_shared_f2_const(twl + ((e[q] >> 16) & 255u) * 128u);
+            const float2 b = ld_shared_f2_const(tzl + (e[q] & 255u) * 128u);
+            z[q] = make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+        } else {
+            z[q] = ld_shared_f2_const(twl + tc_phase<N>(e[q], kyz) * 256u);
+        }
     }
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -175,7 +203,7 @@ __device__ __forceinline__ void tc_entries8(const uint32_t (&e)[8], uint32_t kyz
 // one is summed; the loads may run up to 16 rows past the range, which the
 // entry buffer provides.
 template <bool SIDE, int N>
-__device__ __forceinline__ void tc_walk(const uint4* eq, int nblk, uint32_t kyz, uint32_t twl,
+__device__ __forceinline__ void tc_walk(const uint4* eq, int nblk, uint32_t kyz, uint32_t twl, uint32_t tzl,
                                         uint32_t stg, uint32_t sd, unsigned first, unsigned W, uint4 a0, uint4 a1,
                                         uint4 b0, uint4 b1) {
     (void)W;
@@ -189,7 +217,7 @@ __device__ __forceinline__ void tc_walk(const uint4* eq, int nblk, uint32_t kyz,
     };
     auto sum = [&](const uint4& x0, const uint4& x1) {
         const uint32_t e[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
-        tc_entries8<SIDE, N>(e, kyz, twl, stg, sd, first, cur, acc);
+        tc_entries8<SIDE, N>(e, kyz, twl, tzl, stg, sd, first, cur, acc);
     };
     for (int blk = 0; blk < nblk; blk += 3) {
         ld(blk + 2, c0, c1);
@@ -204,23 +232,29 @@ __device__ __forceinline__ void tc_walk(const uint4* eq, int nblk, uint32_t kyz,
 }
 
 // tinfo: [0, Ka] padded entry starts (multiples of 8) of the Ka non-empty
-// terms, [Ka + 1, 2 Ka] their term ids; n_pad = entry rows per rotation group
+// terms, [Ka + 1, 2 Ka] their term ids; n_pad = entry rows per rotation group.
+// N = 0: a box grid of the sizes in bx (every N-dependent length below is
+// then bx's runtime value).
 template <int N>
 __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
     const float2* __restrict__ circ, const int8_t* __restrict__ cscale, const uint32_t* __restrict__ ent_t,
     const int32_t* __restrict__ tinfo, int Ka, const float2* __restrict__ tw, float2* __restrict__ g2t, int n_pad,
-    int n_rot, int x0, int W, int tg, float2* __restrict__ slots, int n_slots, int* __restrict__ err) {
+    int n_rot, int x0, int W, int tg, float2* __restrict__ slots, int n_slots, TcBox bx, int* __restrict__ err) {
     static_assert(N <= 128, "the tensor pencil stage covers x in one 128-row tile");
-    constexpr int H = N / 2 + 1;
-    constexpr int NH = N * H;
+    constexpr bool BOX = N == 0;
+    const int nx = BOX ? bx.nx : N;                  // x extent (correlation length)
+    const int H = BOX ? bx.hz : N / 2 + 1;           // kz per ky
+    const int NH = BOX ? bx.nh : N * (N / 2 + 1);    // pencils
+    const int NXP = BOX ? bx.nxp : N;                // x extent of the x-quads
     const int NC = W >> 3;
     const int RG = tc_ext_groups(NC);
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* fbuf = smem_raw;                                            // [NC][hi | lo]
     unsigned char* abuf = fbuf + NC * TC_FCHUNK + 1024;                        // [4][RG][256] after the dummy row
-    float2* twr = reinterpret_cast<float2*>(abuf + 4 * RG * 256);              // [N][32]
-    TcPair* pr = reinterpret_cast<TcPair*>(twr + N * 32);                      // [N]
-    float2* side = reinterpret_cast<float2*>(pr + N);                          // [128]
+    float2* twr = reinterpret_cast<float2*>(abuf + 4 * RG * 256);              // [N][32] (box: [ny][16], [nz][16])
+    const int tw_len = BOX ? (bx.ny + bx.nz) * 16 : N * 32;
+    TcPair* pr = reinterpret_cast<TcPair*>(twr + tw_len);                      // [nx]
+    float2* side = reinterpret_cast<float2*>(pr + nx);                         // [128]
     int32_t* tinf = reinterpret_cast<int32_t*>(side + TC_ROT);                 // [2 Ka + 1]
     __shared__ __align__(8) uint64_t full_bar;
     __shared__ __align__(8) uint64_t empty_bar;
@@ -241,9 +275,19 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
     // a timeout elsewhere in this launch already failed the scan: do nothing
     if (abort_flag) return;
 
-    for (int i = tid; i < N * 32; i += blockDim.x) {
-        const float2 v = tw[i >> 5];
-        twr[i] = make_float2(v.x * TC_F_SCALE, v.y * TC_F_SCALE);
+    if constexpr (BOX) {
+        // this pencil's phases along y (scaled by the F scale) and z, per
+        // half-warp lane: the lookups of a half-warp never share a bank
+        for (int i = tid; i < bx.ny * 16; i += blockDim.x) {
+            const float2 v = bx.twy[(int)(((unsigned)(i >> 4) * ky) % (unsigned)bx.ny)];
+            twr[i] = make_float2(v.x * TC_F_SCALE, v.y * TC_F_SCALE);
+        }
+        for (int i = tid; i < bx.nz * 16; i += blockDim.x) twr[bx.ny * 16 + i] = bx.twz[(int)(((unsigned)(i >> 4) * kz) % (unsigned)bx.nz)];
+    } else {
+        for (int i = tid; i < N * 32; i += blockDim.x) {
+            const float2 v = tw[i >> 5];
+            twr[i] = make_float2(v.x * TC_F_SCALE, v.y * TC_F_SCALE);
+        }
     }
     for (int i = tid; i <= 2 * Ka; i += blockDim.x) tinf[i] = tinfo[i];
     if (warp == 0) {
@@ -348,15 +392,15 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
         tc::tmem_ld_32x32b_x8(tmem + trow + c0, dre);
         tc::tmem_ld_32x32b_x8(tmem + trow + TC_ROT + c0, dim);
         tc::tmem_wait_ld();
-        if (xo < N) {
-            float2* ob = g2t + (size_t)(g * TC_ROT + c0) * NH * N + (size_t)(xo >> 2) * NH * 4 + (size_t)p * 4 +
+        if (xo < nx) {
+            float2* ob = g2t + (size_t)(g * TC_ROT + c0) * NH * NXP + (size_t)(xo >> 2) * NH * 4 + (size_t)p * 4 +
                          (xo & 3);
             const int nj = min(8, n_rot - (g * TC_ROT + c0));
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 float2 v = make_float2(__uint_as_float(dre[j]), __uint_as_float(dim[j]));
                 if (with_sum) v = make_float2(run[j].x + v.x, run[j].y + v.y);
-                if (j < nj) ob[(size_t)j * NH * N] = make_float2(v.x * inv, v.y * inv);
+                if (j < nj) ob[(size_t)j * NH * NXP] = make_float2(v.x * inv, v.y * inv);
             }
         }
     };
@@ -367,7 +411,10 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
         const int half = tid >> 7;
         // this rotation's quads of rows of the group ([g][row / 4][rotation][4])
         const uint4* ent_g = reinterpret_cast<const uint4*>(ent_t) + (size_t)g * (n_pad / 4) * TC_ROT + r;
-        const uint32_t twl = tc::smem_u32(twr) + (uint32_t)lane * 8u;  // this lane's copy of the phase table
+        // this lane's copy of the phase table (box: its half-warp column of
+        // the y table, and of the z table)
+        const uint32_t twl = tc::smem_u32(twr) + (uint32_t)(BOX ? (lane & 15) : lane) * 8u;
+        const uint32_t tzl = BOX ? twl + (uint32_t)bx.ny * 128u : 0u;
         const uint32_t stg = fb + (uint32_t)r * 8u;                     // staging row x' at stg + 1024 x'
         const uint32_t sd = tc::smem_u32(side) + (uint32_t)r * 8u;
         const uint32_t r0 = tc::kmajor_offset((uint32_t)r, 0, TC_LBO, TC_SBO);
@@ -385,7 +432,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
             pa1 = __ldg(q + TC_ROT);
             pb0 = __ldg(q + 2 * TC_ROT);
             pb1 = __ldg(q + 3 * TC_ROT);
-            if (tid < N) cpre = circ[((size_t)tinf[Ka + 1 + kk] * NH + p) * N + tid];
+            if (tid < nx) cpre = circ[((size_t)tinf[Ka + 1 + kk] * NH + p) * nx + tid];
         };
         preload(0);
         for (int k = 0; k < Ka; ++k) {
@@ -404,7 +451,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
                 tc::fence_before_sync();
             }
             // receptor circulant samples of the term, scaled and split
-            if (tid < N) {
+            if (tid < nx) {
                 const float2 c = cpre;
                 const float cr = c.x * c_scale, ci = c.y * c_scale;
                 TcPair v;
@@ -418,13 +465,13 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
             asm volatile("bar.sync 1, 256;" ::: "memory");
             // extended circulant tile E: row e, k = 2i + {re, im} -> c((x0 + W - 8 + i - e) mod N)
             for (int e = tid; e < 8 * RG; e += 256) {
-                int d0 = (x0 + W - 8 - e) % N;
-                if (d0 < 0) d0 += N;
+                int d0 = (x0 + W - 8 - e) % nx;
+                if (d0 < 0) d0 += nx;
                 TcPair v[8];
 #pragma unroll
                 for (int i2 = 0; i2 < 8; ++i2) {
                     const int d = d0 + i2;
-                    v[i2] = pr[d < N ? d : d - N];
+                    v[i2] = pr[d < nx ? d : d - nx];
                 }
                 const uint32_t o0 = tc::kmajor_offset((uint32_t)e, 0, TC_LBO, TC_SBO);
                 const uint32_t o1 = tc::kmajor_offset((uint32_t)e, 8, TC_LBO, TC_SBO);
@@ -446,9 +493,9 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
             // the second half's first bin goes to the side slot
             const unsigned first = half && nb8 > 0 ? (pa0.x >> 24) : 0xfffffffeu;
             if (half)
-                tc_walk<true, N>(eq, nb8, kyz, twl, stg, sd, first, (unsigned)W, pa0, pa1, pb0, pb1);
+                tc_walk<true, N>(eq, nb8, kyz, twl, tzl, stg, sd, first, (unsigned)W, pa0, pa1, pb0, pb1);
             else
-                tc_walk<false, N>(eq, nb8, kyz, twl, stg, sd, first, (unsigned)W, pa0, pa1, pb0, pb1);
+                tc_walk<false, N>(eq, nb8, kyz, twl, tzl, stg, sd, first, (unsigned)W, pa0, pa1, pb0, pb1);
             asm volatile("bar.sync 1, 256;" ::: "memory");
             // the second half's first bin: add its partial sum
             if (half && first < (unsigned)W) {
@@ -537,6 +584,27 @@ __global__ void circ_scale_kernel(const float2* __restrict__ circ, int K, int8_t
     if (m > 0.f) {
         int ex;
         frexpf(m, &ex);  // m in [2^(ex-1), 2^ex)
+        e = 13 - ex;
+    }
+    e = e < -100 ? -100 : (e > 100 ? 100 : e);
+    cscale[p] = (int8_t)e;
+}
+
+// box grids: the same per pencil p < nh over samples d < nx
+static __global__ void circ_scale_box_kernel(const float2* __restrict__ circ, int K, int nh, int nx,
+                                      int8_t* __restrict__ cscale) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nh) return;
+    float m = 0.f;
+    for (int t = 0; t < K; ++t)
+        for (int d = 0; d < nx; ++d) {
+            const float2 c = circ[((size_t)t * nh + p) * nx + d];
+            m = fmaxf(m, fmaxf(fabsf(c.x), fabsf(c.y)));
+        }
+    int e = 0;
+    if (m > 0.f) {
+        int ex;
+        frexpf(m, &ex);
         e = 13 - ex;
     }
     e = e < -100 ? -100 : (e > 100 ? 100 : e);

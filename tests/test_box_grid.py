@@ -77,20 +77,23 @@ def test_box_grid_receptor_and_correlation_grids(dims):
     assert err <= REL * np.abs(ref).max(), (err, np.abs(ref).max())
 
 
+@pytest.mark.parametrize("mode", ["fft", "tensor"])
 @pytest.mark.parametrize("dims,term_set", [((90, 96, 100), O.TERMS_SHAPE), ((84, 90, 78), O.TERMS_SHAPE_ACE),
-                                           ((100, 100, 100), O.TERMS_SHAPE), ((88, 104, 91), O.TERMS_SHAPE)])
-def test_box_grid_peaks_vs_live_oracle(dims, term_set):
+                                           ((100, 100, 100), O.TERMS_SHAPE), ((88, 104, 91), O.TERMS_SHAPE),
+                                           ((126, 112, 120), O.TERMS_SHAPE_ACE)])
+def test_box_grid_peaks_vs_live_oracle(dims, term_set, mode):
     """Peaks of uneven grids at the sizes findBestSize returns (including
     factors 11 and 13, 88 = 8 x 11, 104 = 8 x 13, 91 = 7 x 13) and of a cubic
-    edge without compiled plans, against the live FP64 oracle."""
+    edge without compiled plans, against the live FP64 oracle, through both
+    pencil-stage forms."""
     from proddl2_gb300 import synth
     pair = synth.make_pair(1500, 400, 3, seed=81 + dims[2])
     geom, rg, w = _oracle(dims, term_set, pair.ace, pair.receptor.xyz, pair.receptor.ace_type, pair.ligand.ace_type)
     rs = O.receptor_spectra(rg, workers=8)
-    with _ctx(dims, term_set, pair.ace) as s:
+    with _ctx(dims, term_set, pair.ace, pencil_mode=mode) as s:
         s.set_receptor(pair.receptor.xyz, pair.receptor.ace_type)
         s.set_ligand(pair.ligand.xyz, pair.ligand.ace_type)
-        assert s.info()["pencil_path"] == "fft"
+        assert s.info()["pencil_path"] == mode
         res = s.scan(pair.rotations)
         cand = s.candidates(pair.rotations)
     assert np.all(res.n_peaks == 4)

@@ -441,21 +441,28 @@ __global__ void __launch_bounds__(32 * kBoxWarps, 2) box_pencil_kernel(
 // warp 0 merges them into the plane's pool.
 // ---------------------------------------------------------------------------
 // QUAD: input = the tensor pencil stage's x-quads [B][nxp / 4][nh][4]
+// plh (plh.n = nz / 2 for even nz, else 0): each row's real inverse
+// transform as one nz/2-point complex transform of the Hermitian-folded half
+// spectrum, Y[k] = A + i w^k B with A = X[k] + conj(X[nz/2 - k]),
+// B = X[k] - conj(X[nz/2 - k]), w = e^{2 pi i / nz}: output m holds the real
+// values of z = 2m and 2m + 1.
 template <bool DBG, bool QUAD>
 __global__ void __launch_bounds__(32 * kBoxWarps, 2) box_plane_kernel(const float2* __restrict__ g2,
                                                                   const float2* __restrict__ twy_g,
                                                                   const float2* __restrict__ twz_g, BoxPlan ply,
-                                                                  BoxPlan plz, int nx, int pp,
+                                                                  BoxPlan plz, BoxPlan plh, int nx, int pp,
                                                                   float* __restrict__ cand_v,
                                                                   int32_t* __restrict__ cand_i,
                                                                   float* __restrict__ dbg, int nxp) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ny = ply.n, nz = plz.n, hz = nz / 2 + 1;
     const int lmax = ny > nz ? ny : nz;
+    const int ns = plh.n;
     float2* plane = reinterpret_cast<float2*>(smem_raw);  // [Ny][Hz]
     float2* twy = plane + (size_t)ny * hz;                // [ny]
     float2* twz = twy + ny;                               // [nz]
-    float2* wbuf = twz + nz;                              // [8][2][lmax]
+    float2* twh = twz + nz;                               // [nz / 2]: e^{-2 pi i m / (nz / 2)}
+    float2* wbuf = twh + nz / 2;                          // [8][2][lmax]
     __shared__ float lv_s[kBoxWarps * KC];
     __shared__ int li_s[kBoxWarps * KC];
 
@@ -463,6 +470,7 @@ __global__ void __launch_bounds__(32 * kBoxWarps, 2) box_plane_kernel(const floa
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     for (int i = tid; i < ny; i += blockDim.x) twy[i] = twy_g[i];
     for (int i = tid; i < nz; i += blockDim.x) twz[i] = twz_g[i];
+    for (int i = tid; i < ns; i += blockDim.x) twh[i] = twz_g[2 * i];
     if constexpr (QUAD) {
         const size_t nh = (size_t)ny * hz;
         const float2* src = g2 + (size_t)q * nxp * nh + (size_t)(x >> 2) * nh * 4 + (x & 3);
@@ -486,7 +494,29 @@ __global__ void __launch_bounds__(32 * kBoxWarps, 2) box_plane_kernel(const floa
     WarpTopK tk;
     tk.init();
     const size_t row0 = (size_t)x * ny;
-    for (int y = w; y < ny; y += kBoxWarps) {
+    for (int y = w; y < ny && ns > 0; y += kBoxWarps) {
+        __syncwarp();
+        const float2* row = plane + (size_t)y * hz;
+        for (int k = lane; k < ns; k += 32) {
+            const float2 X = row[k], Xm = row[ns - k];
+            const float2 A = make_float2(X.x + Xm.x, X.y - Xm.y);
+            const float2 B = make_float2(X.x - Xm.x, X.y + Xm.y);
+            const float2 wk = twz[k];  // conj(w^k)
+            const float2 cb = make_float2(B.x * wk.x + B.y * wk.y, B.y * wk.x - B.x * wk.y);  // B w^k
+            a[k] = make_float2(A.x - cb.y, A.y + cb.x);
+        }
+        const float2* o = warp_fft<float2, +1>(a, b, twh, plh, lane);
+        for (int z0 = 0; z0 < nz; z0 += 32) {
+            const int z = z0 + lane;
+            const bool ok = z < nz;
+            const float2 c = o[ok ? z >> 1 : 0];
+            const float v = ok ? ((z & 1) ? c.y : c.x) : INFINITY;
+            const int idx = ok ? (int)((row0 + y) * nz + z) : 0x7fffffff;
+            if (DBG && ok) dbg[(size_t)q * nx * ny * nz + (size_t)idx] = v;
+            tk.offer(v, idx, lane);
+        }
+    }
+    for (int y = w; y < ny && ns == 0; y += kBoxWarps) {
         __syncwarp();
         const float2* row = plane + (size_t)y * hz;
         for (int k = lane; k < nz; k += 32) {
@@ -637,7 +667,7 @@ size_t pencil_smem_bytes(int nx, int ny, int nz, int K, int n_ent, bool weighted
 }
 size_t plane_smem_bytes(int ny, int nz) {
     const int hz = nz / 2 + 1, lmax = std::max(ny, nz);
-    return ((size_t)ny * hz + ny + nz + (size_t)kBoxWarps * 2 * lmax) * sizeof(float2);
+    return ((size_t)ny * hz + ny + nz + nz / 2 + (size_t)kBoxWarps * 2 * lmax) * sizeof(float2);
 }
 size_t prep_smem_bytes(int nx, int K, int n_ent) {
     return ((size_t)K * nx + 1) * sizeof(int32_t) + (size_t)n_ent * sizeof(uint32_t);
@@ -665,8 +695,11 @@ cudaError_t box_plane(dim3 grid, size_t sm, const float2* src, const float2* twy
                       const BoxPlan& pz, int nx, const BatchArgs& a, float* dbg, int nxp, cudaStream_t s) {
     cudaError_t e = set_smem((const void*)box_plane_kernel<DBG, QUAD>, sm);
     if (e != cudaSuccess) return e;
-    box_plane_kernel<DBG, QUAD><<<grid, 32 * kBoxWarps, sm, s>>>(src, twy, twz, py, pz, nx, a.PP, a.cand_v, a.cand_i,
-                                                                dbg, nxp);
+    // even nz: rows through the half-length transform
+    BoxPlan ph{};
+    if (pz.n % 2 == 0 && !factor_plan(pz.n / 2, ph)) ph = BoxPlan{};
+    box_plane_kernel<DBG, QUAD><<<grid, 32 * kBoxWarps, sm, s>>>(src, twy, twz, py, pz, ph, nx, a.PP, a.cand_v,
+                                                                a.cand_i, dbg, nxp);
     return cudaGetLastError();
 }
 

@@ -139,16 +139,18 @@ typedef struct fftdock_config {
     int32_t lj_mix;              /* LJ term sets: sigma combination rule (PotentialsT::LJ_MIX_0 = 0:
                                     arithmetic, LJ_MIX_1 = 1: geometric; ljComp requires 1) */
     double lj_cut;               /* LJ term sets: field cutoff ("cutOffFft"), grid length units */
-    int32_t tc_terms_per_sum;    /* tensor pencil stage: terms accumulated in tensor memory before each
-                                    group's sum is added into the FP32 result (round to nearest); the
-                                    tensor core's own accumulation error grows with this chain length.
+    int32_t tc_terms_per_sum;    /* tensor pencil stage: the terms are split into ceil(K / this) groups
+                                    of equal size, each accumulated in a fresh tensor-memory sum, and the
+                                    groups' sums are added in FP32 (round to nearest); the tensor core's
+                                    own accumulation error grows with the group size.
                                     0 = the library default (FFTDOCK_TC_TERMS_PER_SUM_DEFAULT) */
     int32_t grid_nx, grid_ny, grid_nz; /* FFT sizes per axis (the reference's fftSize, each axis from
                                     findBestSize over the padded receptor box, docking_fft.hpp:541-553);
                                     all 0 = grid_n on every axis.  A cubic size with compiled plans
                                     (fftdock_supported_grid) runs the cubic kernels; any other sizes,
                                     each in [8, 256] with no prime factor above 13, run the box-grid
-                                    kernels (FFT pencil stage, up to 16 peaks per rotation, FP32 spectra,
+                                    kernels (the tensor pencil stage for Nx <= 128, else the FFT form; up to
+                                    16 peaks per rotation, FP32 spectra,
                                     no clustering, no pair graph, no no-allocation scan) */
 } fftdock_config;
 #define FFTDOCK_TC_TERMS_PER_SUM_DEFAULT 6

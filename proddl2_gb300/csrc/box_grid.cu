@@ -128,8 +128,9 @@ __device__ __forceinline__ void stockham_stage(const T2* src, T2* dst, const T2*
 
 // Unnormalised DFT of the warp's line in a (n points), b a second buffer of
 // n points; returns the buffer that holds the result.  SIGN -1: forward
-// e^{-2 pi i jk/n}; +1: inverse.  Ends with __syncwarp.
-template <typename T2, int SIGN>
+// e^{-2 pi i jk/n}; +1: inverse.  Ends with __syncwarp.  MAXR < 11: the plan
+// has no factor 11 or 13 (those stages are not compiled: fewer registers).
+template <typename T2, int SIGN, int MAXR = 13>
 __device__ T2* warp_fft(T2* a, T2* b, const T2* tw, const BoxPlan& pl, int lane) {
     T2* src = a;
     T2* dst = b;
@@ -143,8 +144,12 @@ __device__ T2* warp_fft(T2* a, T2* b, const T2* tw, const BoxPlan& pl, int lane)
             case 3: stockham_stage<T2, SIGN, 3>(src, dst, tw, pl.n, ns, lane); break;
             case 5: stockham_stage<T2, SIGN, 5>(src, dst, tw, pl.n, ns, lane); break;
             case 7: stockham_stage<T2, SIGN, 7>(src, dst, tw, pl.n, ns, lane); break;
-            case 11: stockham_stage<T2, SIGN, 11>(src, dst, tw, pl.n, ns, lane); break;
-            default: stockham_stage<T2, SIGN, 13>(src, dst, tw, pl.n, ns, lane); break;
+            default:
+                if constexpr (MAXR >= 11) {
+                    if (R == 11) stockham_stage<T2, SIGN, 11>(src, dst, tw, pl.n, ns, lane);
+                    else stockham_stage<T2, SIGN, 13>(src, dst, tw, pl.n, ns, lane);
+                }
+                break;
         }
         __syncwarp();
         T2* t = src;
@@ -446,8 +451,9 @@ __global__ void __launch_bounds__(32 * kBoxWarps, 2) box_pencil_kernel(
 // spectrum, Y[k] = A + i w^k B with A = X[k] + conj(X[nz/2 - k]),
 // B = X[k] - conj(X[nz/2 - k]), w = e^{2 pi i / nz}: output m holds the real
 // values of z = 2m and 2m + 1.
-template <bool DBG, bool QUAD>
-__global__ void __launch_bounds__(32 * kBoxWarps, 2) box_plane_kernel(const float2* __restrict__ g2,
+// PW warps; MAXR: the largest radix of the y and z plans (7: none of 11, 13)
+template <bool DBG, bool QUAD, int PW, int MAXR>
+__global__ void __launch_bounds__(32 * PW, 2) box_plane_kernel(const float2* __restrict__ g2,
                                                                   const float2* __restrict__ twy_g,
                                                                   const float2* __restrict__ twz_g, BoxPlan ply,
                                                                   BoxPlan plz, BoxPlan plh, int nx, int pp,
@@ -463,8 +469,8 @@ __global__ void __launch_bounds__(32 * kBoxWarps, 2) box_plane_kernel(const floa
     float2* twz = twy + ny;                               // [nz]
     float2* twh = twz + nz;                               // [nz / 2]: e^{-2 pi i m / (nz / 2)}
     float2* wbuf = twh + nz / 2;                          // [8][2][lmax]
-    __shared__ float lv_s[kBoxWarps * KC];
-    __shared__ int li_s[kBoxWarps * KC];
+    __shared__ float lv_s[PW * KC];
+    __shared__ int li_s[PW * KC];
 
     const int x = blockIdx.x, q = blockIdx.y;
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
@@ -483,10 +489,10 @@ __global__ void __launch_bounds__(32 * kBoxWarps, 2) box_plane_kernel(const floa
     float2* a = wbuf + (size_t)w * 2 * lmax;
     float2* b = a + lmax;
     // columns kz: inverse transform along ky
-    for (int kz = w; kz < hz; kz += kBoxWarps) {
+    for (int kz = w; kz < hz; kz += PW) {
         __syncwarp();
         for (int k = lane; k < ny; k += 32) a[k] = plane[k * hz + kz];
-        const float2* o = warp_fft<float2, +1>(a, b, twy, ply, lane);
+        const float2* o = warp_fft<float2, +1, MAXR>(a, b, twy, ply, lane);
         for (int y = lane; y < ny; y += 32) plane[y * hz + kz] = o[y];
     }
     __syncthreads();
@@ -494,7 +500,7 @@ __global__ void __launch_bounds__(32 * kBoxWarps, 2) box_plane_kernel(const floa
     WarpTopK tk;
     tk.init();
     const size_t row0 = (size_t)x * ny;
-    for (int y = w; y < ny && ns > 0; y += kBoxWarps) {
+    for (int y = w; y < ny && ns > 0; y += PW) {
         __syncwarp();
         const float2* row = plane + (size_t)y * hz;
         for (int k = lane; k < ns; k += 32) {
@@ -505,7 +511,7 @@ __global__ void __launch_bounds__(32 * kBoxWarps, 2) box_plane_kernel(const floa
             const float2 cb = make_float2(B.x * wk.x + B.y * wk.y, B.y * wk.x - B.x * wk.y);  // B w^k
             a[k] = make_float2(A.x - cb.y, A.y + cb.x);
         }
-        const float2* o = warp_fft<float2, +1>(a, b, twh, plh, lane);
+        const float2* o = warp_fft<float2, +1, MAXR>(a, b, twh, plh, lane);
         for (int z0 = 0; z0 < nz; z0 += 32) {
             const int z = z0 + lane;
             const bool ok = z < nz;
@@ -516,7 +522,7 @@ __global__ void __launch_bounds__(32 * kBoxWarps, 2) box_plane_kernel(const floa
             tk.offer(v, idx, lane);
         }
     }
-    for (int y = w; y < ny && ns == 0; y += kBoxWarps) {
+    for (int y = w; y < ny && ns == 0; y += PW) {
         __syncwarp();
         const float2* row = plane + (size_t)y * hz;
         for (int k = lane; k < nz; k += 32) {
@@ -527,7 +533,7 @@ __global__ void __launch_bounds__(32 * kBoxWarps, 2) box_plane_kernel(const floa
                 a[k] = make_float2(c.x, -c.y);
             }
         }
-        const float2* o = warp_fft<float2, +1>(a, b, twz, plz, lane);
+        const float2* o = warp_fft<float2, +1, MAXR>(a, b, twz, plz, lane);
         for (int z0 = 0; z0 < nz; z0 += 32) {
             const int z = z0 + lane;
             const bool ok = z < nz;
@@ -543,7 +549,7 @@ __global__ void __launch_bounds__(32 * kBoxWarps, 2) box_plane_kernel(const floa
     }
     __syncthreads();
     if (w == 0) {
-        merge_lists(lv_s, li_s, kBoxWarps * KC, tk, lane);
+        merge_lists(lv_s, li_s, PW * KC, tk, lane);
         if (lane < KC) {
             cand_v[((size_t)q * nx + x) * KC + lane] = tk.lv;
             cand_i[((size_t)q * nx + x) * KC + lane] = tk.li;
@@ -667,7 +673,8 @@ size_t pencil_smem_bytes(int nx, int ny, int nz, int K, int n_ent, bool weighted
 }
 size_t plane_smem_bytes(int ny, int nz) {
     const int hz = nz / 2 + 1, lmax = std::max(ny, nz);
-    return ((size_t)ny * hz + ny + nz + nz / 2 + (size_t)kBoxWarps * 2 * lmax) * sizeof(float2);
+    // up to 16 warps (plans without factors 11 and 13)
+    return ((size_t)ny * hz + ny + nz + nz / 2 + (size_t)16 * 2 * lmax) * sizeof(float2);
 }
 size_t prep_smem_bytes(int nx, int K, int n_ent) {
     return ((size_t)K * nx + 1) * sizeof(int32_t) + (size_t)n_ent * sizeof(uint32_t);
@@ -690,17 +697,34 @@ cudaError_t box_prep(const BatchArgs& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+bool big_radix(const BoxPlan& pl) {
+    for (int i = 0; i < pl.nf; ++i)
+        if (pl.f[i] > 7) return true;
+    return false;
+}
+
+template <bool DBG, bool QUAD, int PW, int MAXR>
+cudaError_t box_plane_launch(dim3 grid, size_t sm, const float2* src, const float2* twy, const float2* twz,
+                             const BoxPlan& py, const BoxPlan& pz, const BoxPlan& ph, int nx, const BatchArgs& a,
+                             float* dbg, int nxp, cudaStream_t s) {
+    cudaError_t e = set_smem((const void*)box_plane_kernel<DBG, QUAD, PW, MAXR>, sm);
+    if (e != cudaSuccess) return e;
+    box_plane_kernel<DBG, QUAD, PW, MAXR><<<grid, 32 * PW, sm, s>>>(src, twy, twz, py, pz, ph, nx, a.PP, a.cand_v,
+                                                                    a.cand_i, dbg, nxp);
+    return cudaGetLastError();
+}
+
+// plans without factors 11 and 13 run 16 warps per CTA (the smaller
+// stages fit 64 registers), others 8
 template <bool DBG, bool QUAD>
 cudaError_t box_plane(dim3 grid, size_t sm, const float2* src, const float2* twy, const float2* twz, const BoxPlan& py,
                       const BoxPlan& pz, int nx, const BatchArgs& a, float* dbg, int nxp, cudaStream_t s) {
-    cudaError_t e = set_smem((const void*)box_plane_kernel<DBG, QUAD>, sm);
-    if (e != cudaSuccess) return e;
     // even nz: rows through the half-length transform
     BoxPlan ph{};
     if (pz.n % 2 == 0 && !factor_plan(pz.n / 2, ph)) ph = BoxPlan{};
-    box_plane_kernel<DBG, QUAD><<<grid, 32 * kBoxWarps, sm, s>>>(src, twy, twz, py, pz, ph, nx, a.PP, a.cand_v,
-                                                                a.cand_i, dbg, nxp);
-    return cudaGetLastError();
+    if (big_radix(py) || big_radix(pz))
+        return box_plane_launch<DBG, QUAD, 8, 13>(grid, sm, src, twy, twz, py, pz, ph, nx, a, dbg, nxp, s);
+    return box_plane_launch<DBG, QUAD, 16, 7>(grid, sm, src, twy, twz, py, pz, ph, nx, a, dbg, nxp, s);
 }
 
 cudaError_t box_middle(const BatchArgs& a, cudaStream_t s) {
@@ -785,7 +809,7 @@ cudaError_t box_load_kernels(int) {
     cudaFuncAttributes fa;
     cudaError_t e = cudaFuncGetAttributes(&fa, (const void*)box_prep_kernel);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)box_pencil_kernel<false>);
-    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)box_plane_kernel<false, false>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)box_plane_kernel<false, false, 16, 7>);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)box_finalize_kernel);
     return e;
 }

@@ -477,13 +477,26 @@ __global__ void __launch_bounds__(32 * PW, 2) box_plane_kernel(const float2* __r
     for (int i = tid; i < ny; i += blockDim.x) twy[i] = twy_g[i];
     for (int i = tid; i < nz; i += blockDim.x) twz[i] = twz_g[i];
     for (int i = tid; i < ns; i += blockDim.x) twh[i] = twz_g[2 * i];
-    if constexpr (QUAD) {
+    {
+        // the plane's values, 8 loads in flight per thread before their stores
         const size_t nh = (size_t)ny * hz;
-        const float2* src = g2 + (size_t)q * nxp * nh + (size_t)(x >> 2) * nh * 4 + (x & 3);
-        for (int i = tid; i < ny * hz; i += blockDim.x) plane[i] = src[(size_t)i * 4];
-    } else {
-        const float2* src = g2 + ((size_t)q * nx + x) * pp;
-        for (int i = tid; i < ny * hz; i += blockDim.x) plane[i] = src[i];
+        const float2* src = QUAD ? g2 + (size_t)q * nxp * nh + (size_t)(x >> 2) * nh * 4 + (x & 3)
+                                 : g2 + ((size_t)q * nx + x) * pp;
+        const int step = QUAD ? 4 : 1;
+        const int tot = ny * hz;
+        for (int i0 = tid; i0 < tot; i0 += 8 * blockDim.x) {
+            float2 v[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int i = i0 + k * blockDim.x;
+                if (i < tot) v[k] = src[(size_t)i * step];
+            }
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int i = i0 + k * blockDim.x;
+                if (i < tot) plane[i] = v[k];
+            }
+        }
     }
     __syncthreads();
     float2* a = wbuf + (size_t)w * 2 * lmax;

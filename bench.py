@@ -79,12 +79,13 @@ def workload(name):
     return w
 
 
-def workload_desc(w):
+def workload_desc(w, dims=None):
     terms = {"shape_ace": "shape + 18 desolvation types (18 folded terms)", "shape": "shape (1 term)",
              "lj_comp": "the reference's ljComp soft-core LJ (2 terms, weighted ligand entries)",
              "lj_avg": "the reference's ljAvg soft-core LJ (1 term)"}[w["term_set"]]
-    return ("%s: receptor %d / ligand %d atoms, %d^3 at %.1f A, %s, %d rotations, %d peaks/rotation"
-            % (w["name"], w["n_rec"], w["n_lig"], w["grid_n"], w["grid_step"], terms, w["n_rot"], w["peaks"]))
+    grid = ("%d x %d x %d" % tuple(dims)) if dims else ("%d^3" % w["grid_n"])
+    return ("%s: receptor %d / ligand %d atoms, %s at %.1f A, %s, %d rotations, %d peaks/rotation"
+            % (w["name"], w["n_rec"], w["n_lig"], grid, w["grid_step"], terms, w["n_rot"], w["peaks"]))
 
 
 class ClockSampler:
@@ -519,12 +520,13 @@ def run_ours(args):
                          "rotation), scipy pocketfft" % (layouts[best]["sample"], n_fft),
                "layouts": layouts}
 
+    metric = METRIC if not dims else "rotations/s on a %d x %d x %d grid (1 GB300), exhaustive FFT scan" % dims
     out = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32",
         "data": "synthetic (seeded globules, uniform quaternion rotations)",
-        "config": {"workload": workload_desc(w), "rot_batch": batch,
+        "config": {"workload": workload_desc(w, dims), "rot_batch": batch,
                    "mode": ("exhaustive, translational clustering of a %d-cell queue per rotation (radius %g A)"
                             % (queue, args.cluster_radius)) if args.cluster else "exhaustive",
                    "parallelism": "replicas" if world == 1 else "rotation sets per rank (replicas)",

@@ -70,8 +70,12 @@ template <typename T2, int SIGN> __device__ __forceinline__ T2 tw_at(const T2* t
 // are held in registers for the whole stage, radices 2 and 4 need none.
 template <typename T2, int SIGN, int R>
 __device__ __forceinline__ void stockham_stage(const T2* src, T2* dst, const T2* tw, int n, int ns, int lane) {
+    using S = decltype(T2::x);
     const int nb = n / R;
     const int tstep = n / (ns * R);
+    // j / ns as a multiply-high by ceil(2^32 / ns) (ns > 1): exact for
+    // j < 2^32 / ns^2 (here j < 256 and ns <= 256)
+    const unsigned magic = ns > 1 ? 0xffffffffu / (unsigned)ns + 1u : 0u;
     T2 root[R];
 #pragma unroll
     for (int m = 1; m < R; ++m) root[m] = tw_at<T2, SIGN>(tw, m * nb);
@@ -79,7 +83,7 @@ __device__ __forceinline__ void stockham_stage(const T2* src, T2* dst, const T2*
         T2 v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) v[r] = src[j + r * nb];
-        const int jq = j / ns;
+        const int jq = ns > 1 ? (int)__umulhi((unsigned)j, magic) : j;
         const int jm = j - jq * ns;
         const int step = jm * tstep;
 #pragma unroll
@@ -105,22 +109,34 @@ __device__ __forceinline__ void stockham_stage(const T2* src, T2* dst, const T2*
             o.x = a.x - c.x; o.y = a.y - c.y; out[2 * ns] = o;
             o.x = b.x - d.x; o.y = b.y - d.y; out[3 * ns] = o;
         } else {
+            // odd R: pairs a_q = v_q + v_(R-q), b_q = v_q - v_(R-q); with
+            // root[m] = (cos, s sin) of the stage's direction,
+            // out_k = v0 + sum_q cos(qk) a_q + i sum_q s sin(qk) b_q and
+            // out_(R-k) the same with - i
+            constexpr int P = (R - 1) / 2;
+            T2 o0 = v[0];
 #pragma unroll
-            for (int k = 0; k < R; ++k) {
-                T2 acc = v[0];
+            for (int q = 1; q <= P; ++q) {
+                o0.x += v[q].x + v[R - q].x;
+                o0.y += v[q].y + v[R - q].y;
+            }
+            out[0] = o0;
 #pragma unroll
-                for (int r = 1; r < R; ++r) {
-                    const int m = (r * k) % R;
-                    if (m == 0) {
-                        acc.x += v[r].x;
-                        acc.y += v[r].y;
-                    } else {
-                        const T2 pr = c_mul(v[r], root[m]);
-                        acc.x += pr.x;
-                        acc.y += pr.y;
-                    }
+            for (int k = 1; k <= P; ++k) {
+                T2 re = v[0];
+                S ix = 0, iy = 0;
+#pragma unroll
+                for (int q = 1; q <= P; ++q) {
+                    const T2 w = root[(q * k) % R];
+                    re.x += w.x * (v[q].x + v[R - q].x);
+                    re.y += w.x * (v[q].y + v[R - q].y);
+                    ix += w.y * (v[q].x - v[R - q].x);
+                    iy += w.y * (v[q].y - v[R - q].y);
                 }
-                out[k * ns] = acc;
+                // i (ix + i iy) = (-iy, ix)
+                T2 o;
+                o.x = re.x - iy; o.y = re.y + ix; out[k * ns] = o;
+                o.x = re.x + iy; o.y = re.y - ix; out[(R - k) * ns] = o;
             }
         }
     }

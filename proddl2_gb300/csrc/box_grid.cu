@@ -480,8 +480,10 @@ __global__ void __launch_bounds__(32 * PW, 2) box_plane_kernel(const float2* __r
     const int ny = ply.n, nz = plz.n, hz = nz / 2 + 1;
     const int lmax = ny > nz ? ny : nz;
     const int ns = plh.n;
-    float2* plane = reinterpret_cast<float2*>(smem_raw);  // [Ny][Hz]
-    float2* twy = plane + (size_t)ny * hz;                // [ny]
+    // rows of an odd pitch: a half-warp reading a column hits 16 bank pairs
+    const int pitch = hz | 1;
+    float2* plane = reinterpret_cast<float2*>(smem_raw);  // [Ny][pitch]
+    float2* twy = plane + (size_t)ny * pitch;             // [ny]
     float2* twz = twy + ny;                               // [nz]
     float2* twh = twz + nz;                               // [nz / 2]: e^{-2 pi i m / (nz / 2)}
     float2* wbuf = twh + nz / 2;                          // [8][2][lmax]
@@ -510,7 +512,7 @@ __global__ void __launch_bounds__(32 * PW, 2) box_plane_kernel(const float2* __r
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
                 const int i = i0 + k * blockDim.x;
-                if (i < tot) plane[i] = v[k];
+                if (i < tot) plane[(i / hz) * pitch + i % hz] = v[k];
             }
         }
     }
@@ -520,9 +522,9 @@ __global__ void __launch_bounds__(32 * PW, 2) box_plane_kernel(const float2* __r
     // columns kz: inverse transform along ky
     for (int kz = w; kz < hz; kz += PW) {
         __syncwarp();
-        for (int k = lane; k < ny; k += 32) a[k] = plane[k * hz + kz];
+        for (int k = lane; k < ny; k += 32) a[k] = plane[k * pitch + kz];
         const float2* o = warp_fft<float2, +1, MAXR>(a, b, twy, ply, lane);
-        for (int y = lane; y < ny; y += 32) plane[y * hz + kz] = o[y];
+        for (int y = lane; y < ny; y += 32) plane[y * pitch + kz] = o[y];
     }
     __syncthreads();
     // rows y: real inverse transform along kz, and the warp's top KC
@@ -531,7 +533,7 @@ __global__ void __launch_bounds__(32 * PW, 2) box_plane_kernel(const float2* __r
     const size_t row0 = (size_t)x * ny;
     for (int y = w; y < ny && ns > 0; y += PW) {
         __syncwarp();
-        const float2* row = plane + (size_t)y * hz;
+        const float2* row = plane + (size_t)y * pitch;
         for (int k = lane; k < ns; k += 32) {
             const float2 X = row[k], Xm = row[ns - k];
             const float2 A = make_float2(X.x + Xm.x, X.y - Xm.y);
@@ -553,7 +555,7 @@ __global__ void __launch_bounds__(32 * PW, 2) box_plane_kernel(const float2* __r
     }
     for (int y = w; y < ny && ns == 0; y += PW) {
         __syncwarp();
-        const float2* row = plane + (size_t)y * hz;
+        const float2* row = plane + (size_t)y * pitch;
         for (int k = lane; k < nz; k += 32) {
             if (k < hz) {
                 a[k] = row[k];
@@ -703,7 +705,7 @@ size_t pencil_smem_bytes(int nx, int ny, int nz, int K, int n_ent, bool weighted
 size_t plane_smem_bytes(int ny, int nz) {
     const int hz = nz / 2 + 1, lmax = std::max(ny, nz);
     // up to 16 warps (plans without factors 11 and 13)
-    return ((size_t)ny * hz + ny + nz + nz / 2 + (size_t)16 * 2 * lmax) * sizeof(float2);
+    return ((size_t)ny * (hz | 1) + ny + nz + nz / 2 + (size_t)16 * 2 * lmax) * sizeof(float2);
 }
 size_t prep_smem_bytes(int nx, int K, int n_ent) {
     return ((size_t)K * nx + 1) * sizeof(int32_t) + (size_t)n_ent * sizeof(uint32_t);

@@ -235,8 +235,11 @@ int check_pipeline(fftdock_ctx* ctx) {
     CK(cudaMemcpy(&err, ctx->err_dev, sizeof(int), cudaMemcpyDeviceToHost));
     if (err != 0) {
         cudaMemset(ctx->err_dev, 0, sizeof(int));
-        return fail(ctx, FFTDOCK_ECUDA,
-                    "tensor pencil stage timed out waiting on a pipeline barrier (code " + std::to_string(err) + ")");
+        // bits 1, 2, 4, 16: a bounded wait on a pipeline barrier ran out; 32: a
+        // CTA found no running-sum slot for its SM (an SM id at or above %nsmid)
+        const std::string what = (err & 32) && !(err & 23) ? "tensor pencil stage found no running-sum slot"
+                                                           : "tensor pencil stage timed out waiting on a pipeline barrier";
+        return fail(ctx, FFTDOCK_ECUDA, what + " (code " + std::to_string(err) + ")");
     }
     return FFTDOCK_OK;
 }

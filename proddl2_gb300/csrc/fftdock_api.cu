@@ -405,10 +405,14 @@ TcTables tc_tables(const double* xyz, const int32_t* term, int n, int K, int N, 
     long hi = (long)std::floor((rmax - zero_h) / h) + 0;
     lo = std::max(lo, 0L);
     hi = std::min(hi, (long)N - 1);
+    // a multiple of 8 cells (whole MMA chunks); on a box grid whose Nx is
+    // not one, the window may run past Nx: those rows hold no entries
+    // (the ligand's cells lie in [lo, hi]) and their circulant index wraps
+    const int n_pad8 = (N + 7) / 8 * 8;
     int W = (int)((hi - lo + 1 + 7) / 8 * 8);
-    if (W > N) W = N;
+    if (W > n_pad8) W = n_pad8;
     long x0 = lo;
-    if (x0 + W > N) x0 = N - W;
+    if (x0 + W > N) x0 = std::max(0L, (long)N - W);
     t.x0 = (int)x0;
     t.W = W;
     // rows of the transposed entries: each non-empty term's range padded to 8

@@ -172,3 +172,59 @@ def test_box_grid_out_of_grid_and_batches():
         with pytest.raises(FFTDockError) as ei:
             s.scan(pair.rotations)
         assert ei.value.code == _lib.FFTDOCK_EOUT_OF_GRID
+
+
+def test_box_grid_forms_agree_over_many_sizes():
+    """Both pencil-stage forms on 12 box grids drawn from the sizes findBestSize
+    can return (x from 10 to 128, including odd and 11/13-factor lengths), 48
+    rotations each: wherever the top-4 lists differ, every cell of either list
+    is adjudicated with its FP64 direct-space energy (each form must hold
+    every cell of the union's best four below the 4th by more than the tie
+    tolerance), and every reported score is the exact energy of its cell."""
+    from proddl2_gb300 import FFTScan, ScanConfig, synth
+    from proddl2_gb300.scan import supported_dims
+    rng = np.random.Generator(np.random.PCG64(2024))
+    sizes = [n for n in range(10, 129) if supported_dims((n, n, n))]
+    checked = 0
+    for case in range(12):
+        dims = tuple(int(v) for v in rng.choice([n for n in sizes if n >= 40], size=3))
+        dims = (int(rng.choice(sizes[:8])) if case < 2 else dims[0],) + dims[1:]
+        # molecules that fit the smallest axis (the first two grids are thin)
+        pair = synth.make_pair(600, 120, 48, seed=300 + case) if case >= 2 else \
+            synth.make_pair(150, 12, 48, seed=300 + case)
+        geom, rg, w = _oracle(dims, O.TERMS_SHAPE_ACE, pair.ace, pair.receptor.xyz, pair.receptor.ace_type,
+                              pair.ligand.ace_type)
+        res = {}
+        for mode in ("fft", "tensor"):
+            with FFTScan(ScanConfig(grid_dims=dims, grid_step=1.2, term_set="shape_ace", peaks_per_rot=4,
+                                    ace_matrix=pair.ace, pencil_mode=mode)) as s:
+                s.set_receptor(pair.receptor.xyz, pair.receptor.ace_type)
+                s.set_ligand(pair.ligand.xyz, pair.ligand.ace_type)
+                assert s.info()["pencil_path"] == mode, dims
+                res[mode] = s.scan(pair.rotations, raise_out_of_grid=False)
+        ok = (res["fft"].n_peaks == 4) & (res["tensor"].n_peaks == 4)
+        nx, ny, nz = dims
+        for i in np.nonzero(ok)[0]:
+            cells, _ = O.bin_ligand(geom, pair.rotations[i], pair.ligand.xyz)
+            lists, exact = {}, {}
+            for mode in ("fft", "tensor"):
+                cell, _, score = res[mode].rotation(i)
+                offs = [int((c[0] * ny + c[1]) * nz + c[2]) for c in cell]
+                lists[mode] = set(offs)
+                if mode == "tensor" or np.any(res["fft"].peaks["cell"][i] != res["tensor"].peaks["cell"][i]):
+                    for o, c, sc in zip(offs, cell, score):
+                        e = O.direct_score(rg, cells, w, c)
+                        assert abs(e - sc) <= 1e-9 * max(1.0, abs(e)), (dims, mode, i, sc, e)
+                        exact[o] = e
+            if lists["fft"] == lists["tensor"]:
+                checked += 1
+                continue
+            best = sorted(exact.items(), key=lambda t: (t[1], t[0]))[:4]
+            last = best[-1][1]
+            tie = REL * max(1.0, abs(last))
+            for mode in ("fft", "tensor"):
+                for o, e in best:
+                    if e < last - tie:
+                        assert o in lists[mode], (dims, mode, i, o, e, last)
+            checked += 1
+    assert checked >= 12 * 24, checked

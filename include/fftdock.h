@@ -70,8 +70,8 @@ enum {
 };
 
 /* how the per-pencil x stage (x transforms and the spectrum product summed
- * over terms) runs.  FFT: FP32 x-FFTs on the CUDA cores.  TENSOR (grid
- * edges <= 128, unweighted term sets) restates the stage as a circular
+ * over terms) runs.  FFT: FP32 x-FFTs on the CUDA cores.  TENSOR (x sizes
+ * <= 256, one or two 128-row output tiles; unweighted term sets) restates the stage as a circular
  * correlation along x computed with split-FP16 tcgen05 GEMMs (hi*hi + hi*lo
  * + lo*hi, FP32 accumulate) over ligand bins summed on the CUDA cores; the
  * scan then takes rotations in groups of 128 (rot_batch is rounded up).  The
@@ -81,9 +81,9 @@ enum {
  * FP32 candidate values stay within 1e-4 relative of FP64 (measured 8.4e-5
  * at 128^3 with 18 terms; one group of all 18 terms: 2.3e-4; FFT: 3.8e-5);
  * reported scores are FP64 direct-space energies either way.  AUTO = TENSOR
- * where it applies (grid edge <= 128, FP32 spectra, an unweighted term set
- * with at least 4 terms: at 64^3 with the single shape term the FFT form is
- * faster), else FFT; a ligand whose window exceeds the tensor stage's shared
+ * where it is the faster form (cubic edges <= 128 and box grids with Nx <=
+ * 256, FP32 spectra, an unweighted term set with at least 4 terms: at 64^3
+ * with the single shape term, and at 144^3, the FFT form is faster), else FFT; a ligand whose window exceeds the tensor stage's shared
  * memory runs the FFT form.  The no-allocation scan always runs the FFT form;
  * fftdock_scan_pairs follows the same rule per grid edge. */
 enum {
@@ -149,7 +149,7 @@ typedef struct fftdock_config {
                                     all 0 = grid_n on every axis.  A cubic size with compiled plans
                                     (fftdock_supported_grid) runs the cubic kernels; any other sizes,
                                     each in [8, 256] with no prime factor above 13, run the box-grid
-                                    kernels (the tensor pencil stage for Nx <= 128, else the FFT form; up to
+                                    kernels (the tensor pencil stage for Nx <= 256, else the FFT form; up to
                                     16 peaks per rotation, FP32 spectra,
                                     no clustering, no pair graph, no no-allocation scan) */
 } fftdock_config;

@@ -779,13 +779,20 @@ cudaError_t box_middle(const BatchArgs& a, cudaStream_t s) {
         // rotations per CTA, then the plane stage from its x-quads
         const int nxp = (nx + 3) / 4 * 4;
         const size_t smt = tc_smem_bytes_box(nx, ny, nz, a.W / 8, a.n_tc_terms);
-        if ((e = set_smem((const void*)pencil_tc_kernel<0>, smt)) != cudaSuccess) return e;
         dim3 gridt(np, (nb + TC_ROT - 1) / TC_ROT);
         const int tg = a.tc_group > 0 ? a.tc_group : FFTDOCK_TC_TERMS_PER_SUM_DEFAULT;
         const TcBox bx{nx, ny, nz, nz / 2 + 1, np, nxp, twy, twz};
-        pencil_tc_kernel<0><<<gridt, TC_THREADS, smt, s>>>(a.circ, a.cscale, a.ent_t, a.tinfo, a.n_tc_terms, nullptr,
-                                                          a.g2t, a.n_pad, nb, a.x0, a.W, tg, a.tc_slots,
-                                                          a.tc_n_slots, bx, a.err);
+        if (tc_tiles(nx) == 1) {
+            if ((e = set_smem((const void*)pencil_tc_kernel<0, 1>, smt)) != cudaSuccess) return e;
+            pencil_tc_kernel<0, 1><<<gridt, TC_THREADS, smt, s>>>(a.circ, a.cscale, a.ent_t, a.tinfo, a.n_tc_terms,
+                                                                 nullptr, a.g2t, a.n_pad, nb, a.x0, a.W, tg,
+                                                                 a.tc_slots, a.tc_n_slots, bx, a.err);
+        } else {
+            if ((e = set_smem((const void*)pencil_tc_kernel<0, 2>, smt)) != cudaSuccess) return e;
+            pencil_tc_kernel<0, 2><<<gridt, TC_THREADS, smt, s>>>(a.circ, a.cscale, a.ent_t, a.tinfo, a.n_tc_terms,
+                                                                 nullptr, a.g2t, a.n_pad, nb, a.x0, a.W, tg,
+                                                                 a.tc_slots, a.tc_n_slots, bx, a.err);
+        }
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if (a.ev && (e = cudaEventRecord(a.ev[1], s)) != cudaSuccess) return e;
         e = a.dbg_corr ? box_plane<true, true>(grid3, sm3, a.g2t, twy, twz, py, pz, nx, a, a.dbg_corr, nxp, s)
@@ -908,6 +915,8 @@ cudaError_t box_circ_scales(const float2* circ, int K, int nh, int nx, int8_t* c
 size_t box_tc_smem(const int dims[3], int n_chunks, int n_terms) {
     return tc_smem_bytes_box(dims[0], dims[1], dims[2], n_chunks, n_terms);
 }
+
+size_t cubic_tc_smem(int n, int n_chunks, int n_terms) { return tc_smem_bytes(n, n_chunks, n_terms); }
 
 const SizeOps* box_ops() {
     static const SizeOps o{0, nullptr, nullptr, false, &box_scan_batch, &box_pencil_smem_unknown, &box_prep,

@@ -40,7 +40,8 @@ template <int N> struct SizeOpsImpl {
         return cudaGetLastError();
     }
 
-    static constexpr bool kHasTc = N <= 128;
+    // the tensor pencil stage: one 128-row x tile up to 128, two up to 256
+    static constexpr bool kHasTc = N <= 256;
 
 
     static cudaError_t circ_scales(const float2* circ, int K, int8_t* cscale, cudaStream_t s) {
@@ -159,12 +160,14 @@ template <int N> struct SizeOpsImpl {
             if (a.use_tc) {
                 tc = true;
                 const size_t smt = tc_smem_bytes(N, a.W / 8, a.n_tc_terms);
-                if ((e = set_smem((const void*)pencil_tc_kernel<N>, smt)) != cudaSuccess) return e;
+                constexpr int MT = tc_tiles(N);
+                if ((e = set_smem((const void*)pencil_tc_kernel<N, MT>, smt)) != cudaSuccess) return e;
                 dim3 gridt(N * H, (nb + TC_ROT - 1) / TC_ROT);
                 const int tg = a.tc_group > 0 ? a.tc_group : FFTDOCK_TC_TERMS_PER_SUM_DEFAULT;
-                pencil_tc_kernel<N><<<gridt, TC_THREADS, smt, s>>>(a.circ, a.cscale, a.ent_t, a.tinfo,
-                                                                  a.n_tc_terms, a.tw32, a.g2t, a.n_pad, nb, a.x0,
-                                                                  a.W, tg, a.tc_slots, a.tc_n_slots, TcBox{}, a.err);
+                pencil_tc_kernel<N, MT><<<gridt, TC_THREADS, smt, s>>>(a.circ, a.cscale, a.ent_t, a.tinfo,
+                                                                      a.n_tc_terms, a.tw32, a.g2t, a.n_pad, nb, a.x0,
+                                                                      a.W, tg, a.tc_slots, a.tc_n_slots, TcBox{},
+                                                                      a.err);
                 if ((e = cudaGetLastError()) != cudaSuccess) return e;
             }
         }

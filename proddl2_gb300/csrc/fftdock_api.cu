@@ -434,7 +434,8 @@ TcTables tc_tables(const double* xyz, const int32_t* term, int n, int K, int N, 
     t.n_pad = prun;
     t.info = starts;
     t.info.insert(t.info.end(), ids.begin(), ids.end());
-    t.ok = W / 8 <= kTcMaxChunks && t.ka <= kTcMaxTerms && t.ka >= 1;
+    t.ok = W / 8 <= kTcMaxChunks && t.ka <= kTcMaxTerms && t.ka >= 1 &&
+           cubic_tc_smem(N, W / 8, t.ka) <= kMaxSmem;
     return t;
 }
 
@@ -615,9 +616,9 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
                                                        "] with no prime factor above 13");
         ctx->ops = fftdock::box_ops();
         ctx->box = true;
-        if (c.pencil_mode == FFTDOCK_PENCIL_TENSOR && dims[0] > fftdock::kTcRot)
+        if (c.pencil_mode == FFTDOCK_PENCIL_TENSOR && dims[0] > 2 * fftdock::kTcRot)
             return fail(ctx, FFTDOCK_EUNSUPPORTED,
-                        "the tensor-core pencil stage covers x sizes up to 128 (grid " + dims_s + ")");
+                        "the tensor-core pencil stage covers x sizes up to 256 (grid " + dims_s + ")");
         if (c.precision != FFTDOCK_PREC_FP32)
             return fail(ctx, FFTDOCK_EUNSUPPORTED, "box grids keep FP32 receptor spectra");
         if (c.cluster_trans || c.peaks_per_rot > fftdock::kKC)
@@ -636,16 +637,21 @@ int fftdock_create(const fftdock_config* cfg_in, fftdock_ctx** out) {
         return fail(ctx, FFTDOCK_EINVAL, "unknown pencil_mode");
     if (c.tc_terms_per_sum < 0 || c.tc_terms_per_sum > fftdock::kTcMaxTerms)
         return fail(ctx, FFTDOCK_EINVAL, "tc_terms_per_sum must be in [0, 64]");
-    // the tensor form: cubic edges up to 128, box grids with Nx up to 128
-    const bool has_tc = ctx->box ? dims[0] <= fftdock::kTcRot : ctx->ops->has_tc;
+    // the tensor form: cubic edges and box grids with Nx up to 256 (two
+    // 128-row output tiles above 128)
+    const bool has_tc = ctx->box ? dims[0] <= 2 * fftdock::kTcRot : ctx->ops->has_tc;
     if (c.pencil_mode == FFTDOCK_PENCIL_TENSOR && !has_tc)
-        return fail(ctx, FFTDOCK_EUNSUPPORTED, "the tensor-core pencil stage covers grid edges up to 128");
-    // AUTO runs the tensor form where it applies (faster at 128^3 with 18
-    // terms); the FFT form keeps the more accurate FP32 candidate values
+        return fail(ctx, FFTDOCK_EUNSUPPORTED, "the tensor-core pencil stage covers grid edges up to 256");
+    // AUTO runs the tensor form where it is the faster one with many terms:
+    // cubic edges up to 128 (one 128-row x tile; at 144 the second tile is
+    // 7/8 empty and the FFT form wins) and every box grid it covers (the box
+    // FFT pencil kernel is the generic runtime-radix one).  The FFT form
+    // keeps the more accurate FP32 candidate values.
     const bool lj_set = c.term_set == FFTDOCK_TERMS_LJ_COMP || c.term_set == FFTDOCK_TERMS_LJ_AVG;
     const int k_terms = c.term_set == FFTDOCK_TERMS_SHAPE_ACE ? c.n_types : 1;
+    const bool tc_faster = ctx->box || dims[0] <= fftdock::kTcRot;
     ctx->use_tc = c.pencil_mode == FFTDOCK_PENCIL_TENSOR ||
-                  (c.pencil_mode == FFTDOCK_PENCIL_AUTO && has_tc && !lj_set &&
+                  (c.pencil_mode == FFTDOCK_PENCIL_AUTO && has_tc && tc_faster && !lj_set &&
                    c.precision == FFTDOCK_PREC_FP32 && k_terms >= fftdock::kTcMinTerms);
     if (!(c.shape_core_radius >= 0.0) || !(c.shape_surface_width >= 0.0))
         return fail(ctx, FFTDOCK_EINVAL, "shape radii must be >= 0");

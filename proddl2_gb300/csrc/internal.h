@@ -112,7 +112,7 @@ cudaError_t build_receptor_grids(const ReceptorGridArgs& a, cudaStream_t s);
 // tensor pencil stage: rotations per CTA (the MMA's N), largest window in
 // 8-cell chunks, most non-empty terms
 constexpr int kTcRot = 128;
-constexpr int kTcMaxChunks = 16;  // the whole x range at N = 128
+constexpr int kTcMaxChunks = 32;  // the whole x range at N = 256 (two 128-row output tiles)
 constexpr int kTcMaxTerms = 64;
 
 constexpr int kWideMax = 16384;
@@ -286,8 +286,10 @@ cudaError_t box_receptor_fft(const double* rgrid_t, double2* cbuf, double2* hbuf
                              const int dims[3], void* spec_t, int PP, float2* circ_t, cudaStream_t s);
 // per-pencil scale exponents of the box grid's circulant samples
 cudaError_t box_circ_scales(const float2* circ, int K, int nh, int nx, int8_t* cscale, cudaStream_t s);
-// dynamic shared memory of the tensor pencil stage on a box grid
+// dynamic shared memory of the tensor pencil stage on a box grid, and on a
+// cubic grid of edge n
 size_t box_tc_smem(const int dims[3], int n_chunks, int n_terms);
+size_t cubic_tc_smem(int n, int n_chunks, int n_terms);
 
 // Read-only view of a ready context's scan inputs (receptor spectra and
 // grids, ligand, geometry); the work pointers of `args` are the context's own.

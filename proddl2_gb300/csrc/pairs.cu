@@ -536,7 +536,9 @@ int setup_sizes(Run& r, int n_pairs, const fftdock_pair* pairs) {
         sd.center0 = zero + h / 2.0;
         sd.ops = fftdock::size_ops(N);
         sd.batch = r.cfg.rot_batch;
-        sd.tc = r.tc && sd.ops->has_tc;
+        // AUTO keeps the FFT form above 128 (the tensor form's second x tile
+        // is mostly empty there); TENSOR asks for it wherever it is built
+        sd.tc = r.tc && sd.ops->has_tc && (r.cfg.pencil_mode == FFTDOCK_PENCIL_TENSOR || N <= fftdock::kTcRot);
         // the tensor form takes rotations in groups of 128
         if (sd.tc) sd.batch = (sd.batch + fftdock::kTcRot - 1) / fftdock::kTcRot * fftdock::kTcRot;
         std::vector<float2> t32(N);

@@ -117,12 +117,15 @@ __device__ __forceinline__ float2 ld_relaxed_f2(const float2* p) {
     return v;
 }
 
-// 8-row groups of the extended circulant tile E for a window of 8 n_chunks cells
-__host__ __device__ constexpr int tc_ext_groups(int n_chunks) { return 15 + n_chunks; }
+// 8-row groups of the extended circulant tile E for a window of 8 n_chunks
+// cells and mt 128-row output tiles
+__host__ __device__ constexpr int tc_ext_groups(int n_chunks, int mt = 1) { return 16 * mt - 1 + n_chunks; }
+// output tiles of 128 x rows for an x extent of n cells (n <= 256)
+__host__ __device__ constexpr int tc_tiles(int n) { return n > 128 ? 2 : 1; }
 
-// Box grids (pencil_tc_kernel<0>): sizes per axis, nx <= 128 (one 128-row
-// tile), pencil p = ky hz + kz of nh = ny hz pencils, x-quads over nxp = nx
-// rounded up to 4, and the FP32 twiddle tables of the y and z axes
+// Box grids (pencil_tc_kernel<0, MT>): sizes per axis, nx <= 128 MT, pencil
+// p = ky hz + kz of nh = ny hz pencils, x-quads over nxp = nx rounded up to
+// 4, and the FP32 twiddle tables of the y and z axes
 // (e^{-2 pi i m / n}).  The phase of an entry is the product of its y and z
 // phases, from two tables per CTA (its pencil's ky and kz).
 struct TcBox {
@@ -136,15 +139,16 @@ struct TcBox {
 // float2, staged samples [N], side slots [128] float2, term table; at least
 // 76 KB so that no more than two CTAs (2 x 256 TMEM columns) share an SM
 __host__ __device__ inline size_t tc_smem_bytes(int N, int n_chunks, int n_terms) {
-    size_t b = (size_t)n_chunks * TC_FCHUNK + 1024 + (size_t)4 * tc_ext_groups(n_chunks) * 256 + (size_t)N * 32 * 8 +
-               (size_t)N * sizeof(TcPair) + (size_t)TC_ROT * 8 + (size_t)(2 * n_terms + 1) * 4;
+    const int mt = tc_tiles(N);
+    size_t b = (size_t)n_chunks * TC_FCHUNK + 1024 + (size_t)4 * tc_ext_groups(n_chunks, mt) * 256 +
+               (size_t)N * 32 * 8 + (size_t)N * sizeof(TcPair) + (size_t)TC_ROT * 8 + (size_t)(2 * n_terms + 1) * 4;
     b = (b + 15) & ~(size_t)15;
     return b < 76 * 1024 ? 76 * 1024 : b;
 }
 // box grids: the y and z phase tables per half-warp lane ([n][16] float2)
 // in place of the [N][32] table
 __host__ __device__ inline size_t tc_smem_bytes_box(int nx, int ny, int nz, int n_chunks, int n_terms) {
-    size_t b = (size_t)n_chunks * TC_FCHUNK + 1024 + (size_t)4 * tc_ext_groups(n_chunks) * 256 +
+    size_t b = (size_t)n_chunks * TC_FCHUNK + 1024 + (size_t)4 * tc_ext_groups(n_chunks, tc_tiles(nx)) * 256 +
                (size_t)(ny + nz) * 16 * 8 + (size_t)nx * sizeof(TcPair) + (size_t)TC_ROT * 8 +
                (size_t)(2 * n_terms + 1) * 4;
     b = (b + 15) & ~(size_t)15;
@@ -234,20 +238,24 @@ __device__ __forceinline__ void tc_walk(const uint4* eq, int nblk, uint32_t kyz,
 // tinfo: [0, Ka] padded entry starts (multiples of 8) of the Ka non-empty
 // terms, [Ka + 1, 2 Ka] their term ids; n_pad = entry rows per rotation group.
 // N = 0: a box grid of the sizes in bx (every N-dependent length below is
-// then bx's runtime value).
-template <int N>
-__global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
+// then bx's runtime value).  MT output tiles of 128 x rows: MT = 2 (x extent
+// up to 256) doubles the MMAs of a chunk (the second tile's circulant rows
+// start 16 8-row groups further into E) and takes 512 TMEM columns, one CTA
+// per SM.
+template <int N, int MT>
+__global__ void __launch_bounds__(TC_THREADS, MT == 1 ? 2 : 1) pencil_tc_kernel(
     const float2* __restrict__ circ, const int8_t* __restrict__ cscale, const uint32_t* __restrict__ ent_t,
     const int32_t* __restrict__ tinfo, int Ka, const float2* __restrict__ tw, float2* __restrict__ g2t, int n_pad,
     int n_rot, int x0, int W, int tg, float2* __restrict__ slots, int n_slots, TcBox bx, int* __restrict__ err) {
-    static_assert(N <= 128, "the tensor pencil stage covers x in one 128-row tile");
+    static_assert(N <= 128 * MT && (MT == 1 || MT == 2), "the tensor pencil stage covers x in MT 128-row tiles");
     constexpr bool BOX = N == 0;
+    constexpr uint32_t TM_COLS = 256u * MT;
     const int nx = BOX ? bx.nx : N;                  // x extent (correlation length)
     const int H = BOX ? bx.hz : N / 2 + 1;           // kz per ky
     const int NH = BOX ? bx.nh : N * (N / 2 + 1);    // pencils
     const int NXP = BOX ? bx.nxp : N;                // x extent of the x-quads
     const int NC = W >> 3;
-    const int RG = tc_ext_groups(NC);
+    const int RG = tc_ext_groups(NC, MT);
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* fbuf = smem_raw;                                            // [NC][hi | lo]
     unsigned char* abuf = fbuf + NC * TC_FCHUNK + 1024;                        // [4][RG][256] after the dummy row
@@ -291,7 +299,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
     }
     for (int i = tid; i <= 2 * Ka; i += blockDim.x) tinf[i] = tinfo[i];
     if (warp == 0) {
-        tc::tmem_alloc(&tmem_base, 256);
+        tc::tmem_alloc(&tmem_base, TM_COLS);
         tc::tmem_relinquish();
     }
     if (tid == 0) {
@@ -316,23 +324,26 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
     // commit that arrives on empty_bar once they have read the tiles
     const uint32_t idesc = tc::idesc_f16_f32(128, TC_ROT);
     auto issue_term = [&](int k) {
-        const uint32_t d_re = tmem, d_im = tmem + TC_ROT;
         for (int c = 0; c < NC; ++c) {
-            const uint32_t ao = (uint32_t)(NC - 1 - c) * TC_SBO;
-            const uint64_t cre_h = tc::smem_desc(ab + 0 * RG * 256 + ao, TC_LBO, TC_SBO);
-            const uint64_t cre_l = tc::smem_desc(ab + 1 * RG * 256 + ao, TC_LBO, TC_SBO);
-            const uint64_t cim_h = tc::smem_desc(ab + 2 * RG * 256 + ao, TC_LBO, TC_SBO);
-            const uint64_t cim_l = tc::smem_desc(ab + 3 * RG * 256 + ao, TC_LBO, TC_SBO);
             const uint64_t f_h = tc::smem_desc(fb + c * TC_FCHUNK, TC_LBO, TC_SBO);
             const uint64_t f_l = tc::smem_desc(fb + c * TC_FCHUNK + TC_FTILE, TC_LBO, TC_SBO);
             // each group of terms starts a fresh accumulator
             const uint32_t acc = (starts_group(k) && c == 0) ? 0u : 1u;
-            tc::mma_f16(d_re, cre_h, f_h, idesc, acc);
-            tc::mma_f16(d_re, cre_h, f_l, idesc, 1u);
-            tc::mma_f16(d_re, cre_l, f_h, idesc, 1u);
-            tc::mma_f16(d_im, cim_h, f_h, idesc, acc);
-            tc::mma_f16(d_im, cim_h, f_l, idesc, 1u);
-            tc::mma_f16(d_im, cim_l, f_h, idesc, 1u);
+#pragma unroll
+            for (int mt = 0; mt < MT; ++mt) {
+                const uint32_t d_re = tmem + 256u * mt, d_im = d_re + TC_ROT;
+                const uint32_t ao = (uint32_t)(NC - 1 - c + 16 * mt) * TC_SBO;
+                const uint64_t cre_h = tc::smem_desc(ab + 0 * RG * 256 + ao, TC_LBO, TC_SBO);
+                const uint64_t cre_l = tc::smem_desc(ab + 1 * RG * 256 + ao, TC_LBO, TC_SBO);
+                const uint64_t cim_h = tc::smem_desc(ab + 2 * RG * 256 + ao, TC_LBO, TC_SBO);
+                const uint64_t cim_l = tc::smem_desc(ab + 3 * RG * 256 + ao, TC_LBO, TC_SBO);
+                tc::mma_f16(d_re, cre_h, f_h, idesc, acc);
+                tc::mma_f16(d_re, cre_h, f_l, idesc, 1u);
+                tc::mma_f16(d_re, cre_l, f_h, idesc, 1u);
+                tc::mma_f16(d_im, cim_h, f_h, idesc, acc);
+                tc::mma_f16(d_im, cim_h, f_l, idesc, 1u);
+                tc::mma_f16(d_im, cim_l, f_h, idesc, 1u);
+            }
         }
         tc::mma_commit(&empty_bar);
     };
@@ -348,8 +359,10 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
     // is fixed ((S1 + S2) + S3 ...) and the result the same in every run.
     uint32_t smid;
     asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
-    const int slot = (int)smid * 2 + (int)((tmem >> 8) & 1u);  // 256-column allocations start at column 0 or 256
-    const bool slot_ok = slot < n_slots;
+    // 256-column allocations start at column 0 or 256 (two CTAs per SM);
+    // with two tiles the CTA holds all 512 columns and both of the SM's slots
+    const int slot = MT == 1 ? (int)smid * 2 + (int)((tmem >> 8) & 1u) : (int)smid * 2;
+    const bool slot_ok = slot + MT - 1 < n_slots;
     if (ng > 1 && !slot_ok && tid == 0) {
         atomicOr(err, 32);
         abort_flag = 1;
@@ -361,17 +374,19 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
     auto drain_group = [&](bool first) {
         if (!slot_ok) return;
 #pragma unroll 1
-        for (int cb = 0; cb < 4; ++cb) {
-            const int c0 = half * 64 + cb * 16;
+        for (int cb = 0; cb < 4 * MT; ++cb) {
+            const int mt = cb >> 2;  // tile: its own slot and 256 TMEM columns
+            const int c0 = half * 64 + (cb & 3) * 16;
+            float2* const st = sb + (size_t)mt * (TC_ROT * 128);
             uint32_t dre[16], dim[16];
-            tc::tmem_ld_32x32b_x16(tmem + trow + c0, dre);
-            tc::tmem_ld_32x32b_x16(tmem + trow + TC_ROT + c0, dim);
+            tc::tmem_ld_32x32b_x16(tmem + 256u * mt + trow + c0, dre);
+            tc::tmem_ld_32x32b_x16(tmem + 256u * mt + trow + TC_ROT + c0, dim);
             tc::tmem_wait_ld();
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
                 const float2 v = make_float2(__uint_as_float(dre[j]), __uint_as_float(dim[j]));
-                if (first) st_relaxed_f2(sb + (size_t)(c0 + j) * 128, v);
-                else atomicAdd(sb + (size_t)(c0 + j) * 128, v);
+                if (first) st_relaxed_f2(st + (size_t)(c0 + j) * 128, v);
+                else atomicAdd(st + (size_t)(c0 + j) * 128, v);
             }
         }
     };
@@ -381,20 +396,24 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
     // before the wait for the last MMAs.
     const float inv = 1.0f / (c_scale * TC_F_SCALE);
     const bool with_sum = ng > 1 && slot_ok;
+    // block cb: tile cb / 8, rotations half * 64 + (cb % 8) * 8 ..
     auto load_run = [&](int cb, float2 (&run)[8]) {
-        const int c0 = half * 64 + cb * 8;
+        const int c0 = half * 64 + (cb & 7) * 8;
+        const float2* st = sb + (size_t)(cb >> 3) * (TC_ROT * 128);
 #pragma unroll
-        for (int j = 0; j < 8; ++j) run[j] = ld_relaxed_f2(sb + (size_t)(c0 + j) * 128);
+        for (int j = 0; j < 8; ++j) run[j] = ld_relaxed_f2(st + (size_t)(c0 + j) * 128);
     };
     auto out_block = [&](int cb, const float2 (&run)[8]) {
-        const int c0 = half * 64 + cb * 8;
+        const int mt = cb >> 3;
+        const int c0 = half * 64 + (cb & 7) * 8;
+        const int x = 128 * mt + xo;  // output row
         uint32_t dre[8], dim[8];
-        tc::tmem_ld_32x32b_x8(tmem + trow + c0, dre);
-        tc::tmem_ld_32x32b_x8(tmem + trow + TC_ROT + c0, dim);
+        tc::tmem_ld_32x32b_x8(tmem + 256u * mt + trow + c0, dre);
+        tc::tmem_ld_32x32b_x8(tmem + 256u * mt + trow + TC_ROT + c0, dim);
         tc::tmem_wait_ld();
-        if (xo < nx) {
-            float2* ob = g2t + (size_t)(g * TC_ROT + c0) * NH * NXP + (size_t)(xo >> 2) * NH * 4 + (size_t)p * 4 +
-                         (xo & 3);
+        if (x < nx) {
+            float2* ob = g2t + (size_t)(g * TC_ROT + c0) * NH * NXP + (size_t)(x >> 2) * NH * 4 + (size_t)p * 4 +
+                         (x & 3);
             const int nj = min(8, n_rot - (g * TC_ROT + c0));
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
@@ -553,10 +572,10 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
         }
         tc::fence_after_sync();
 #pragma unroll 1
-        for (int cb = 0; cb < 8; cb += 2) {
+        for (int cb = 0; cb < 8 * MT; cb += 2) {
             if (with_sum) load_run(cb + 1, run_b);
             out_block(cb, run_a);
-            if (with_sum && cb + 2 < 8) load_run(cb + 2, run_a);
+            if (with_sum && cb + 2 < 8 * MT) load_run(cb + 2, run_a);
             out_block(cb + 1, run_b);
         }
     }
@@ -564,7 +583,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pencil_tc_kernel(
     if (tid == 0 && !tc::mbar_wait(&done_bar, 0, TC_WAIT_NS)) atomicOr(err, 16);
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, 256);
+    if (warp == 0) tc::tmem_dealloc(tmem, TM_COLS);
 }
 
 // per-pencil power-of-two exponent so that the largest circulant component

@@ -107,7 +107,7 @@ def test_create_rejects_bad_config(built_lib):
     bad = [
         (dict(grid_n=97), _lib.FFTDOCK_EUNSUPPORTED),           # prime: no FFT plan
         (dict(grid_n=300), _lib.FFTDOCK_EUNSUPPORTED),          # beyond the box-grid sizes
-        (dict(grid_dims=(150, 96, 100), pencil_mode="tensor"), _lib.FFTDOCK_EUNSUPPORTED),  # x beyond 128
+        (dict(grid_dims=(90, 96, 100), precision="bf16"), _lib.FFTDOCK_EUNSUPPORTED),  # box grids keep FP32
         (dict(grid_dims=(90, 96, 100), cluster_trans=True), _lib.FFTDOCK_EUNSUPPORTED),
         (dict(grid_dims=(90, 96, 100), peaks_per_rot=17), _lib.FFTDOCK_EUNSUPPORTED),
         (dict(grid_dims=(90, 96, 102)), _lib.FFTDOCK_EUNSUPPORTED),  # 102 = 2 * 3 * 17

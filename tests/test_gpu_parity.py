@@ -531,3 +531,83 @@ def test_receptor_setup_is_bit_reproducible():
             outs.append((s.receptor_grid(3), s.scan(pair.rotations)))
     assert np.array_equal(outs[0][0], outs[1][0])
     assert np.array_equal(outs[0][1].peaks, outs[1][1].peaks)
+
+
+@pytest.mark.parametrize("terms_per_sum", [1, 2, 5, 7, 18])
+def test_tensor_groups_of_any_size_match_the_fft_form(terms_per_sum):
+    """The tensor stage's accumulator groups (18 terms in ceil(18 / g) groups,
+    from 18 groups of one term to one chain), their running sums in the
+    per-SM slots: the top-4 cells equal the FFT form's up to ties within the
+    tolerance, adjudicated with FP64 energies, on 256 rotations at 64^3."""
+    from proddl2_gb300 import synth
+    n, k = 64, 4
+    pair = synth.make_pair(1500, 400, 256, seed=47)
+    res = {}
+    for mode, kw in (("fft", {}), ("tensor", {"tc_terms_per_sum": terms_per_sum})):
+        with _scan(n, O.TERMS_SHAPE_ACE, pair.ace, k=k, mode=mode, batch=256, **kw) as s:
+            s.set_receptor(pair.receptor.xyz, pair.receptor.ace_type)
+            s.set_ligand(pair.ligand.xyz, pair.ligand.ace_type)
+            assert s.info()["pencil_path"] == mode
+            res[mode] = s.scan(pair.rotations)
+    geom, rg, w = _oracle_setup(n, O.TERMS_SHAPE_ACE, pair.ace, pair.receptor.xyz, pair.receptor.ace_type,
+                                pair.ligand.ace_type)
+    cf, ct = res["fft"].peaks["cell"], res["tensor"].peaks["cell"]
+    differ = np.nonzero(~np.all(cf == ct, axis=(1, 2)))[0]
+    assert len(differ) <= 16, len(differ)
+    for i in differ:
+        cells, _ = O.bin_ligand(geom, pair.rotations[i], pair.ligand.xyz)
+        lists, exact = {}, {}
+        for mode in ("fft", "tensor"):
+            cell, _, score = res[mode].rotation(i)
+            offs = [int((c[0] * n + c[1]) * n + c[2]) for c in cell]
+            lists[mode] = set(offs)
+            for o, c, sc in zip(offs, cell, score):
+                e = O.direct_score(rg, cells, w, c)
+                assert abs(e - sc) <= 1e-9 * max(1.0, abs(e))
+                exact[o] = e
+        best = sorted(exact.items(), key=lambda t: (t[1], t[0]))[:k]
+        last = best[-1][1]
+        tie = REL * max(1.0, abs(last))
+        for mode in ("fft", "tensor"):
+            for o, e in best:
+                if e < last - tie:
+                    assert o in lists[mode], (terms_per_sum, mode, i, o, e, last)
+
+
+def test_tensor_form_at_144_matches_the_fft_form():
+    """The cubic 144 edge runs the tensor stage with two 128-row output tiles
+    (512 TMEM columns): its top-4 cells equal the FFT form's up to ties within
+    the tolerance (FP64-adjudicated) on 128 rotations, and every reported
+    score is the exact energy of its cell."""
+    from proddl2_gb300 import synth
+    n, k = 144, 4
+    pair = synth.make_pair(2500, 600, 128, seed=61)
+    res = {}
+    for mode in ("fft", "tensor"):
+        with _scan(n, O.TERMS_SHAPE_ACE, pair.ace, k=k, mode=mode, batch=128) as s:
+            s.set_receptor(pair.receptor.xyz, pair.receptor.ace_type)
+            s.set_ligand(pair.ligand.xyz, pair.ligand.ace_type)
+            assert s.info()["pencil_path"] == mode
+            res[mode] = s.scan(pair.rotations)
+    geom, rg, w = _oracle_setup(n, O.TERMS_SHAPE_ACE, pair.ace, pair.receptor.xyz, pair.receptor.ace_type,
+                                pair.ligand.ace_type)
+    for i in range(len(pair.rotations)):
+        cells, _ = O.bin_ligand(geom, pair.rotations[i], pair.ligand.xyz)
+        lists, exact = {}, {}
+        for mode in ("fft", "tensor"):
+            cell, _, score = res[mode].rotation(i)
+            offs = [int((c[0] * n + c[1]) * n + c[2]) for c in cell]
+            lists[mode] = set(offs)
+            for o, c, sc in zip(offs, cell, score):
+                e = O.direct_score(rg, cells, w, c)
+                assert abs(e - sc) <= 1e-9 * max(1.0, abs(e))
+                exact[o] = e
+        if lists["fft"] == lists["tensor"]:
+            continue
+        best = sorted(exact.items(), key=lambda t: (t[1], t[0]))[:k]
+        last = best[-1][1]
+        tie = REL * max(1.0, abs(last))
+        for mode in ("fft", "tensor"):
+            for o, e in best:
+                if e < last - tie:
+                    assert o in lists[mode], (mode, i, o, e, last)

@@ -235,7 +235,7 @@ int check_pipeline(fftdock_ctx* ctx) {
     CK(cudaMemcpy(&err, ctx->err_dev, sizeof(int), cudaMemcpyDeviceToHost));
     if (err != 0) {
         cudaMemset(ctx->err_dev, 0, sizeof(int));
-        // bits 1, 2, 4, 16: a bounded wait on a pipeline barrier ran out; 32: a
+        // bits 2, 4, 16: a bounded wait on a pipeline barrier ran out; 32: a
         // CTA found no running-sum slot for its SM (an SM id at or above %nsmid)
         const std::string what = (err & 32) && !(err & 23) ? "tensor pencil stage found no running-sum slot"
                                                            : "tensor pencil stage timed out waiting on a pipeline barrier";

@@ -68,7 +68,9 @@ constexpr uint32_t TC_FCHUNK = 2 * TC_FTILE;      // hi + lo of one window chunk
 constexpr uint64_t TC_WAIT_NS = 2000000000ull;    // 2 s per wait
 constexpr float TC_F_SCALE = 16.0f;               // scale of the ligand sums before the FP16 split
 
-struct TcPair {      // one receptor circulant sample d, as FP16 pairs
+// stored and loaded as one 128-bit shared-memory access (four 32-bit
+// accesses 16 bytes apart would conflict four ways)
+struct __align__(16) TcPair {      // one receptor circulant sample d, as FP16 pairs
     __half2 re_h;    // (Re c, -Im c) hi: multiplies (F_re, F_im) into the real output
     __half2 im_h;    // (Im c,  Re c) hi: into the imaginary output
     __half2 re_l;
@@ -104,6 +106,18 @@ __device__ __forceinline__ float2 ld_shared_f2_const(uint32_t addr) {
     return v;
 }
 __device__ __forceinline__ uint32_t h2u(__half2 h) { return *reinterpret_cast<uint32_t*>(&h); }
+__device__ __forceinline__ __half2 u2h(uint32_t u) { return *reinterpret_cast<__half2*>(&u); }
+// one circulant sample (re_h, im_h, re_l, im_l) as one 128-bit load
+__device__ __forceinline__ TcPair ld_pair(uint32_t addr) {
+    uint32_t a, b, c, d;
+    asm volatile("ld.shared.v4.b32 {%0, %1, %2, %3}, [%4];" : "=r"(a), "=r"(b), "=r"(c), "=r"(d) : "r"(addr));
+    TcPair v;
+    v.re_h = u2h(a);
+    v.im_h = u2h(b);
+    v.re_l = u2h(c);
+    v.im_l = u2h(d);
+    return v;
+}
 
 // Running-sum slot accesses: relaxed at GPU scope, like the atomic adds
 // between them, so that one thread's accesses to a cell stay in program
@@ -264,7 +278,6 @@ __global__ void __launch_bounds__(TC_THREADS, MT == 1 ? 2 : 1) pencil_tc_kernel(
     TcPair* pr = reinterpret_cast<TcPair*>(twr + tw_len);                      // [nx]
     float2* side = reinterpret_cast<float2*>(pr + nx);                         // [128]
     int32_t* tinf = reinterpret_cast<int32_t*>(side + TC_ROT);                 // [2 Ka + 1]
-    __shared__ __align__(8) uint64_t full_bar;
     __shared__ __align__(8) uint64_t empty_bar;
     __shared__ __align__(8) uint64_t done_bar;
     __shared__ uint32_t tmem_base;
@@ -303,7 +316,6 @@ __global__ void __launch_bounds__(TC_THREADS, MT == 1 ? 2 : 1) pencil_tc_kernel(
         tc::tmem_relinquish();
     }
     if (tid == 0) {
-        tc::mbar_init(&full_bar, 256);
         tc::mbar_init(&empty_bar, 1);
         tc::mbar_init(&done_bar, 1);
         tc::fence_barrier_init();
@@ -318,6 +330,7 @@ __global__ void __launch_bounds__(TC_THREADS, MT == 1 ? 2 : 1) pencil_tc_kernel(
     auto starts_group = [&](int k) { return k == 0 || group_of(k) != group_of(k - 1); };
     const uint32_t fb = tc::smem_u32(fbuf);
     const uint32_t ab = tc::smem_u32(abuf);
+    const uint32_t prb = tc::smem_u32(pr);
 
     // MMA issue for term k (thread 0, after the producers' arrivals): 6 MMAs
     // per window chunk into the real and imaginary accumulators, then a
@@ -455,15 +468,21 @@ __global__ void __launch_bounds__(TC_THREADS, MT == 1 ? 2 : 1) pencil_tc_kernel(
         };
         preload(0);
         for (int k = 0; k < Ka; ++k) {
-            // the tensor core has read the previous term's tiles
-            if (k >= 1 && !*(volatile int*)&abort_flag &&
-                !tc::mbar_wait(&empty_bar, (uint32_t)((k - 1) & 1), TC_WAIT_NS)) {
-                atomicOr(err, 2);
-                abort_flag = 1;
+            // the tensor core has read the previous term's tiles: one lane
+            // per warp polls the barrier and the warp follows it, except
+            // before a drain, whose tensor-memory loads every thread orders
+            // after its own wait
+            if (k >= 1) {
+                if ((lane == 0 || starts_group(k)) && !*(volatile int*)&abort_flag &&
+                    !tc::mbar_wait(&empty_bar, (uint32_t)((k - 1) & 1), TC_WAIT_NS)) {
+                    atomicOr(err, 2);
+                    abort_flag = 1;
+                }
+                __syncwarp();
             }
             // a group of terms is complete in TMEM: add it into the output
             // before term k restarts the accumulator (the loads have finished
-            // when this thread arrives on full_bar below)
+            // when this thread reaches the barrier before the MMA issue)
             if (k >= 1 && starts_group(k) && !*(volatile int*)&abort_flag) {
                 tc::fence_after_sync();
                 drain_group(group_of(k - 1) == 0);
@@ -476,7 +495,7 @@ __global__ void __launch_bounds__(TC_THREADS, MT == 1 ? 2 : 1) pencil_tc_kernel(
                 TcPair v;
                 split_h2(cr, -ci, v.re_h, v.re_l);
                 split_h2(ci, cr, v.im_h, v.im_l);
-                pr[tid] = v;
+                st_shared_v4(prb + (uint32_t)tid * 16u, h2u(v.re_h), h2u(v.im_h), h2u(v.re_l), h2u(v.im_l));
             }
             // zero the staging rows (W x 128 float2, the F tile bytes)
             for (uint32_t off = (uint32_t)tid * 16u; off < (uint32_t)W * 1024u; off += 256u * 16u)
@@ -490,7 +509,7 @@ __global__ void __launch_bounds__(TC_THREADS, MT == 1 ? 2 : 1) pencil_tc_kernel(
 #pragma unroll
                 for (int i2 = 0; i2 < 8; ++i2) {
                     const int d = d0 + i2;
-                    v[i2] = pr[d < nx ? d : d - nx];
+                    v[i2] = ld_pair(prb + (uint32_t)(d < nx ? d : d - nx) * 16u);
                 }
                 const uint32_t o0 = tc::kmajor_offset((uint32_t)e, 0, TC_LBO, TC_SBO);
                 const uint32_t o1 = tc::kmajor_offset((uint32_t)e, 8, TC_LBO, TC_SBO);
@@ -548,18 +567,15 @@ __global__ void __launch_bounds__(TC_THREADS, MT == 1 ? 2 : 1) pencil_tc_kernel(
                     st_shared_v4(fc + TC_FTILE + r1, lo[4], lo[5], lo[6], lo[7]);
                 }
             }
-            tc::fence_proxy_async_smem();
-            tc::mbar_arrive(&full_bar);
-            if (tid == 0 && !*(volatile int*)&abort_flag) {
-                if (!tc::mbar_wait(&full_bar, (uint32_t)(k & 1), TC_WAIT_NS)) {
-                    atomicOr(err, 1);
-                    abort_flag = 1;
-                } else {
-                    tc::fence_after_sync();
-                    issue_term(k);
-                }
-            }
+            // the next term's first loads, then the tiles are complete: a
+            // CTA barrier (no polling), after which thread 0 issues the MMAs
             if (k + 1 < Ka) preload(k + 1);
+            tc::fence_proxy_async_smem();
+            asm volatile("bar.sync 1, 256;" ::: "memory");
+            if (tid == 0 && !*(volatile int*)&abort_flag) {
+                tc::fence_after_sync();
+                issue_term(k);
+            }
         }
         // arrives when every MMA issued above has completed
         if (tid == 0) tc::mma_commit(&done_bar);

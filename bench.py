@@ -591,7 +591,8 @@ def run_pairs(args):
     w, n_pairs, n_rot, ace, pairs = pairs_workload(args)
     base = ScanConfig(term_set=w["term_set"], ace_matrix=ace, peaks_per_rot=w["peaks"], rot_batch=w["rot_batch"],
                       device=local)
-    # warm-up: the tuned call fixes the plan (streams, rotations per launch)
+    # warm-up: the tuned call fixes the plan (streams; per grid edge the
+    # rotations per launch and the pencil form)
     t0 = time.perf_counter()
     _, plan = scan_pairs(base, pairs, tune=True)
     tune_call_s = time.perf_counter() - t0
@@ -646,7 +647,8 @@ def run_pairs(args):
         "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded globules, uniform quaternion rotations)",
         "config": {"workload": pairs_desc(w, n_pairs, n_rot, [p.grid_n for p in pairs]),
                    "mode": "exhaustive, all pairs in one CUDA graph",
-                   "plan": {"streams": plan["n_streams"], "rot_batch_by_grid": plan["rot_batch"]},
+                   "plan": {"streams": plan["n_streams"], "rot_batch_by_grid": plan["rot_batch"],
+                            "pencil_form_by_grid": plan["pencil_form"]},
                    "l2": "inputs larger than L2 (per-pair receptor spectra + x-planes rewritten every batch)"},
         "pairs_per_s": n_pairs * world / (ms_per_step / 1000.0),
         "e2e": {"value": rot_total * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,

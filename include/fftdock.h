@@ -425,14 +425,18 @@ typedef struct fftdock_pairs_report {
     double run_ms;                        /* the graph's execution, CUDA events */
     int64_t rotations;                    /* rotations scanned */
     int32_t n_out_of_grid;                /* rotations that left the grid (no peaks) */
+    int32_t pencil_form[FFTDOCK_N_SIZES]; /* pencil-stage form used per edge: FFTDOCK_PENCIL_FFT or
+                                             FFTDOCK_PENCIL_TENSOR (0: edge unused); under AUTO the
+                                             autotuner times both where either can run */
 } fftdock_pairs_report;
 
 /* Scan every pair; FFTDOCK_EOUT_OF_GRID (outputs still written) if any
  * rotation put a ligand atom outside its grid.  Errors are described by
  * fftdock_pairs_last_error() (per calling thread).  With tune == 0, a report
- * whose n_streams > 0 is read as the plan to use (streams and rotations per
- * launch per edge, e.g. from an earlier tuned call); otherwise one stream
- * and cfg->rot_batch. */
+ * whose n_streams > 0 is read as the plan to use (streams, and per edge the
+ * rotations per launch and, under AUTO, the pencil form; e.g. from an
+ * earlier tuned call); otherwise one stream, cfg->rot_batch and the AUTO
+ * rule. */
 int fftdock_scan_pairs(const fftdock_config* cfg, int32_t n_pairs, const fftdock_pair* pairs, int32_t tune,
                        fftdock_pairs_report* report);
 const char* fftdock_pairs_last_error(void);

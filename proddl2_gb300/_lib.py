@@ -126,6 +126,7 @@ class PairsReport(C.Structure):
         ("run_ms", C.c_double),
         ("rotations", C.c_int64),
         ("n_out_of_grid", C.c_int32),
+        ("pencil_form", C.c_int32 * N_SIZES),
     ]
 
 

@@ -9,10 +9,12 @@
 // into one CUDA graph over several streams ("queues", pairs spread by
 // longest-processing-time first), launched once.  Grid edges up to 128 run
 // the tensor form of the pencil stage under the same rule as the single-pair
-// contexts (AUTO: term sets of at least kTcMinTerms terms).  The autotuner picks the
-// rotations per launch for each grid size (timed probe scans of the pair's own
-// kernels) and the number of queues (timed probe graphs over a subset of the
-// pairs).  The FFT radix plan of each grid size is fixed at compile time.
+// contexts (AUTO: term sets of at least kTcMinTerms terms).  The autotuner picks,
+// for each grid size, the pencil-stage form (tensor-core GEMM or radix FFT,
+// where AUTO could run either) and the rotations per launch (timed probe
+// scans of the pair's own kernels), and the number of queues (timed probe
+// graphs over a subset of the pairs).  Each form's radix plan is fixed at
+// compile time.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -69,7 +71,8 @@ struct SizeData {
     int batch = 64;
     int max_lig = 1;
     int max_rec = 1;
-    bool tc = false;      // tensor form of the pencil stage
+    bool tc = false;      // tensor form of the pencil stage (the form that runs)
+    bool tc_ok = false;   // the tensor form is available for this edge (the tuner may choose it)
     int max_pad = 16;     // largest padded entry rows per rotation among its pairs
 };
 
@@ -500,7 +503,7 @@ int stage(Run& r, int n_pairs, const fftdock_pair* pairs) {
         SizeData& sd = r.sizes[pairs[i].grid_n];
         st.info_off.push_back(info_all.size());
         st.tpad_off.push_back(tpad_all.size());
-        if (!sd.tc) continue;
+        if (!sd.tc_ok) continue;
         st.tct[i] = fftdock::tc_tables(pairs[i].lig_xyz, lt.data() + st.lig_off[i], pairs[i].n_lig, r.K, sd.N,
                                       r.cfg.grid_step, sd.zero_h);
         if (!st.tct[i].ok) continue;
@@ -537,8 +540,10 @@ int setup_sizes(Run& r, int n_pairs, const fftdock_pair* pairs) {
         sd.ops = fftdock::size_ops(N);
         sd.batch = r.cfg.rot_batch;
         // AUTO keeps the FFT form above 128 (the tensor form's second x tile
-        // is mostly empty there); TENSOR asks for it wherever it is built
-        sd.tc = r.tc && sd.ops->has_tc && (r.cfg.pencil_mode == FFTDOCK_PENCIL_TENSOR || N <= fftdock::kTcRot);
+        // is mostly empty there); TENSOR asks for it wherever it is built;
+        // the autotuner times both forms wherever AUTO could run either
+        sd.tc_ok = r.tc && sd.ops->has_tc;
+        sd.tc = sd.tc_ok && (r.cfg.pencil_mode == FFTDOCK_PENCIL_TENSOR || N <= fftdock::kTcRot);
         // the tensor form takes rotations in groups of 128
         if (sd.tc) sd.batch = (sd.batch + fftdock::kTcRot - 1) / fftdock::kTcRot * fftdock::kTcRot;
         std::vector<float2> t32(N);
@@ -556,8 +561,12 @@ int setup_sizes(Run& r, int n_pairs, const fftdock_pair* pairs) {
     return FFTDOCK_OK;
 }
 
-// rotations per launch for one grid size: time the scan of the first pair
-// of that size over a probe of rotations for each candidate
+// plan of one grid size: the pencil-stage form (the tensor-core GEMM form or
+// the radix-FFT form, both where AUTO could run either) and the rotations
+// per launch.  For each candidate, the first pair of that size is timed
+// with its set-up alone and with a probe of rotations; the candidate with
+// the least set-up + (the pair's rotations x the probe's time per rotation)
+// wins.
 int tune_batch(Run& r, const fftdock_pair* pairs, int n_pairs, int N, cudaStream_t s, cudaEvent_t a, cudaEvent_t b) {
     static const int cand[] = {32, 64, 128, 256};
     SizeData& sd = r.sizes.at(N);
@@ -568,33 +577,47 @@ int tune_batch(Run& r, const fftdock_pair* pairs, int n_pairs, int N, cudaStream
     const int n_probe = std::min(pairs[pi].n_rot, 512);
     double best = 1e300;
     int best_b = sd.batch;
+    bool best_tc = sd.tc;
+    // the forms to time: both when AUTO could run either and the pair has
+    // the tensor form's tables, else the one set up
+    const bool both = sd.tc_ok && r.cfg.pencil_mode == FFTDOCK_PENCIL_AUTO && r.st.tct[pi].ok;
+    for (int f = 0; f < (both ? 2 : 1); ++f)
     for (int B : cand) {
+        const bool tc = both ? f == 0 : sd.tc;
         // rotations per launch: multiples of 128 for the tensor form
-        if (B > 1024 || (sd.tc && B % fftdock::kTcRot)) continue;
+        if (B > 1024 || (tc && B % fftdock::kTcRot)) continue;
         Work w;
         SizeData tmp = sd;
+        tmp.tc = tc;
         int rc = alloc_work(r, w, tmp, B);
         if (rc) {
             w.release();
             return rc;
         }
-        // warm-up (also sets kernel attributes before any capture), then time
+        // warm-up (also sets kernel attributes before any capture), then
+        // time the set-up alone and with the probe's rotations
         cudaError_t e = enqueue_pair(r, pairs[pi], pi, w, tmp, B, 0, n_probe, s);
-        float ms = 0.f;
-        if (e == cudaSuccess) e = cudaEventRecord(a, s);
-        if (e == cudaSuccess) e = enqueue_pair(r, pairs[pi], pi, w, tmp, B, 0, n_probe, s);
-        if (e == cudaSuccess) e = cudaEventRecord(b, s);
-        if (e == cudaSuccess) e = cudaEventSynchronize(b);
-        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+        float ms = 0.f, ms0 = 0.f;
+        auto timed = [&](int n, float* out) {
+            if (e == cudaSuccess) e = cudaEventRecord(a, s);
+            if (e == cudaSuccess) e = enqueue_pair(r, pairs[pi], pi, w, tmp, B, 0, n, s);
+            if (e == cudaSuccess) e = cudaEventRecord(b, s);
+            if (e == cudaSuccess) e = cudaEventSynchronize(b);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(out, a, b);
+        };
+        timed(n_probe, &ms);
+        timed(0, &ms0);
         w.release();
         if (e != cudaSuccess) return fail(FFTDOCK_ECUDA, std::string("batch probe: ") + cudaGetErrorString(e));
-        const double per = ms / n_probe;
+        const double per = ms0 + (double)pairs[pi].n_rot * std::max(0.0, (double)(ms - ms0)) / n_probe;
         if (per < best * 0.98) {
             best = per;
             best_b = B;
+            best_tc = tc;
         }
     }
     sd.batch = best_b;
+    sd.tc = best_tc;
     return FFTDOCK_OK;
 }
 
@@ -730,6 +753,11 @@ int fftdock_scan_pairs(const fftdock_config* cfg, int32_t n_pairs, const fftdock
             for (auto& kv : r.sizes) {
                 const int b = report->rot_batch[size_slot(kv.first)];
                 if (b >= 1 && b <= 1024) kv.second.batch = b;
+                // the planned pencil form, where AUTO could run either
+                const int form = report->pencil_form[size_slot(kv.first)];
+                if (kv.second.tc_ok && r.cfg.pencil_mode == FFTDOCK_PENCIL_AUTO &&
+                    (form == FFTDOCK_PENCIL_FFT || form == FFTDOCK_PENCIL_TENSOR))
+                    kv.second.tc = form == FFTDOCK_PENCIL_TENSOR;
                 if (kv.second.tc)
                     kv.second.batch = (kv.second.batch + fftdock::kTcRot - 1) / fftdock::kTcRot * fftdock::kTcRot;
             }
@@ -767,7 +795,10 @@ int fftdock_scan_pairs(const fftdock_config* cfg, int32_t n_pairs, const fftdock
         if (rc2) return rc2;
         rep.run_ms = ms;
         rep.n_streams = queues;
-        for (auto& kv : r.sizes) rep.rot_batch[size_slot(kv.first)] = kv.second.batch;
+        for (auto& kv : r.sizes) {
+            rep.rot_batch[size_slot(kv.first)] = kv.second.batch;
+            rep.pencil_form[size_slot(kv.first)] = kv.second.tc ? FFTDOCK_PENCIL_TENSOR : FFTDOCK_PENCIL_FFT;
+        }
         // outputs
         size_t no = 0;
         for (int i = 0; i < n_pairs; ++i) no += pairs[i].n_rot;

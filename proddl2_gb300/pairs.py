@@ -45,8 +45,9 @@ def pair_grid(rec_xyz, lig_xyz, step=1.2, margin=6.0):
 
 
 def scan_pairs(config: ScanConfig, pairs, tune=True, raise_out_of_grid=True, plan=None):
-    """``plan``: the report of an earlier call, reused (streams, rotations
-    per launch per grid edge) when ``tune`` is false."""
+    """``plan``: the report of an earlier call, reused (streams, and per grid
+    edge the rotations per launch and the pencil-stage form) when ``tune`` is
+    false."""
     lib = _lib.lib()
     cfg, ace = native_config(config)
     P = config.peaks_per_rot
@@ -72,13 +73,17 @@ def scan_pairs(config: ScanConfig, pairs, tune=True, raise_out_of_grid=True, pla
     rep = _lib.PairsReport()
     if plan is not None and not tune:
         rep.n_streams = int(plan["n_streams"])
+        forms = {"fft": _lib.FFTDOCK_PENCIL_FFT, "tensor": _lib.FFTDOCK_PENCIL_TENSOR}
         for k in range(_lib.N_SIZES):
             rep.rot_batch[k] = int(plan["rot_batch"].get(int(_lib.BUILT_SIZES[k]), 0))
+            rep.pencil_form[k] = forms.get(plan.get("pencil_form", {}).get(int(_lib.BUILT_SIZES[k])), 0)
     rc = lib.fftdock_scan_pairs(C.byref(cfg), len(pairs), descs, 1 if tune else 0, C.byref(rep))
     msg = lib.fftdock_pairs_last_error().decode() if rc else ""
     report = {
         "n_streams": rep.n_streams,
         "rot_batch": {int(rep.grid_sizes[k]): int(rep.rot_batch[k]) for k in range(_lib.N_SIZES) if rep.rot_batch[k]},
+        "pencil_form": {int(rep.grid_sizes[k]): ("tensor" if rep.pencil_form[k] == _lib.FFTDOCK_PENCIL_TENSOR else "fft")
+                        for k in range(_lib.N_SIZES) if rep.rot_batch[k]},
         "setup_ms": rep.setup_ms, "tune_ms": rep.tune_ms, "capture_ms": rep.capture_ms, "run_ms": rep.run_ms,
         "rotations": int(rep.rotations), "n_out_of_grid": int(rep.n_out_of_grid),
         "grid_n": [int(descs[i].grid_n) for i in range(len(pairs))],

@@ -49,9 +49,14 @@ def test_pair_graph_matches_single_pair_scans(tune):
     if tune:
         assert rep["n_streams"] in (1, 2, 4)
         assert set(rep["rot_batch"].values()) <= {32, 64, 128, 256}
+        # the tuner chose a pencil form per edge (a tensor-form edge takes
+        # rotations in multiples of 128)
+        assert set(rep["pencil_form"]) == set(rep["rot_batch"])
+        assert all(rep["rot_batch"][n] % 128 == 0 for n, f in rep["pencil_form"].items() if f == "tensor")
         # the tuned plan, reused without tuning, gives the same peaks
         res2, rep2 = scan_pairs(base, pairs, tune=False, plan=rep)
         assert rep2["n_streams"] == rep["n_streams"] and rep2["rot_batch"] == rep["rot_batch"]
+        assert rep2["pencil_form"] == rep["pencil_form"]
         for a, b in zip(res, res2):
             assert np.array_equal(a.n_peaks, b.n_peaks) and np.array_equal(a.peaks, b.peaks)
     else:
@@ -60,8 +65,11 @@ def test_pair_graph_matches_single_pair_scans(tune):
         assert rep["n_streams"] == 1
         assert all((b >= 128 and b % 128 == 0) if int(n) <= 128 else b == 48
                    for n, b in rep["rot_batch"].items()), rep["rot_batch"]
+        assert all(f == ("tensor" if n <= 128 else "fft") for n, f in rep["pencil_form"].items())
+    # each pair against a single-pair scan with the pencil form its edge ran
     for p, r, n in zip(pairs, res, rep["grid_n"]):
-        cfg = ScanConfig(grid_n=n, term_set="shape_ace", ace_matrix=ace, peaks_per_rot=4)
+        cfg = ScanConfig(grid_n=n, term_set="shape_ace", ace_matrix=ace, peaks_per_rot=4,
+                         pencil_mode=rep["pencil_form"][n])
         with FFTScan(cfg) as s:
             s.set_receptor(p.rec_xyz, p.rec_type)
             s.set_ligand(p.lig_xyz, p.lig_type)

@@ -69,38 +69,6 @@ __device__ __forceinline__ bool better(float a, int ia, float b, int ib) {
     return a < b || (a == b && ia < ib);
 }
 
-struct WarpTopK {
-    float lv;
-    int li;
-    float tv;  // current KC-th value (threshold)
-    int ti;
-    __device__ __forceinline__ void init() { lv = INFINITY; li = 0x7fffffff; tv = INFINITY; ti = 0x7fffffff; }
-    // offer one candidate per lane (all lanes of the warp must call)
-    __device__ __forceinline__ void offer(float v, int idx, int lane) {
-        // v <= tv is necessary for (v, idx) < (tv, ti); the exact test runs
-        // only on the rare candidates
-        if (__ballot_sync(0xffffffffu, v <= tv) == 0u) return;
-        unsigned mask = __ballot_sync(0xffffffffu, better(v, idx, tv, ti));
-        while (mask) {
-            const int src = __ffs(mask) - 1;
-            const float cv = __shfl_sync(0xffffffffu, v, src);
-            const int ci = __shfl_sync(0xffffffffu, idx, src);
-            const unsigned below = __ballot_sync(0xffffffffu, lane < KC && better(lv, li, cv, ci));
-            const int pos = __popc(below);
-            const float upv = __shfl_up_sync(0xffffffffu, lv, 1);
-            const int upi = __shfl_up_sync(0xffffffffu, li, 1);
-            if (pos < KC) {
-                if (lane == pos) { lv = cv; li = ci; }
-                else if (lane > pos && lane < KC) { lv = upv; li = upi; }
-            }
-            tv = __shfl_sync(0xffffffffu, lv, KC - 1);
-            ti = __shfl_sync(0xffffffffu, li, KC - 1);
-            mask &= ~(1u << src);
-            mask &= __ballot_sync(0xffffffffu, better(v, idx, tv, ti));
-        }
-    }
-};
-
 // Compare-exchange with lane ^ j under better(): this lane keeps the better
 // of the two pairs when keep_min, else the other one.
 __device__ __forceinline__ void warp_cmp_swap(float& v, int& i, int j, bool keep_min) {
@@ -127,6 +95,58 @@ __device__ __forceinline__ void warp_merge32(float& v, int& i, int lane) {
 #pragma unroll
     for (int j = 16; j > 0; j >>= 1) warp_cmp_swap(v, i, j, (lane & j) == 0);
 }
+
+struct WarpTopK {
+    float lv;
+    int li;
+    float tv;  // current KC-th value (threshold)
+    int ti;
+    __device__ __forceinline__ void init() { lv = INFINITY; li = 0x7fffffff; tv = INFINITY; ti = 0x7fffffff; }
+    // offer one candidate per lane (all lanes of the warp must call)
+    __device__ __forceinline__ void offer(float v, int idx, int lane) {
+        // v <= tv is necessary for (v, idx) < (tv, ti); the exact test runs
+        // only on the rare candidates
+        if (__ballot_sync(0xffffffffu, v <= tv) == 0u) return;
+        unsigned mask = __ballot_sync(0xffffffffu, better(v, idx, tv, ti));
+        if (__popc(mask) > 6) {
+            // many at once: sort the qualifying offers and merge them with
+            // the list (lanes < KC ascending, the best KC offers descending
+            // above them: one bitonic sequence) -- the same KC best by
+            // (value, index) as one insertion each
+            static_assert(KC == 16, "the batch merge takes lists of 16");
+            float sv = (mask >> lane) & 1u ? v : INFINITY;
+            int si = (mask >> lane) & 1u ? idx : 0x7fffffff;
+            warp_sort32(sv, si, lane);
+            const float rv = __shfl_sync(0xffffffffu, sv, 31 - lane);
+            const int ri = __shfl_sync(0xffffffffu, si, 31 - lane);
+            float mv = lane < KC ? lv : rv;
+            int mi = lane < KC ? li : ri;
+            warp_merge32(mv, mi, lane);
+            lv = mv;
+            li = mi;
+            tv = __shfl_sync(0xffffffffu, lv, KC - 1);
+            ti = __shfl_sync(0xffffffffu, li, KC - 1);
+            return;
+        }
+        while (mask) {
+            const int src = __ffs(mask) - 1;
+            const float cv = __shfl_sync(0xffffffffu, v, src);
+            const int ci = __shfl_sync(0xffffffffu, idx, src);
+            const unsigned below = __ballot_sync(0xffffffffu, lane < KC && better(lv, li, cv, ci));
+            const int pos = __popc(below);
+            const float upv = __shfl_up_sync(0xffffffffu, lv, 1);
+            const int upi = __shfl_up_sync(0xffffffffu, li, 1);
+            if (pos < KC) {
+                if (lane == pos) { lv = cv; li = ci; }
+                else if (lane > pos && lane < KC) { lv = upv; li = upi; }
+            }
+            tv = __shfl_sync(0xffffffffu, lv, KC - 1);
+            ti = __shfl_sync(0xffffffffu, li, KC - 1);
+            mask &= ~(1u << src);
+            mask &= __ballot_sync(0xffffffffu, better(v, idx, tv, ti));
+        }
+    }
+};
 
 // Merge per-warp lists staged in shared memory (nw lists of KC) into warp 0's
 // list; the caller syncs before and reads lanes < KC of warp 0 after.

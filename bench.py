@@ -494,9 +494,10 @@ def run_ours(args):
                     "flops_basis": "executed split-FP16 MMA work: N^2(N/2+1) pencils x K x W/8 chunks x 6 MMAs "
                                    "of 128x128x16 per 128-rotation group (W = %d); useful = executed / 3 (the "
                                    "hi*hi, hi*lo, lo*hi products emulate one FP32 product)" % info["window_w"],
-                    "limiter": "shared-memory bandwidth and instruction issue: the MMAs' operand reads "
-                               "(8 KB per 128x128x16 MMA) and the producers' loads and stores share the "
-                               "SM's 128 B per clock",
+                    "limiter": "the CUDA-core producers of the MMA operands (entry walk, tile conversion "
+                               "and build: shared-memory and LSU traffic and its latency); the tensor pipe "
+                               "is busy about a third of the time, and halving the MMAs' shared-memory "
+                               "operand reads did not change the kernel's time",
                     "kernel_share": share, "hbm": hbm}
     else:
         roofline = {"bound": "hbm", "achieved": pencil_gbs, "peak": peak_gbs, "unit": "GB/s",

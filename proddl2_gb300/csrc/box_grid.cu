@@ -502,6 +502,8 @@ __global__ void __launch_bounds__(32 * PW, 2) box_plane_kernel(const float2* __r
                                  : g2 + ((size_t)q * nx + x) * pp;
         const int step = QUAD ? 4 : 1;
         const int tot = ny * hz;
+        // i / hz as a multiply-high by ceil(2^32 / hz): exact for i < 2^32 / hz
+        const unsigned mhz = 0xffffffffu / (unsigned)hz + 1u;
         for (int i0 = tid; i0 < tot; i0 += 8 * blockDim.x) {
             float2 v[8];
 #pragma unroll
@@ -512,7 +514,10 @@ __global__ void __launch_bounds__(32 * PW, 2) box_plane_kernel(const float2* __r
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
                 const int i = i0 + k * blockDim.x;
-                if (i < tot) plane[(i / hz) * pitch + i % hz] = v[k];
+                if (i < tot) {
+                    const int yq = (int)__umulhi((unsigned)i, mhz);
+                    plane[yq * pitch + (i - yq * hz)] = v[k];
+                }
             }
         }
     }

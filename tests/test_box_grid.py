@@ -175,10 +175,10 @@ def test_box_grid_out_of_grid_and_batches():
 
 
 def test_box_grid_forms_agree_over_many_sizes():
-    """Both pencil-stage forms on 14 box grids drawn from the sizes findBestSize
+    """Both pencil-stage forms on 15 box grids drawn from the sizes findBestSize
     can return (x from 10 to 128, including odd and 11/13-factor lengths, and
-    two with x above 128, where the tensor stage takes two 128-row output
-    tiles), 48 rotations each: wherever the top-4 lists differ, every cell of either list
+    three with x above 128, up to 250, where the tensor stage takes two
+    128-row output tiles), 48 rotations each: wherever the top-4 lists differ, every cell of either list
     is adjudicated with its FP64 direct-space energy (each form must hold
     every cell of the union's best four below the 4th by more than the tie
     tolerance), and every reported score is the exact energy of its cell."""
@@ -187,11 +187,11 @@ def test_box_grid_forms_agree_over_many_sizes():
     rng = np.random.Generator(np.random.PCG64(2024))
     sizes = [n for n in range(10, 129) if supported_dims((n, n, n))]
     checked = 0
-    for case in range(14):
+    for case in range(15):
         dims = tuple(int(v) for v in rng.choice([n for n in sizes if n >= 40], size=3))
         dims = (int(rng.choice(sizes[:8])) if case < 2 else dims[0],) + dims[1:]
         if case >= 12:
-            dims = ((150, 52, 44), (176, 60, 65))[case - 12]
+            dims = ((150, 52, 44), (176, 60, 65), (250, 40, 42))[case - 12]
         # molecules that fit the smallest axis (the first two grids are thin)
         pair = synth.make_pair(600, 120, 48, seed=300 + case) if case >= 2 else \
             synth.make_pair(150, 12, 48, seed=300 + case)
@@ -230,4 +230,4 @@ def test_box_grid_forms_agree_over_many_sizes():
                     if e < last - tie:
                         assert o in lists[mode], (dims, mode, i, o, e, last)
             checked += 1
-    assert checked >= 14 * 24, checked
+    assert checked >= 15 * 24, checked

@@ -68,7 +68,7 @@ template <typename T2, int SIGN> __device__ __forceinline__ T2 tw_at(const T2* t
 // and writes its R-point DFT to dst[(j / Ns) Ns R + j mod Ns + k Ns].  The
 // twiddle index (j mod Ns) r n/(Ns R) stays below n; the R-th roots of unity
 // are held in registers for the whole stage, radices 2 and 4 need none.
-template <typename T2, int SIGN, int R>
+template <typename T2, int SIGN, int R, int LS = 32>
 __device__ __forceinline__ void stockham_stage(const T2* src, T2* dst, const T2* tw, int n, int ns, int lane) {
     using S = decltype(T2::x);
     const int nb = n / R;
@@ -79,7 +79,7 @@ __device__ __forceinline__ void stockham_stage(const T2* src, T2* dst, const T2*
     T2 root[R];
 #pragma unroll
     for (int m = 1; m < R; ++m) root[m] = tw_at<T2, SIGN>(tw, m * nb);
-    for (int j = lane; j < nb; j += 32) {
+    for (int j = lane; j < nb; j += LS) {
         T2 v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) v[r] = src[j + r * nb];
@@ -146,7 +146,9 @@ __device__ __forceinline__ void stockham_stage(const T2* src, T2* dst, const T2*
 // n points; returns the buffer that holds the result.  SIGN -1: forward
 // e^{-2 pi i jk/n}; +1: inverse.  Ends with __syncwarp.  MAXR < 11: the plan
 // has no factor 11 or 13 (those stages are not compiled: fewer registers).
-template <typename T2, int SIGN, int MAXR = 13>
+// LS = 16: two lines per warp, lane = the thread's index within its half
+// (each half passes its own line's buffers).
+template <typename T2, int SIGN, int MAXR = 13, int LS = 32>
 __device__ T2* warp_fft(T2* a, T2* b, const T2* tw, const BoxPlan& pl, int lane) {
     T2* src = a;
     T2* dst = b;
@@ -155,15 +157,15 @@ __device__ T2* warp_fft(T2* a, T2* b, const T2* tw, const BoxPlan& pl, int lane)
     for (int s = 0; s < pl.nf; ++s) {
         const int R = pl.f[s];
         switch (R) {
-            case 4: stockham_stage<T2, SIGN, 4>(src, dst, tw, pl.n, ns, lane); break;
-            case 2: stockham_stage<T2, SIGN, 2>(src, dst, tw, pl.n, ns, lane); break;
-            case 3: stockham_stage<T2, SIGN, 3>(src, dst, tw, pl.n, ns, lane); break;
-            case 5: stockham_stage<T2, SIGN, 5>(src, dst, tw, pl.n, ns, lane); break;
-            case 7: stockham_stage<T2, SIGN, 7>(src, dst, tw, pl.n, ns, lane); break;
+            case 4: stockham_stage<T2, SIGN, 4, LS>(src, dst, tw, pl.n, ns, lane); break;
+            case 2: stockham_stage<T2, SIGN, 2, LS>(src, dst, tw, pl.n, ns, lane); break;
+            case 3: stockham_stage<T2, SIGN, 3, LS>(src, dst, tw, pl.n, ns, lane); break;
+            case 5: stockham_stage<T2, SIGN, 5, LS>(src, dst, tw, pl.n, ns, lane); break;
+            case 7: stockham_stage<T2, SIGN, 7, LS>(src, dst, tw, pl.n, ns, lane); break;
             default:
                 if constexpr (MAXR >= 11) {
-                    if (R == 11) stockham_stage<T2, SIGN, 11>(src, dst, tw, pl.n, ns, lane);
-                    else stockham_stage<T2, SIGN, 13>(src, dst, tw, pl.n, ns, lane);
+                    if (R == 11) stockham_stage<T2, SIGN, 11, LS>(src, dst, tw, pl.n, ns, lane);
+                    else stockham_stage<T2, SIGN, 13, LS>(src, dst, tw, pl.n, ns, lane);
                 }
                 break;
         }
@@ -532,30 +534,43 @@ __global__ void __launch_bounds__(32 * PW, 2) box_plane_kernel(const float2* __r
         for (int y = lane; y < ny; y += 32) plane[y * pitch + kz] = o[y];
     }
     __syncthreads();
-    // rows y: real inverse transform along kz, and the warp's top KC
+    // rows y: real inverse transform along kz, and the warp's top KC.  Even
+    // nz: two rows per warp, 16 lanes each (the short nz/2-point transforms
+    // leave most of a warp idle in their larger-radix stages); each half's
+    // line sits at offset line * ns of the warp's two buffers.
     WarpTopK tk;
     tk.init();
     const size_t row0 = (size_t)x * ny;
-    for (int y = w; y < ny && ns > 0; y += PW) {
+    const int line = lane >> 4, li = lane & 15;
+    for (int y0 = 2 * w; y0 < ny && ns > 0; y0 += 2 * PW) {
         __syncwarp();
+        const int y = y0 + line < ny ? y0 + line : y0;  // an odd last row: both halves take it
         const float2* row = plane + (size_t)y * pitch;
-        for (int k = lane; k < ns; k += 32) {
+        float2* al = a + line * ns;
+        for (int k = li; k < ns; k += 16) {
             const float2 X = row[k], Xm = row[ns - k];
             const float2 A = make_float2(X.x + Xm.x, X.y - Xm.y);
             const float2 B = make_float2(X.x - Xm.x, X.y + Xm.y);
             const float2 wk = twz[k];  // conj(w^k)
             const float2 cb = make_float2(B.x * wk.x + B.y * wk.y, B.y * wk.x - B.x * wk.y);  // B w^k
-            a[k] = make_float2(A.x - cb.y, A.y + cb.x);
+            al[k] = make_float2(A.x - cb.y, A.y + cb.x);
         }
-        const float2* o = warp_fft<float2, +1, MAXR>(a, b, twh, plh, lane);
-        for (int z0 = 0; z0 < nz; z0 += 32) {
-            const int z = z0 + lane;
-            const bool ok = z < nz;
-            const float2 c = o[ok ? z >> 1 : 0];
-            const float v = ok ? ((z & 1) ? c.y : c.x) : INFINITY;
-            const int idx = ok ? (int)((row0 + y) * nz + z) : 0x7fffffff;
-            if (DBG && ok) dbg[(size_t)q * nx * ny * nz + (size_t)idx] = v;
-            tk.offer(v, idx, lane);
+        const float2* o = warp_fft<float2, +1, MAXR, 16>(al, b + line * ns, twh, plh, li);
+        // the same plan in both halves: both results in a, or both in b
+        const float2* res = (o == al ? a : b);
+#pragma unroll 1
+        for (int hl = 0; hl < 2 && y0 + hl < ny; ++hl) {
+            const float2* ol = res + hl * ns;
+            const int yy = y0 + hl;
+            for (int z0 = 0; z0 < nz; z0 += 32) {
+                const int z = z0 + lane;
+                const bool ok = z < nz;
+                const float2 c = ol[ok ? z >> 1 : 0];
+                const float v = ok ? ((z & 1) ? c.y : c.x) : INFINITY;
+                const int idx = ok ? (int)((row0 + yy) * nz + z) : 0x7fffffff;
+                if (DBG && ok) dbg[(size_t)q * nx * ny * nz + (size_t)idx] = v;
+                tk.offer(v, idx, lane);
+            }
         }
     }
     for (int y = w; y < ny && ns == 0; y += PW) {

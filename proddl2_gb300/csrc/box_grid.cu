@@ -38,7 +38,7 @@ constexpr int kBoxWarps = 8;  // lines (pencils, columns, rows) per CTA
 
 // radices in Stockham stage order; false if n has another prime factor
 bool factor_plan(int n, BoxPlan& pl) {
-    static const int radices[] = {4, 2, 3, 5, 7, 11, 13};
+    static const int radices[] = {4, 6, 2, 3, 5, 7, 11, 13};
     pl.n = n;
     pl.nf = 0;
     int m = n;
@@ -95,6 +95,37 @@ __device__ __forceinline__ void stockham_stage(const T2* src, T2* dst, const T2*
             o1.x -= v[1].x; o1.y -= v[1].y;
             out[0] = o0;
             out[ns] = o1;
+        } else if constexpr (R == 6) {
+            // two 3-point DFTs of the even and odd inputs, the odd ones
+            // turned by W6^k (W6 = e^(SIGN i pi / 3)): out_k = e_k + W6^k o_k,
+            // out_(k+3) = e_k - W6^k o_k
+            constexpr S c3 = (S)0.86602540378443864676;  // sin(pi / 3)
+            constexpr S sg = SIGN < 0 ? (S)-1 : (S)1;
+            T2 e3[3], o3[3];
+#pragma unroll
+            for (int t = 0; t < 2; ++t) {
+                const T2 x0 = v[t], x1 = v[t + 2], x2 = v[t + 4];
+                T2 sm, df, u;
+                sm.x = x1.x + x2.x; sm.y = x1.y + x2.y;
+                df.x = sg * c3 * (x1.x - x2.x); df.y = sg * c3 * (x1.y - x2.y);
+                u.x = x0.x - (S)0.5 * sm.x; u.y = x0.y - (S)0.5 * sm.y;
+                T2* y = t == 0 ? e3 : o3;
+                y[0].x = x0.x + sm.x; y[0].y = x0.y + sm.y;
+                // y1 = u + i df, y2 = u - i df
+                y[1].x = u.x - df.y; y[1].y = u.y + df.x;
+                y[2].x = u.x + df.y; y[2].y = u.y - df.x;
+            }
+            // W6 = (1/2, sg c3), W6^2 = (-1/2, sg c3)
+            T2 t1, t2;
+            t1.x = (S)0.5 * o3[1].x - sg * c3 * o3[1].y; t1.y = (S)0.5 * o3[1].y + sg * c3 * o3[1].x;
+            t2.x = (S)-0.5 * o3[2].x - sg * c3 * o3[2].y; t2.y = (S)-0.5 * o3[2].y + sg * c3 * o3[2].x;
+            T2 o;
+            o.x = e3[0].x + o3[0].x; o.y = e3[0].y + o3[0].y; out[0] = o;
+            o.x = e3[1].x + t1.x; o.y = e3[1].y + t1.y; out[ns] = o;
+            o.x = e3[2].x + t2.x; o.y = e3[2].y + t2.y; out[2 * ns] = o;
+            o.x = e3[0].x - o3[0].x; o.y = e3[0].y - o3[0].y; out[3 * ns] = o;
+            o.x = e3[1].x - t1.x; o.y = e3[1].y - t1.y; out[4 * ns] = o;
+            o.x = e3[2].x - t2.x; o.y = e3[2].y - t2.y; out[5 * ns] = o;
         } else if constexpr (R == 4) {
             // W4 = e^(SIGN i pi / 2): out1 = (v0 - v2) + W4 (v1 - v3), out3 = (v0 - v2) - W4 (v1 - v3)
             T2 a, b, c, d, e;
@@ -158,6 +189,7 @@ __device__ T2* warp_fft(T2* a, T2* b, const T2* tw, const BoxPlan& pl, int lane)
         const int R = pl.f[s];
         switch (R) {
             case 4: stockham_stage<T2, SIGN, 4, LS>(src, dst, tw, pl.n, ns, lane); break;
+            case 6: stockham_stage<T2, SIGN, 6, LS>(src, dst, tw, pl.n, ns, lane); break;
             case 2: stockham_stage<T2, SIGN, 2, LS>(src, dst, tw, pl.n, ns, lane); break;
             case 3: stockham_stage<T2, SIGN, 3, LS>(src, dst, tw, pl.n, ns, lane); break;
             case 5: stockham_stage<T2, SIGN, 5, LS>(src, dst, tw, pl.n, ns, lane); break;

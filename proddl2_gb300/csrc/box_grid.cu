@@ -38,7 +38,7 @@ constexpr int kBoxWarps = 8;  // lines (pencils, columns, rows) per CTA
 
 // radices in Stockham stage order; false if n has another prime factor
 bool factor_plan(int n, BoxPlan& pl) {
-    static const int radices[] = {4, 6, 2, 3, 5, 7, 11, 13};
+    static const int radices[] = {4, 6, 2, 9, 3, 5, 7, 11, 13};
     pl.n = n;
     pl.nf = 0;
     int m = n;
@@ -77,6 +77,8 @@ __device__ __forceinline__ void stockham_stage(const T2* src, T2* dst, const T2*
     // j < 2^32 / ns^2 (here j < 256 and ns <= 256)
     const unsigned magic = ns > 1 ? 0xffffffffu / (unsigned)ns + 1u : 0u;
     T2 root[R];
+    root[0].x = 1;  // W^0 (a composite odd radix pairs some q k = 0 mod R)
+    root[0].y = 0;
 #pragma unroll
     for (int m = 1; m < R; ++m) root[m] = tw_at<T2, SIGN>(tw, m * nb);
     for (int j = lane; j < nb; j += LS) {
@@ -194,6 +196,7 @@ __device__ T2* warp_fft(T2* a, T2* b, const T2* tw, const BoxPlan& pl, int lane)
             case 3: stockham_stage<T2, SIGN, 3, LS>(src, dst, tw, pl.n, ns, lane); break;
             case 5: stockham_stage<T2, SIGN, 5, LS>(src, dst, tw, pl.n, ns, lane); break;
             case 7: stockham_stage<T2, SIGN, 7, LS>(src, dst, tw, pl.n, ns, lane); break;
+            case 9: stockham_stage<T2, SIGN, 9, LS>(src, dst, tw, pl.n, ns, lane); break;
             default:
                 if constexpr (MAXR >= 11) {
                     if (R == 11) stockham_stage<T2, SIGN, 11, LS>(src, dst, tw, pl.n, ns, lane);
@@ -501,7 +504,7 @@ __global__ void __launch_bounds__(32 * kBoxWarps, 2) box_pencil_kernel(
 // spectrum, Y[k] = A + i w^k B with A = X[k] + conj(X[nz/2 - k]),
 // B = X[k] - conj(X[nz/2 - k]), w = e^{2 pi i / nz}: output m holds the real
 // values of z = 2m and 2m + 1.
-// PW warps; MAXR: the largest radix of the y and z plans (7: none of 11, 13)
+// PW warps; MAXR: the largest radix of the y and z plans (9: none of 11, 13)
 template <bool DBG, bool QUAD, int PW, int MAXR>
 __global__ void __launch_bounds__(32 * PW, 2) box_plane_kernel(const float2* __restrict__ g2,
                                                                   const float2* __restrict__ twy_g,
@@ -782,7 +785,7 @@ cudaError_t box_prep(const BatchArgs& a, cudaStream_t s) {
 
 bool big_radix(const BoxPlan& pl) {
     for (int i = 0; i < pl.nf; ++i)
-        if (pl.f[i] > 7) return true;
+        if (pl.f[i] > 9) return true;
     return false;
 }
 
@@ -807,7 +810,7 @@ cudaError_t box_plane(dim3 grid, size_t sm, const float2* src, const float2* twy
     if (pz.n % 2 == 0 && !factor_plan(pz.n / 2, ph)) ph = BoxPlan{};
     if (big_radix(py) || big_radix(pz))
         return box_plane_launch<DBG, QUAD, 8, 13>(grid, sm, src, twy, twz, py, pz, ph, nx, a, dbg, nxp, s);
-    return box_plane_launch<DBG, QUAD, 16, 7>(grid, sm, src, twy, twz, py, pz, ph, nx, a, dbg, nxp, s);
+    return box_plane_launch<DBG, QUAD, 16, 9>(grid, sm, src, twy, twz, py, pz, ph, nx, a, dbg, nxp, s);
 }
 
 cudaError_t box_middle(const BatchArgs& a, cudaStream_t s) {
@@ -899,7 +902,7 @@ cudaError_t box_load_kernels(int) {
     cudaFuncAttributes fa;
     cudaError_t e = cudaFuncGetAttributes(&fa, (const void*)box_prep_kernel);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)box_pencil_kernel<false>);
-    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)box_plane_kernel<false, false, 16, 7>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)box_plane_kernel<false, false, 16, 9>);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)box_finalize_kernel);
     return e;
 }

@@ -9,8 +9,9 @@
 // (inverse y transform, real inverse z transform, exact per-plane top 16),
 // finalize (merge, FP64 direct-space rescoring, sort, maxValCorr, unwrap per
 // axis) -- with every transform length a runtime value: one warp per line
-// runs a mixed-radix Stockham FFT (radices 4, 2, 3, 5, 7, 11, 13) out of
-// shared memory with a twiddle table per axis.  The receptor's transforms
+// runs a mixed-radix Stockham FFT (radices 4, 6, 2, 9, 3, 5, 7, 11, 13 in
+// that order of preference) out of shared memory with a twiddle table per
+// axis (even-length plane rows: two lines per warp, 16 lanes each).  The receptor's transforms
 // run the same line FFT in FP64.
 //
 // Layout (Hz = Nz/2 + 1, pencil p = ky Hz + kz, PP = Ny Hz rounded up to 32):
@@ -67,7 +68,9 @@ template <typename T2, int SIGN> __device__ __forceinline__ T2 tw_at(const T2* t
 // butterfly j reads src[j + r n/R], applies the twiddles W^(j mod Ns) r n/(Ns R),
 // and writes its R-point DFT to dst[(j / Ns) Ns R + j mod Ns + k Ns].  The
 // twiddle index (j mod Ns) r n/(Ns R) stays below n; the R-th roots of unity
-// are held in registers for the whole stage, radices 2 and 4 need none.
+// are held in registers for the whole stage, radices 2 and 4 need none, 6
+// is two 3-point DFTs joined by W6 twiddles.  LS lanes share one line
+// (butterflies j = lane, lane + LS, ..).
 template <typename T2, int SIGN, int R, int LS = 32>
 __device__ __forceinline__ void stockham_stage(const T2* src, T2* dst, const T2* tw, int n, int ns, int lane) {
     using S = decltype(T2::x);

@@ -44,7 +44,7 @@
 // that the 32 lanes' lookups never share a bank.
 //
 // CTA (256 threads): eight producer warps (two threads per rotation); thread
-// 0 also issues each term's MMAs once every producer has arrived.  The
+// 0 also issues each term's MMAs after a barrier of all producers.  The
 // producers fill the next term's tiles only after the tensor core has read
 // the current ones, so two CTAs share an SM (shared memory and 2 x 256 TMEM
 // columns permitting) and overlap each other's MMAs and production; 16 warps

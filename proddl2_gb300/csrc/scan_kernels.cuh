@@ -444,8 +444,7 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     constexpr int PCAND = 256;                            // candidate list capacity
     __shared__ float cand_sv[PCAND];
     __shared__ int cand_si[PCAND];
-    __shared__ float bound_v;
-    __shared__ int bound_i, n_cand;
+    __shared__ int n_cand;
 
     const int x = blockIdx.x;
     const int q = blockIdx.y;
@@ -687,6 +686,24 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     // Every warp sorts its threads' minima; warp 0 merges the warps' 16 best
     // (the KC best of all minima are among them).
     static_assert(KC == 16, "the bitonic selection keeps 16 of 32 lanes");
+    // lists 0 .. nl-1 of KC (lv_s, li_s, ascending) merged pairwise over
+    // log2(nl) levels into list 0 (warp w merges list w + step into list w);
+    // every thread calls it
+    auto tree_merge = [&](int nl) {
+        for (int step = 1; step < nl; step <<= 1) {
+            __syncthreads();
+            if ((w & (2 * step - 1)) == 0 && w + step < nl) {
+                float sv = l < KC ? lv_s[w * KC + l] : lv_s[(w + step) * KC + 31 - l];
+                int si = l < KC ? li_s[w * KC + l] : li_s[(w + step) * KC + 31 - l];
+                warp_merge32(sv, si, l);
+                if (l < KC) {
+                    lv_s[w * KC + l] = sv;
+                    li_s[w * KC + l] = si;
+                }
+            }
+        }
+        __syncthreads();
+    };
     {
         float sv = bmin_v;
         int si = bmin_i;
@@ -697,25 +714,9 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
         }
     }
     if (tid == 0) n_cand = 0;
-    __syncthreads();
-    if (w == 0) {
-        float sv = l < KC ? lv_s[l] : INFINITY;
-        int si = l < KC ? li_s[l] : 0x7fffffff;
-        for (int g = 1; g < G; ++g) {
-            if (l >= KC) {  // warp g's list, reversed
-                sv = lv_s[g * KC + 31 - l];
-                si = li_s[g * KC + 31 - l];
-            }
-            warp_merge32(sv, si, l);
-        }
-        if (l == KC - 1) {
-            bound_v = sv;
-            bound_i = si;
-        }
-    }
-    __syncthreads();
-    const float tv = bound_v;
-    const int ti = bound_i;
+    tree_merge(G);
+    const float tv = lv_s[KC - 1];
+    const int ti = li_s[KC - 1];
     auto offer = [&](float v, int i) {
         if (!better(tv, ti, v, i)) {
             const int at = atomicAdd(&n_cand, 1);
@@ -760,33 +761,37 @@ __global__ void __launch_bounds__(32 * SizeTraits<N>::G) plane_kernel(
     __syncthreads();
     const int nc = n_cand;
     if (nc <= PCAND) {
-        if (w == 0) {
-            // running best KC in lanes < KC; each chunk of 32 is sorted and its
-            // best KC merged in
-            float sv = INFINITY;
-            int si = 0x7fffffff;
-            for (int base = 0; base < nc; base += 32) {
-                const int e = base + l;
-                float cv = e < nc ? cand_sv[e] : INFINITY;
-                int ci = e < nc ? cand_si[e] : 0x7fffffff;
-                warp_sort32(cv, ci, l);
+        // warp w sorts chunks w, w + G, .. of 32 candidates and keeps their
+        // best KC in list w; the lists are then tree-merged
+        const int nchunk = (nc + 31) >> 5;
+        float sv = INFINITY;
+        int si = 0x7fffffff;
+        for (int c = w; c < nchunk; c += G) {
+            const int e = 32 * c + l;
+            float cv = e < nc ? cand_sv[e] : INFINITY;
+            int ci = e < nc ? cand_si[e] : 0x7fffffff;
+            warp_sort32(cv, ci, l);
+            if (c == w) {
+                sv = cv;
+                si = ci;
+            } else {
                 const float rv = __shfl_sync(0xffffffffu, cv, 31 - l);
                 const int ri = __shfl_sync(0xffffffffu, ci, 31 - l);
-                if (base == 0) {
-                    sv = cv;
-                    si = ci;
-                } else {
-                    if (l >= KC) {
-                        sv = rv;
-                        si = ri;
-                    }
-                    warp_merge32(sv, si, l);
+                if (l >= KC) {
+                    sv = rv;
+                    si = ri;
                 }
+                warp_merge32(sv, si, l);
             }
-            if (l < KC) {
-                cand_v[((size_t)q * N + x) * KC + l] = sv;
-                cand_i[((size_t)q * N + x) * KC + l] = si;
-            }
+        }
+        if (l < KC) {
+            lv_s[w * KC + l] = sv;
+            li_s[w * KC + l] = si;
+        }
+        tree_merge(nchunk < G ? nchunk : G);
+        if (w == 0 && l < KC) {
+            cand_v[((size_t)q * N + x) * KC + l] = lv_s[l];
+            cand_i[((size_t)q * N + x) * KC + l] = li_s[l];
         }
         return;
     }

@@ -636,13 +636,24 @@ __global__ void __launch_bounds__(32 * PW, 2) box_plane_kernel(const float2* __r
         lv_s[w * KC + lane] = tk.lv;
         li_s[w * KC + lane] = tk.li;
     }
-    __syncthreads();
-    if (w == 0) {
-        merge_lists(lv_s, li_s, PW * KC, tk, lane);
-        if (lane < KC) {
-            cand_v[((size_t)q * nx + x) * KC + lane] = tk.lv;
-            cand_i[((size_t)q * nx + x) * KC + lane] = tk.li;
+    // the warps' sorted lists merged pairwise over log2(PW) levels into
+    // list 0 (warp w merges list w + step into list w)
+    for (int step = 1; step < PW; step <<= 1) {
+        __syncthreads();
+        if ((w & (2 * step - 1)) == 0 && w + step < PW) {
+            float sv = lane < KC ? lv_s[w * KC + lane] : lv_s[(w + step) * KC + 31 - lane];
+            int si = lane < KC ? li_s[w * KC + lane] : li_s[(w + step) * KC + 31 - lane];
+            warp_merge32(sv, si, lane);
+            if (lane < KC) {
+                lv_s[w * KC + lane] = sv;
+                li_s[w * KC + lane] = si;
+            }
         }
+    }
+    __syncthreads();
+    if (w == 0 && lane < KC) {
+        cand_v[((size_t)q * nx + x) * KC + lane] = lv_s[lane];
+        cand_i[((size_t)q * nx + x) * KC + lane] = li_s[lane];
     }
 }
 
